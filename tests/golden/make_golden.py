@@ -1,0 +1,347 @@
+"""Generate the golden vectors in this folder by running the HCIPy reference itself.
+
+The reference is pure Python; it imports here through the small stand-ins in
+``refshim/`` (numexpr -> numpy eval, numba -> identity decorators, xxhash ->
+blake2b, a minimal YAML reader, numpy-only array_api_compat, and import stubs
+for the plotting / FITS packages that the diffraction path never calls).
+
+Usage (from the repository root, with the reference checked out read-only)::
+
+    python tests/golden/make_golden.py /root/reference
+
+Every case is small and seeded; the outputs are written as compressed ``.npz``
+files next to this script.  Nothing in the test suite runs this script: the
+tests only read the ``.npz`` files, so they run where the reference is absent.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def import_reference(path):
+    sys.dont_write_bytecode = True
+    sys.path.insert(0, os.path.join(HERE, 'refshim'))
+    sys.path.insert(0, path)
+    import packaging.version  # noqa: F401  (the reference's io module needs it pre-imported)
+    import hcipy
+    return hcipy
+
+
+def grid_record(prefix, grid):
+    """Store the regular-grid description (delta, dims, zero) of a grid."""
+    return {
+        prefix + '_delta': np.asarray(grid.delta, dtype=np.float64),
+        prefix + '_dims': np.asarray(grid.dims, dtype=np.int64),
+        prefix + '_zero': np.asarray(grid.zero, dtype=np.float64),
+        prefix + '_weights': np.asarray(np.broadcast_to(grid.weights, (grid.size,)), dtype=np.float64),
+    }
+
+
+def separated_record(prefix, grid):
+    x, y = grid.separated_coords
+    return {prefix + '_x': np.asarray(x, np.float64), prefix + '_y': np.asarray(y, np.float64)}
+
+
+def random_field(rng, grid, aperture=None):
+    e = rng.standard_normal(grid.size) + 1j * rng.standard_normal(grid.size)
+    if aperture is not None:
+        e = e * aperture
+    return e
+
+
+def make_mft_cases(hp, out):
+    rng = np.random.default_rng(11)
+    cases = [
+        # (pupil dims, pupil diameter, focal q, num_airy, scale)
+        ((64, 64), 1.0, 4, 8, 2 * np.pi),
+        ((48, 40), 1.3, 3, (5, 7), 2 * np.pi / 1.7),
+        ((33, 31), 0.8, 2.5, 6.3, 2 * np.pi * 1.1),
+    ]
+    for i, (dims, diam, q, num_airy, scale) in enumerate(cases):
+        pupil = hp.make_pupil_grid(dims, diam)
+        focal = hp.make_focal_grid(q, num_airy).scaled(scale).shifted([0.013 * i, -0.02 * i])
+        e = random_field(rng, pupil)
+        f = random_field(rng, focal)
+        mft = hp.MatrixFourierTransform(pupil, focal)
+        rec = {}
+        rec.update(separated_record('in', pupil))
+        rec.update(separated_record('out', focal))
+        rec.update(grid_record('ingrid', pupil))
+        rec.update(grid_record('outgrid', focal))
+        rec['E'] = e
+        rec['F'] = f
+        rec['fwd_c128'] = np.asarray(mft.forward(hp.Field(e, pupil)))
+        rec['bwd_c128'] = np.asarray(mft.backward(hp.Field(f, focal)))
+        rec['fwd_c64'] = np.asarray(mft.forward(hp.Field(e.astype(np.complex64), pupil)))
+        rec['bwd_c64'] = np.asarray(mft.backward(hp.Field(f.astype(np.complex64), focal)))
+        out['mft_%d' % i] = rec
+
+    # One-dimensional MFT.
+    g1 = hp.make_uniform_grid(37, 1.0)
+    f1 = hp.make_uniform_grid(29, 40.0, center=0.3)
+    mft1 = hp.MatrixFourierTransform(g1, f1)
+    e = random_field(rng, g1)
+    f = random_field(rng, f1)
+    out['mft_1d'] = {
+        'in_x': np.asarray(g1.x, np.float64), 'out_x': np.asarray(f1.x, np.float64),
+        'w_in': np.float64(g1.weights), 'w_out': np.float64(f1.weights),
+        'E': e, 'F': f,
+        'fwd_c128': np.asarray(mft1.forward(hp.Field(e, g1))),
+        'bwd_c128': np.asarray(mft1.backward(hp.Field(f, f1))),
+    }
+
+
+def make_fraunhofer_cfg1(hp, out):
+    """The 256^2 circular pupil with a 0.1 rad RMS Zernike 2-21 phase to a 128^2 focal grid."""
+    pupil = hp.make_pupil_grid(256, 1)
+    aperture = hp.make_circular_aperture(1)(pupil)
+    zb = hp.make_zernike_basis(20, 1, pupil, starting_mode=2)
+    rng = np.random.default_rng(0)
+    c = rng.standard_normal(20)
+    phase = zb.linear_combination(c)
+    inside = aperture > 0
+    phase = phase * (0.1 / np.std(phase[inside]))
+    e = aperture * np.exp(1j * phase)
+    focal = hp.make_focal_grid(q=4, num_airy=16)
+    prop = hp.FraunhoferPropagator(pupil, focal)
+    wf = hp.Wavefront(hp.Field(e, pupil), 1)
+    res128 = prop.forward(wf).electric_field
+    wf64 = hp.Wavefront(hp.Field(e.astype(np.complex64), pupil), 1)
+    res64 = prop.forward(wf64).electric_field
+    back = prop.backward(hp.Wavefront(res128, 1)).electric_field
+    out['fraunhofer_cfg1'] = {
+        'E': e.astype(np.complex128), 'focal_c128': np.asarray(res128), 'focal_c64': np.asarray(res64),
+        'back_c128': np.asarray(back),
+        **grid_record('pupil', pupil), **grid_record('focal', focal),
+    }
+
+
+def make_fft_cases(hp, out):
+    rng = np.random.default_rng(22)
+    cases = [
+        ((32, 32), 1.0, 2, 1, 0),
+        ((15, 17), 0.7, 3, 0.75, (0.5, -1.2)),
+        ((16, 12), 2.0, 1.5, 0.8, 0.3),
+        ((20, 20), 1.0, 1, 1, 0),
+    ]
+    for i, (dims, diam, q, fov, shift) in enumerate(cases):
+        pupil = hp.make_pupil_grid(dims, diam)
+        fft = hp.FastFourierTransform(pupil, q=q, fov=fov, shift=shift)
+        fft2 = hp.FastFourierTransform(pupil, q=q, fov=fov, shift=shift, emulate_fftshifts=False)
+        e = random_field(rng, pupil)
+        f = random_field(rng, fft.output_grid)
+        out['fft_%d' % i] = {
+            'q': np.float64(q), 'fov': np.float64(fov), 'shift': np.broadcast_to(np.asarray(shift, np.float64), (2,)).copy(),
+            'E': e, 'F': f,
+            'fwd_c128': np.asarray(fft.forward(hp.Field(e, pupil))),
+            'bwd_c128': np.asarray(fft.backward(hp.Field(f, fft.output_grid))),
+            'fwd_exact_c128': np.asarray(fft2.forward(hp.Field(e, pupil))),
+            'fwd_c64': np.asarray(fft.forward(hp.Field(e.astype(np.complex64), pupil))),
+            **grid_record('ingrid', pupil), **grid_record('outgrid', fft.output_grid),
+            **grid_record('internal', fft.internal_grid),
+        }
+
+
+def make_czt_cases(hp, out):
+    rng = np.random.default_rng(33)
+    recs = {}
+    for i, (n, m) in enumerate([(37, 23), (64, 100), (101, 7), (250, 250)]):
+        x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        w = np.exp(1j * rng.uniform(0, 2 * np.pi))
+        a = np.exp(1j * rng.uniform(0, 2 * np.pi))
+        czt = hp.ChirpZTransform(n, m, w, a)
+        recs['x_%d' % i] = x
+        recs['w_%d' % i] = np.complex128(w)
+        recs['a_%d' % i] = np.complex128(a)
+        recs['y_%d' % i] = np.asarray(czt(x))
+        recs['y64_%d' % i] = np.asarray(czt(x.astype(np.complex64)))
+        recs['n_%d' % i] = np.int64(n)
+        recs['m_%d' % i] = np.int64(m)
+    # A batched call along the last axis.
+    xb = rng.standard_normal((3, 5, 19)) + 1j * rng.standard_normal((3, 5, 19))
+    czt = hp.ChirpZTransform(19, 31, np.exp(-0.2j), np.exp(0.7j))
+    recs['xb'] = xb
+    recs['yb'] = np.asarray(czt(xb))
+    out['czt'] = recs
+
+    # ZoomFFT on a small grid.
+    pupil = hp.make_pupil_grid((24, 20), 1)
+    focal = hp.make_focal_grid(3, (5, 4)).scaled(2 * np.pi).shifted([0.1, -0.2])
+    zfft = hp.ZoomFastFourierTransform(pupil, focal)
+    e = random_field(rng, pupil)
+    f = random_field(rng, focal)
+    out['zoomfft'] = {
+        'E': e, 'F': f,
+        'fwd_c128': np.asarray(zfft.forward(hp.Field(e, pupil))),
+        'bwd_c128': np.asarray(zfft.backward(hp.Field(f, focal))),
+        **grid_record('ingrid', pupil), **grid_record('outgrid', focal),
+    }
+
+
+def make_asp_cases(hp, out):
+    rng = np.random.default_rng(44)
+    recs = {}
+    # The native transfer-function branch (large distance relative to sampling is the other branch).
+    for i, (n, diam, wl, d) in enumerate([(64, 8.0, 1.6e-6, 0.5), (48, 8.0, 1.6e-6, 5.0), (40, 2e-3, 500e-9, 0.05)]):
+        pupil = hp.make_pupil_grid(n, diam)
+        aperture = hp.make_circular_aperture(diam * 0.9)(pupil)
+        e = aperture * np.exp(1j * rng.standard_normal(pupil.size) * 0.3)
+        asp = hp.AngularSpectrumPropagator(pupil, d)
+        wf = hp.Wavefront(hp.Field(e, pupil), wl)
+        fwd = asp.forward(wf).electric_field
+        bwd = asp.backward(hp.Wavefront(fwd, wl)).electric_field
+        fwd64 = asp.forward(hp.Wavefront(hp.Field(e.astype(np.complex64), pupil), wl)).electric_field
+        # Which branch did the reference take?
+        L_max = np.max(np.asarray(pupil.dims) * pupil.delta)
+        impulse_branch = bool(np.any(pupil.delta < wl * abs(d) / L_max))
+        recs['case_%d' % i] = {
+            'n': np.int64(n), 'diam': np.float64(diam), 'wavelength': np.float64(wl), 'distance': np.float64(d),
+            'E': e, 'fwd_c128': np.asarray(fwd), 'bwd_c128': np.asarray(bwd), 'fwd_c64': np.asarray(fwd64),
+            'impulse_branch': np.bool_(impulse_branch),
+        }
+    out.update({'asp_%d' % i: r for i, r in enumerate(recs.values())})
+
+    # FourierFilter with a generic scalar transfer function, q=2.
+    g = hp.make_pupil_grid((30, 26), 1.0)
+    def tf(fg):
+        return hp.Field(np.exp(-0.01 * (fg.x**2 + 2 * fg.y**2)) * np.exp(0.3j * fg.x), fg)
+    ff = hp.FourierFilter(g, tf, q=2)
+    e = random_field(rng, g)
+    internal = ff.internal_grid
+    out['fourier_filter'] = {
+        'E': e, 'fwd_c128': np.asarray(ff.forward(hp.Field(e, g))), 'bwd_c128': np.asarray(ff.backward(hp.Field(e, g))),
+        'tf': np.asarray(tf(internal)),
+        **grid_record('ingrid', g), **grid_record('internal', internal),
+    }
+
+
+def make_lyot_case(hp, out):
+    """A 128^2 pupil Lyot chain: focal-plane mask radius 4 lambda/D on a q=8 num_airy=8 grid."""
+    pupil = hp.make_pupil_grid(128, 1)
+    aperture = hp.make_circular_aperture(1)(pupil)
+    zb = hp.make_zernike_basis(30, 1, pupil, starting_mode=2)
+    rng = np.random.default_rng(3)
+    c = rng.standard_normal(30)
+    phase = zb.linear_combination(c)
+    phase *= 2 * np.pi * 1e-2 / np.std(phase[aperture > 0])
+    e = aperture * np.exp(1j * phase)
+    fpm_grid = hp.make_focal_grid(8, 8)
+    fpm = 1 - hp.make_circular_aperture(8)(fpm_grid)
+    stop = hp.make_circular_aperture(0.9)(pupil)
+    lyot = hp.LyotCoronagraph(pupil, fpm, stop)
+    focal = hp.make_focal_grid(4, 16)
+    prop = hp.FraunhoferPropagator(pupil, focal)
+    wf = hp.Wavefront(hp.Field(e, pupil), 1)
+    lyot_plane = lyot.forward(wf).electric_field
+    img = prop.forward(hp.Wavefront(lyot_plane, 1)).electric_field
+    ref_img = prop.forward(hp.Wavefront(hp.Field(aperture.astype(complex), pupil), 1)).power
+    wf64 = hp.Wavefront(hp.Field(e.astype(np.complex64), pupil), 1)
+    lyot64 = lyot.forward(wf64).electric_field
+    out['lyot'] = {
+        'E': e, 'aperture': np.asarray(aperture), 'fpm': np.asarray(fpm), 'stop': np.asarray(stop),
+        'lyot_c128': np.asarray(lyot_plane), 'lyot_c64': np.asarray(lyot64), 'image_c128': np.asarray(img),
+        'ref_peak': np.float64(np.max(ref_img)),
+        **grid_record('pupil', pupil), **grid_record('fpm', fpm_grid), **grid_record('focal', focal),
+    }
+
+
+def make_subpixel_cases(hp, out):
+    from hcipy._math import subpixel_shift as sp
+    rng = np.random.default_rng(55)
+    img = rng.standard_normal((40, 50))
+    recs = {'img': img}
+    shifts = [(0.3, -0.2), (-0.5, 0.5), (0.0, 0.11), (-0.37, 0.0)]
+    for i, (dy, dx) in enumerate(shifts):
+        recs['dy_%d' % i] = np.float64(dy)
+        recs['dx_%d' % i] = np.float64(dx)
+        recs['out_%d' % i] = sp.subpixel_shift(img, dy, dx)
+        recs['wy_%d' % i] = sp._quintic_weights(dy)
+        recs['wx_%d' % i] = sp._quintic_weights(dx)
+    out['subpixel'] = recs
+
+
+def make_atmosphere_case(hp, out):
+    """InfiniteAtmosphericLayer on a 24^2 grid: matrices, stencils and an extrusion replay."""
+    import copy
+    pupil = hp.make_pupil_grid(24, 1.0)
+    cn2 = hp.Cn_squared_from_fried_parameter(0.2, 500e-9)
+    layer = hp.InfiniteAtmosphericLayer(pupil, cn2, L0=25, velocity=(3.0, 0.0), use_interpolation=True, seed=5)
+    rec = {
+        'A_vertical': layer.A_vertical, 'B_vertical': layer.B_vertical,
+        'A_horizontal': layer.A_horizontal, 'B_horizontal': layer.B_horizontal,
+        'stencil_bottom_idx': layer.stencil_bottom_idx.astype(np.int64),
+        'stencil_left_idx': layer.stencil_left_idx.astype(np.int64),
+        'screen0': np.asarray(layer._achromatic_screen), 'cn2': np.float64(cn2),
+        'cov_vertical': layer.cov_matrix_vertical,
+    }
+    # Replay: record the noise of each extrusion by drawing from a copy of the generator.
+    noises = []
+    screens = []
+    kinds = []
+    dts = [0.011, 0.013, 0.004]
+    t = 0.0
+    for dt in dts:
+        rng_copy = copy.deepcopy(layer.rng)
+        old = np.round(layer.center / pupil.delta).astype('int')
+        new_center = layer.center + layer.velocity * dt
+        new = np.round(new_center / pupil.delta).astype('int')
+        nsteps = int(abs(new[0] - old[0]))
+        noise = [rng_copy.normal(0, np.sqrt(cn2), size=layer.B_horizontal.shape[1]) for _ in range(nsteps)]
+        t += dt
+        layer.t = t
+        noises.append(np.array(noise).reshape((nsteps, layer.B_horizontal.shape[1])))
+        screens.append(np.asarray(layer._achromatic_screen))
+        kinds.append(np.asarray(layer.phase_for(1.0)))
+    for i in range(len(dts)):
+        rec['noise_%d' % i] = noises[i]
+        rec['screen_%d' % i] = screens[i]
+        rec['shifted_%d' % i] = kinds[i]
+        rec['dt_%d' % i] = np.float64(dts[i])
+    rec['velocity'] = np.asarray(layer.velocity, dtype=np.float64)
+    rec.update(grid_record('pupil', pupil))
+    out['atmosphere'] = rec
+
+
+def make_dm_case(hp, out):
+    pupil = hp.make_pupil_grid(64, 1)
+    inf = hp.make_gaussian_influence_functions(pupil, 8, 1 / 8, crosstalk=0.15)
+    dm = hp.DeformableMirror(inf)
+    rng = np.random.default_rng(66)
+    dm.actuators = rng.standard_normal(dm.num_actuators) * 1e-3
+    e = hp.make_circular_aperture(1)(pupil).astype(complex)
+    wf = hp.Wavefront(hp.Field(e, pupil), 1.0)
+    out['dm'] = {
+        'influence': np.asarray(inf.transformation_matrix.toarray() if hasattr(inf.transformation_matrix, 'toarray') else inf.transformation_matrix),
+        'actuators': dm.actuators.copy(), 'surface': np.asarray(dm.surface),
+        'E': e, 'fwd_c128': np.asarray(dm.forward(wf).electric_field),
+        **grid_record('pupil', pupil),
+    }
+
+
+def save(out):
+    for name, rec in out.items():
+        np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
+        print('wrote', name, sum(np.asarray(v).nbytes for v in rec.values()), 'bytes')
+
+
+def main():
+    ref_path = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+    hp = import_reference(ref_path)
+    out = {}
+    make_mft_cases(hp, out)
+    make_fraunhofer_cfg1(hp, out)
+    make_fft_cases(hp, out)
+    make_czt_cases(hp, out)
+    make_asp_cases(hp, out)
+    make_lyot_case(hp, out)
+    make_subpixel_cases(hp, out)
+    make_atmosphere_case(hp, out)
+    make_dm_case(hp, out)
+    save(out)
+
+
+if __name__ == '__main__':
+    main()
