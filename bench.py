@@ -1,0 +1,384 @@
+#!/usr/bin/env python
+"""Benchmark of the HCIPy diffraction hot path on GB300: the Lyot-coronagraph precision workload.
+
+Workload (one "propagation" = one step): a 2048^2 circular pupil with seeded
+Zernike 2-100 aberrations at 1 nm RMS, MFT to a 512^2 focal-plane-mask grid
+(q=8, num_airy=32), occulter of radius 4 lambda/D, Babinet subtraction, Lyot
+stop 0.9 D, final MFT to a 512^2 focal grid: three 2048^2 <-> 512^2 matrix
+Fourier transforms (8,053,063,680 complex MACs = 64.42 GFLOP per propagation).
+
+Prints one JSON line (rank 0).  ``--impl ours`` (default) times the CUDA path:
+``value`` with inputs resident in HBM and L2 flushed between steps (a 256 MiB
+write outside the per-step CUDA events); ``e2e`` through the public API with
+the pupil field copied from pinned host memory and the final image copied
+back inside the timed region.  ``--impl reference`` times the reference
+algorithm's CPU port (oracle.optics.LyotChain, matrices precomputed as in the
+reference's default configuration) on all host cores.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'MFT propagations/s & adjoint grad steps/s at ≤1e-11 contrast err vs FP64'
+UNIT = 'propagations/s'
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=200)
+    p.add_argument('--warmup', type=int, default=10)
+    p.add_argument('--impl', choices=['ours', 'reference'], default='ours')
+    p.add_argument('--precision', choices=['fp32', 'split'], default='fp32')
+    p.add_argument('--pupil', type=int, default=2048)
+    p.add_argument('--no-cpu-baseline', action='store_true')
+    p.add_argument('--cpu-seconds', type=float, default=10.0)
+    return p.parse_args()
+
+
+def workload(args):
+    from hcipy_gb300 import workloads
+    return workloads.lyot_workload(pupil_n=args.pupil)
+
+
+def flops_per_propagation(w):
+    from oracle.fourier import mft_cmacs
+    nx, ny = (int(d) for d in w['pupil'].dims)
+    nu, nv = (int(d) for d in w['fpm_grid'].dims)
+    fu, fv = (int(d) for d in w['focal'].dims)
+    cmacs = 2 * mft_cmacs(nx, ny, nu, nv) + mft_cmacs(nx, ny, fu, fv)
+    return cmacs, 8 * cmacs
+
+
+def oracle_grid(g):
+    from oracle.grids import RegularGrid
+    return RegularGrid(g.delta, g.dims, g.zero)
+
+
+# ---------------------------------------------------------------------------
+# Clock sampling (nvidia-smi during the timed region)
+# ---------------------------------------------------------------------------
+
+class ClockSampler(object):
+    FIELDS = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+              'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+              'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, bus_id=None):
+        self.bus_id = bus_id
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        cmd = ['nvidia-smi', '--query-gpu=' + self.FIELDS, '--format=csv,noheader,nounits', '-lms', '100']
+        if self.bus_id:
+            cmd[1:1] = ['-i', self.bus_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(',')]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(('hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap'),
+                                 parts[4:8]):
+                if val.lower().startswith('active'):
+                    reasons.add(name)
+        if not sm:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': [], 'samples': 0}
+        return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': max(smax), 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+def bus_id_of(dev):
+    import torch
+    try:
+        p = torch.cuda.get_device_properties(dev)
+        return '%08x:%02x:%02x.0' % (p.pci_domain_id, p.pci_bus_id, p.pci_device_id)
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the reference algorithm's port
+# ---------------------------------------------------------------------------
+
+def cpu_port_time(w, dtype, seconds, min_iters=1):
+    """Propagations/s of oracle.optics.LyotChain on the host cores, over a bounded sample."""
+    from oracle import optics
+    chain = optics.LyotChain(oracle_grid(w['pupil']), oracle_grid(w['fpm_grid']), oracle_grid(w['focal']),
+                             w['fpm'], w['stop'], dtype=dtype)
+    e = w['E'].astype(dtype)
+    chain(e)  # warm caches / BLAS threads
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        chain(e)
+        n += 1
+        if n >= min_iters and time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return n / dt, n, dt
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------
+# Reference arm
+# ---------------------------------------------------------------------------
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    w = workload(args)
+    from oracle import optics
+    chain = optics.LyotChain(oracle_grid(w['pupil']), oracle_grid(w['fpm_grid']), oracle_grid(w['focal']),
+                             w['fpm'], w['stop'], dtype=np.complex64)
+    e = w['E'].astype(np.complex64)
+    for _ in range(args.warmup):
+        chain(e)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        chain(e)
+    dt = time.perf_counter() - t0
+    value = args.steps / dt
+    cores = host_cores()
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': args.gpus,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * dt / args.steps,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'fp32', 'data': 'synthetic',
+        'config': {'workload': 'lyot-coronagraph 2048^2 pupil -> 512^2 FPM grid -> 512^2 image (3 MFTs)',
+                   'pupil': args.pupil, 'fpm_grid': 512, 'image': 512, 'batch': 1, 'field_dtype': 'complex64'},
+        'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+                         'sample': '%d propagations (the full workload) after %d warm-up, numpy/OpenBLAS cgemm '
+                                   'with matrices precomputed' % (args.steps, args.warmup)},
+        'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# Our arm
+# ---------------------------------------------------------------------------
+
+def dark_hole_error(img, ref_img, focal, aperture_peak):
+    from hcipy_gb300 import workloads
+    mask = workloads.dark_hole_mask(focal)
+    ni = np.abs(img.astype(np.complex128))**2 / aperture_peak
+    ni_ref = np.abs(ref_img)**2 / aperture_peak
+    d = np.abs(ni - ni_ref)[mask]
+    return float(d.max()), float(d.mean()), float(ni_ref[mask].mean())
+
+
+def run_ours(args, rank, world, dist):
+    import torch
+    import hcipy_gb300 as hg
+
+    dev = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
+    torch.cuda.set_device(dev)
+    w = workload(args)
+    pupil, fpm_grid, focal = w['pupil'], w['fpm_grid'], w['focal']
+    cmacs, flops = flops_per_propagation(w)
+
+    lyot = hg.LyotCoronagraph(pupil, hg.Field(w['fpm'], fpm_grid), hg.Field(w['stop'], pupil),
+                              precision=args.precision)
+    prop = hg.FraunhoferPropagator(pupil, focal, precision=args.precision)
+    e_dev = torch.from_numpy(w['E'].astype(np.complex64)).to(dev)
+    stream = torch.cuda.current_stream()
+
+    def step(e):
+        wf = hg.Wavefront(hg.Field(e, pupil), 1.0)
+        return prop.forward(lyot.forward(wf)).electric_field.data
+
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    for _ in range(max(args.warmup, 3)):
+        img = step(e_dev)
+    torch.cuda.synchronize()
+
+    # -- device-resident timing: per-step events, L2 flushed between steps outside the events --------
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(bus_id_of(dev))
+    sampler.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = hg.launch_count()
+    wall0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        starts[i].record(stream)
+        img = step(e_dev)
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = hg.launch_count() - launches0
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps / (total_ms * 1e-3)
+    ms_per_step = total_ms / args.steps
+    gpu_launches = launches  # our kernels only (the L2 flush is a torch fill, not counted)
+
+    # -- end to end through the public API with host buffers ------------------------------------------
+    e_host = torch.from_numpy(w['E'].astype(np.complex64)).pin_memory()
+    img_host = torch.empty(focal.size, dtype=torch.complex64).pin_memory()
+    e2e_steps = max(10, min(args.steps, 100))
+    for _ in range(3):
+        img_host.copy_(step(e_host.to(dev, non_blocking=True)), non_blocking=True)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(e2e_steps):
+        e_d = e_host.to(dev, non_blocking=True)
+        img_host.copy_(step(e_d), non_blocking=True)
+    t1.record(stream)
+    t1.synchronize()
+    e2e_ms = t0.elapsed_time(t1)
+    if dist:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * e2e_steps / (e2e_ms * 1e-3)
+
+    if rank != 0:
+        return
+
+    # -- roofline of the dominant kernel (the complex GEMM: all launches of a step) -------------------
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        pass
+    achieved_tflops = flops / (ms_per_step * 1e-3) / 1e12
+    if args.precision == 'split':
+        peak = peaks.get('bf16_tflops', 1900.0)
+        bound, peak_note = 'tensor', 'bf16 dense, %s' % ('of measured' if 'bf16_tflops' in peaks else 'of fallback')
+    else:
+        props = torch.cuda.get_device_properties(dev)
+        max_mhz = (clocks or {}).get('sm_max_mhz') or peaks.get('sm_max_mhz', 2070.0)
+        peak = props.multi_processor_count * 128 * 2 * max_mhz * 1e6 / 1e12
+        bound = 'fp32'
+        peak_note = ('nominal FP32 CUDA-core rate %d SMs x 128 lanes x 2 FLOP x %.0f MHz; '
+                     'MEASURED_PEAKS.json has no FP32 figure' % (props.multi_processor_count, max_mhz))
+    traffic = None
+    tpath = os.path.join(ROOT, 'profiles', 'traffic.json')
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get('lyot2048_%s' % args.precision)
+
+    # -- accuracy against the float64 oracle -----------------------------------------------------------
+    from oracle import optics
+    chain64 = optics.LyotChain(oracle_grid(pupil), oracle_grid(fpm_grid), oracle_grid(focal), w['fpm'], w['stop'])
+    ref_img = chain64(w['E'])
+    peak_img = np.abs(chain64.image(w['aperture'].astype(np.complex128))).max()**2
+    ni_max, ni_mean, ni_level = dark_hole_error(img.cpu().numpy(), ref_img, focal, peak_img)
+
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        v, n, dt = cpu_port_time(w, np.complex64, args.cpu_seconds)
+        cpu = {'value': v, 'unit': UNIT, 'cores': host_cores(), 'kind': 'port',
+               'sample': '%d propagations of the same workload in %.1f s (numpy/OpenBLAS cgemm, complex64, '
+                         'matrices precomputed)' % (n, dt)}
+
+    line = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'fp32' if args.precision == 'fp32' else 'bf16-split/fp32-acc',
+        'data': 'synthetic (seeded Zernike 2-100 aberrations, 1 nm RMS)',
+        'config': {'workload': 'lyot-coronagraph 2048^2 pupil -> 512^2 FPM grid -> 512^2 image (3 MFTs)',
+                   'pupil': args.pupil, 'fpm_grid': int(fpm_grid.dims[0]), 'image': int(focal.dims[0]),
+                   'batch': 1, 'precision': args.precision, 'field_dtype': 'complex64',
+                   'l2': 'flushed between steps (256 MiB write outside the per-step events)',
+                   'parallelism': 'replicas' if world > 1 else 'single-gpu'},
+        'roofline': {'bound': bound, 'achieved': achieved_tflops, 'peak': peak, 'unit': 'TFLOP/s',
+                     'frac': achieved_tflops / peak, 'traffic': traffic, 'kernel': 'cgemm_nn_simt<float>'
+                     if args.precision == 'fp32' else 'split tcgen05 GEMM',
+                     'algorithmic': '%d complex MACs x 8 FLOP per propagation' % cmacs, 'peak_note': peak_note},
+        'e2e': {'value': e2e_value, 'unit': UNIT, 'h2d_bytes_per_step': int(e_host.numel() * 8),
+                'd2h_bytes_per_step': int(img_host.numel() * 8)},
+        'gpu_launches': int(gpu_launches),
+        'clocks': clocks,
+        'accuracy': {'ni_err_max': ni_max, 'ni_err_mean': ni_mean, 'dark_hole_mean_ni': ni_level,
+                     'region': '3-15 lambda/D', 'against': 'float64 oracle'},
+        'wall_s_timed': wall,
+    }
+    if cpu is not None:
+        line['cpu_baseline'] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    dist = None
+    if args.impl == 'reference':
+        return run_reference(args, rank, world)
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', 0)))
+        tdist.init_process_group('nccl')
+        dist = tdist
+    try:
+        run_ours(args, rank, world, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,25 @@
+"""hcipy_gb300: the HCIPy diffraction hot path on one GB300 GPU (sm_103a).
+
+Drop-in classes with the reference signatures; fields live on the device and
+every operator runs hand-written CUDA kernels from ``lib/libhcipy_gb300.so``
+through the C ABI of ``include/hcipy_gb300.h``.  There is no CPU path.
+"""
+from .field import (Field, CartesianGrid, RegularCoords, SeparatedCoords, UnstructuredCoords, make_uniform_grid,
+                    make_pupil_grid, make_focal_grid, make_focal_grid_from_pupil_grid)
+from .fourier import (FourierTransform, ComputationalComplexity, MatrixFourierTransform, make_fourier_transform,
+                      make_fft_grid, get_fft_parameters, is_fft_grid)
+from .optics import (Wavefront, OpticalElement, AgnosticOpticalElement, Apodizer, PhaseApodizer,
+                     make_agnostic_forward, make_agnostic_backward)
+from .propagation import FraunhoferPropagator
+from .coronagraphy import LyotCoronagraph
+from ._lib import HXError, launch_count
+
+__all__ = [
+    'Field', 'CartesianGrid', 'RegularCoords', 'SeparatedCoords', 'UnstructuredCoords', 'make_uniform_grid',
+    'make_pupil_grid', 'make_focal_grid', 'make_focal_grid_from_pupil_grid',
+    'FourierTransform', 'ComputationalComplexity', 'MatrixFourierTransform', 'make_fourier_transform',
+    'make_fft_grid', 'get_fft_parameters', 'is_fft_grid',
+    'Wavefront', 'OpticalElement', 'AgnosticOpticalElement', 'Apodizer', 'PhaseApodizer',
+    'make_agnostic_forward', 'make_agnostic_backward',
+    'FraunhoferPropagator', 'LyotCoronagraph', 'HXError', 'launch_count',
+]

@@ -1,0 +1,122 @@
+"""ctypes binding of the C ABI in ``include/hcipy_gb300.h``.
+
+The shared library is built in-tree (``hcipy_gb300/lib/libhcipy_gb300.so``).
+There is no CPU path: every operator of this package calls into it, and
+loading fails loudly when it has not been built or no CUDA device is present.
+"""
+import ctypes
+import os
+
+import torch
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, 'lib', 'libhcipy_gb300.so')
+
+HX_OK = 0
+HX_ERR_INVALID = -1
+HX_ERR_CUDA = -2
+HX_ERR_UNSUPPORTED = -3
+HX_ERR_TIMEOUT = -4
+HX_ERR_ALLOC = -5
+HX_ERR_INJECTED = -6
+
+HX_C64 = 0
+HX_C128 = 1
+HX_FORWARD = 0
+HX_BACKWARD = 1
+HX_ADJOINT = 2
+HX_PREC_FP32 = 0
+HX_PREC_SPLIT = 1
+HX_EPI_NONE = 0
+HX_EPI_MUL = 1
+HX_EPI_BABINET = 2
+
+c_int = ctypes.c_int
+c_double = ctypes.c_double
+c_size_t = ctypes.c_size_t
+c_void_p = ctypes.c_void_p
+c_ll = ctypes.c_longlong
+P = ctypes.POINTER
+
+# name -> (restype, argtypes); mirrors include/hcipy_gb300.h.
+SIGNATURES = {
+    'hx_last_error': (ctypes.c_char_p, []),
+    'hx_version': (c_int, []),
+    'hx_launch_count': (c_ll, []),
+    'hx_mft_plan_create': (c_int, [c_int, c_int, c_int, c_int, P(c_double), P(c_double), P(c_double), P(c_double),
+                                   P(c_double), P(c_double), P(c_double), P(c_double), c_int, c_int, c_void_p,
+                                   P(c_void_p)]),
+    'hx_mft_workspace_bytes': (c_size_t, [c_void_p, c_int, c_int]),
+    'hx_mft_execute': (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_double, c_double, c_void_p, c_size_t,
+                               c_void_p]),
+    'hx_mft_execute_ex': (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_double, c_double, c_int, c_void_p,
+                                  c_void_p, c_void_p, c_size_t, c_void_p]),
+    'hx_mft_plan_destroy': (c_int, [c_void_p]),
+}
+
+_lib = None
+
+
+class HXError(RuntimeError):
+    """A failure reported by the CUDA library (status code and message)."""
+
+    def __init__(self, code, message):
+        RuntimeError.__init__(self, '%s (status %d)' % (message, code))
+        self.code = code
+
+
+def load():
+    """Load the shared library; raise ImportError when it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError('hcipy_gb300: the CUDA library %s is not built; run `python -m hcipy_gb300._build` '
+                          '(or __graft_entry__.build()) first' % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def lib():
+    lib_ = load()
+    if not torch.cuda.is_available():
+        raise RuntimeError('hcipy_gb300 needs a CUDA device (GB300, sm_103a); no CPU path exists')
+    return lib_
+
+
+def check(rc, what=''):
+    if rc == HX_OK:
+        return
+    msg = load().hx_last_error().decode(errors='replace')
+    if what:
+        msg = '%s: %s' % (what, msg)
+    if rc == HX_ERR_INVALID:
+        raise ValueError(msg)
+    raise HXError(rc, msg)
+
+
+def stream_handle(stream=None):
+    s = torch.cuda.current_stream() if stream is None else stream
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def dptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def darr(a):
+    """A float64 host array as a ctypes pointer (None -> NULL); keeps the buffer alive via the return tuple."""
+    import numpy as np
+    if a is None:
+        return None, None
+    buf = np.ascontiguousarray(a, dtype=np.float64)
+    return buf, buf.ctypes.data_as(P(c_double))
+
+
+def launch_count():
+    return int(load().hx_launch_count())

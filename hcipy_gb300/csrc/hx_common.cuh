@@ -1,0 +1,68 @@
+// Shared helpers of the hcipy_gb300 CUDA library: status codes, error text,
+// launch accounting and small complex-arithmetic utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <cstdio>
+#include <cstring>
+
+#include "../../include/hcipy_gb300.h"
+
+namespace hx {
+
+// Records the message of the last failure on this host thread (read back by hx_last_error()).
+void set_error(const char* fmt, ...);
+
+// Counts every kernel this library launches (hx_launch_count()).
+void count_launch(int n = 1);
+
+// Host-side fault injection: when HX_FAULT names `site` ("alloc", "plan" or
+// "launch"), the entry point returns HX_ERR_INJECTED before touching the GPU.
+bool fault_injected(const char* site);
+
+inline int cuda_status(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return HX_OK;
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return HX_ERR_CUDA;
+}
+
+// Checks the launch that was just issued.
+inline int launch_status(const char* what) {
+    count_launch();
+    return cuda_status(cudaGetLastError(), what);
+}
+
+inline unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
+
+template <typename T> struct cplx;
+template <> struct cplx<float> { using type = float2; };
+template <> struct cplx<double> { using type = double2; };
+
+template <typename T> __host__ __device__ inline typename cplx<T>::type make_c(T re, T im);
+template <> __host__ __device__ inline float2 make_c<float>(float re, float im) { return make_float2(re, im); }
+template <> __host__ __device__ inline double2 make_c<double>(double re, double im) { return make_double2(re, im); }
+
+template <typename C> __host__ __device__ inline C cmul(C a, C b) {
+    C r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+
+}  // namespace hx
+
+#define HX_TRY(expr)                  \
+    do {                              \
+        int _hx_rc = (expr);          \
+        if (_hx_rc != HX_OK) return _hx_rc; \
+    } while (0)
+
+#define HX_CHECK_ARG(cond, ...)                 \
+    do {                                        \
+        if (!(cond)) {                          \
+            hx::set_error(__VA_ARGS__);         \
+            return HX_ERR_INVALID;              \
+        }                                       \
+    } while (0)

@@ -1,0 +1,235 @@
+// Matrix Fourier transform plans (hcipy/fourier/matrix_fourier_transform.py).
+//
+// A plan holds the phase matrices of the three directions, generated once on
+// the device in float64 (sincos of the float64 product a[r]*b[c], exactly the
+// numpy outer product the reference exponentiates at :95-102) and stored in the
+// plan's element type.  Separable non-uniform weights are folded into the
+// matrices, so every execute is two plain GEMMs:
+//   forward : T = in . M2f (stacked over the batch), out[b] = alpha * M1f . T[b]
+//   backward: T[b] = M1b . in[b],                   out = alpha * T . M2b (stacked)
+// The adjoint uses the backward matrices when the grids have uniform weights.
+#include "hx_common.cuh"
+#include "gemm_simt.cuh"
+#include "mft_tc.cuh"
+
+#include <vector>
+
+struct hx_mft_plan {
+    int nx, ny, nu, nv;
+    int dtype;
+    int precision;
+    size_t esize;
+    void* m1f = nullptr;  // nv x ny : exp(-i v y) wy[y]
+    void* m2f = nullptr;  // nx x nu : wx[x] exp(-i x u)
+    void* m1b = nullptr;  // ny x nv : exp(+i y v) wv[v]
+    void* m2b = nullptr;  // nu x nx : wu[u] exp(+i u x)
+    void* m1a = nullptr;  // ny x nv : wy[y] exp(+i y v)
+    void* m2a = nullptr;  // nu x nx : exp(+i u x) wx[x]
+    bool own_adjoint = false;
+    hx::SplitMftPlan* split = nullptr;  // tensor-core operands (HX_PREC_SPLIT)
+};
+
+namespace {
+
+// M[r, c] = wr[r] * wc[c] * exp(sign * i * a[r] * b[c]), computed in float64.
+template <typename T>
+__global__ void phase_matrix_kernel(int rows, int cols, const double* __restrict__ a, const double* __restrict__ b,
+                                    double sign, const double* __restrict__ wr, const double* __restrict__ wc,
+                                    typename hx::cplx<T>::type* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)rows * cols;
+    if (idx >= total) return;
+    const int r = (int)(idx / cols);
+    const int c = (int)(idx % cols);
+    const double phase = a[r] * b[c];
+    double s, co;
+    sincos(phase, &s, &co);
+    double w = 1.0;
+    if (wr) w *= wr[r];
+    if (wc) w *= wc[c];
+    out[idx] = hx::make_c<T>((T)(w * co), (T)(w * sign * s));
+}
+
+int upload(const double* host, int n, double** dev, cudaStream_t stream) {
+    *dev = nullptr;
+    if (host == nullptr) return HX_OK;
+    HX_TRY(hx::cuda_status(cudaMalloc(dev, sizeof(double) * n), "cudaMalloc(coords)"));
+    return hx::cuda_status(cudaMemcpyAsync(*dev, host, sizeof(double) * n, cudaMemcpyHostToDevice, stream), "upload coords");
+}
+
+int gen_matrix(int dtype, int rows, int cols, const double* a, const double* b, double sign,
+               const double* wr, const double* wc, void** out, cudaStream_t stream) {
+    const size_t es = dtype == HX_C64 ? sizeof(float2) : sizeof(double2);
+    HX_TRY(hx::cuda_status(cudaMalloc(out, es * (size_t)rows * cols), "cudaMalloc(phase matrix)"));
+    const long long total = (long long)rows * cols;
+    const unsigned blocks = hx::ceil_div(total, 256);
+    if (dtype == HX_C64)
+        phase_matrix_kernel<float><<<blocks, 256, 0, stream>>>(rows, cols, a, b, sign, wr, wc, (float2*)*out);
+    else
+        phase_matrix_kernel<double><<<blocks, 256, 0, stream>>>(rows, cols, a, b, sign, wr, wc, (double2*)*out);
+    return hx::launch_status("phase_matrix_kernel");
+}
+
+void free_plan(hx_mft_plan* p) {
+    if (!p) return;
+    cudaFree(p->m1f);
+    cudaFree(p->m2f);
+    cudaFree(p->m1b);
+    cudaFree(p->m2b);
+    if (p->own_adjoint) {
+        cudaFree(p->m1a);
+        cudaFree(p->m2a);
+    }
+    hx::split_mft_destroy(p->split);
+    delete p;
+}
+
+template <typename T>
+int execute_t(const hx_mft_plan* p, int direction, int batch, const void* in_, void* out_, double are, double aim,
+              int epilogue, const void* mask, const void* src, void* ws_, cudaStream_t stream) {
+    using Cx = typename hx::cplx<T>::type;
+    const Cx* in = (const Cx*)in_;
+    Cx* out = (Cx*)out_;
+    Cx* T1 = (Cx*)ws_;
+    const Cx one = hx::make_c<T>(T(1), T(0));
+    const Cx alpha = hx::make_c<T>((T)are, (T)aim);
+    const int nx = p->nx, ny = p->ny, nu = p->nu, nv = p->nv;
+    hx::Epilogue<Cx> epi;
+    epi.kind = epilogue;
+    epi.mask = (const Cx*)mask;
+    epi.src = (const Cx*)src;
+    if (direction == HX_FORWARD) {
+        // T (batch*ny x nu) = in (batch*ny x nx) . M2f (nx x nu)
+        HX_TRY(hx::cgemm_nn<T>(batch * ny, nu, nx, one, in, nx, 0, (const Cx*)p->m2f, nu, 0, T1, nu, 0, 1, stream));
+        // out[b] (nv x nu) = alpha * M1f (nv x ny) . T[b] (ny x nu)
+        epi.rows_per_field = nv;
+        return hx::cgemm_nn<T>(nv, nu, ny, alpha, (const Cx*)p->m1f, ny, 0, T1, nu, (long long)ny * nu, out, nu,
+                               (long long)nv * nu, batch, stream, epi);
+    }
+    const Cx* m1 = (const Cx*)(direction == HX_BACKWARD ? p->m1b : p->m1a);
+    const Cx* m2 = (const Cx*)(direction == HX_BACKWARD ? p->m2b : p->m2a);
+    // T[b] (ny x nu) = M1 (ny x nv) . in[b] (nv x nu)
+    HX_TRY(hx::cgemm_nn<T>(ny, nu, nv, one, m1, nv, 0, in, nu, (long long)nv * nu, T1, nu, (long long)ny * nu, batch,
+                           stream));
+    // out (batch*ny x nx) = alpha * T (batch*ny x nu) . M2 (nu x nx)
+    epi.rows_per_field = ny;
+    return hx::cgemm_nn<T>(batch * ny, nx, nu, alpha, T1, nu, 0, m2, nx, 0, out, nx, 0, 1, stream, epi);
+}
+
+}  // namespace
+
+extern "C" {
+
+int hx_mft_plan_create(int nx, int ny, int nu, int nv, const double* x, const double* y, const double* u,
+                       const double* v, const double* w_in_x, const double* w_in_y, const double* w_out_u,
+                       const double* w_out_v, int dtype, int precision, void* stream_, hx_mft_plan** plan) {
+    HX_CHECK_ARG(plan != nullptr, "hx_mft_plan_create: plan pointer is NULL");
+    *plan = nullptr;
+    HX_CHECK_ARG(nx > 0 && ny > 0 && nu > 0 && nv > 0, "hx_mft_plan_create: dimensions must be positive (%d %d %d %d)",
+                 nx, ny, nu, nv);
+    HX_CHECK_ARG(x && y && u && v, "hx_mft_plan_create: coordinate arrays must not be NULL");
+    HX_CHECK_ARG(dtype == HX_C64 || dtype == HX_C128, "hx_mft_plan_create: unknown dtype %d", dtype);
+    HX_CHECK_ARG(precision == HX_PREC_FP32 || precision == HX_PREC_SPLIT, "hx_mft_plan_create: unknown precision %d",
+                 precision);
+    HX_CHECK_ARG(!(precision == HX_PREC_SPLIT && dtype != HX_C64),
+                 "hx_mft_plan_create: the split tensor-core form takes complex64 fields");
+    if (hx::fault_injected("plan")) return HX_ERR_INJECTED;
+    if (hx::fault_injected("alloc")) return HX_ERR_INJECTED;
+    cudaStream_t stream = (cudaStream_t)stream_;
+
+    hx_mft_plan* p = new hx_mft_plan();
+    p->nx = nx; p->ny = ny; p->nu = nu; p->nv = nv;
+    p->dtype = dtype;
+    p->precision = precision;
+    p->esize = dtype == HX_C64 ? sizeof(float2) : sizeof(double2);
+
+    double *dx, *dy, *du, *dv, *dwx, *dwy, *dwu, *dwv;
+    dx = dy = du = dv = dwx = dwy = dwu = dwv = nullptr;
+    int rc = HX_OK;
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(stream);
+        for (double* q : {dx, dy, du, dv, dwx, dwy, dwu, dwv}) cudaFree(q);
+    };
+    do {
+        if ((rc = upload(x, nx, &dx, stream))) break;
+        if ((rc = upload(y, ny, &dy, stream))) break;
+        if ((rc = upload(u, nu, &du, stream))) break;
+        if ((rc = upload(v, nv, &dv, stream))) break;
+        if ((rc = upload(w_in_x, nx, &dwx, stream))) break;
+        if ((rc = upload(w_in_y, ny, &dwy, stream))) break;
+        if ((rc = upload(w_out_u, nu, &dwu, stream))) break;
+        if ((rc = upload(w_out_v, nv, &dwv, stream))) break;
+        if ((rc = gen_matrix(dtype, nv, ny, dv, dy, -1.0, nullptr, dwy, &p->m1f, stream))) break;
+        if ((rc = gen_matrix(dtype, nx, nu, dx, du, -1.0, dwx, nullptr, &p->m2f, stream))) break;
+        if ((rc = gen_matrix(dtype, ny, nv, dy, dv, +1.0, nullptr, dwv, &p->m1b, stream))) break;
+        if ((rc = gen_matrix(dtype, nu, nx, du, dx, +1.0, dwu, nullptr, &p->m2b, stream))) break;
+        const bool weighted_in = (w_in_x != nullptr) || (w_in_y != nullptr);
+        const bool weighted_out = (w_out_u != nullptr) || (w_out_v != nullptr);
+        if (!weighted_in && !weighted_out) {
+            p->m1a = p->m1b;
+            p->m2a = p->m2b;
+        } else {
+            p->own_adjoint = true;
+            if ((rc = gen_matrix(dtype, ny, nv, dy, dv, +1.0, dwy, nullptr, &p->m1a, stream))) break;
+            if ((rc = gen_matrix(dtype, nu, nx, du, dx, +1.0, nullptr, dwx, &p->m2a, stream))) break;
+        }
+        if (precision == HX_PREC_SPLIT) {
+            if ((rc = hx::split_mft_create(nx, ny, nu, nv, (const float2*)p->m1f, (const float2*)p->m2f,
+                                           (const float2*)p->m1b, (const float2*)p->m2b, (const float2*)p->m1a,
+                                           (const float2*)p->m2a, stream, &p->split)))
+                break;
+        }
+    } while (false);
+    cleanup();
+    if (rc != HX_OK) {
+        free_plan(p);
+        return rc;
+    }
+    *plan = p;
+    return HX_OK;
+}
+
+size_t hx_mft_workspace_bytes(const hx_mft_plan* p, int direction, int batch) {
+    if (!p || batch <= 0) return 0;
+    size_t base = p->esize * (size_t)batch * p->ny * p->nu;
+    if (p->precision == HX_PREC_SPLIT) return hx::split_mft_workspace_bytes(p->split, direction, batch);
+    return base;
+}
+
+int hx_mft_execute(const hx_mft_plan* p, int direction, int batch, const void* in, void* out, double are, double aim,
+                   void* ws, size_t ws_bytes, void* stream_) {
+    return hx_mft_execute_ex(p, direction, batch, in, out, are, aim, HX_EPI_NONE, nullptr, nullptr, ws, ws_bytes,
+                             stream_);
+}
+
+int hx_mft_execute_ex(const hx_mft_plan* p, int direction, int batch, const void* in, void* out, double are,
+                      double aim, int epilogue, const void* mask, const void* src, void* ws, size_t ws_bytes,
+                      void* stream_) {
+    HX_CHECK_ARG(p != nullptr, "hx_mft_execute: plan is NULL");
+    HX_CHECK_ARG(direction == HX_FORWARD || direction == HX_BACKWARD || direction == HX_ADJOINT,
+                 "hx_mft_execute: unknown direction %d", direction);
+    HX_CHECK_ARG(batch >= 1, "hx_mft_execute: batch must be >= 1 (got %d)", batch);
+    HX_CHECK_ARG(in != nullptr && out != nullptr, "hx_mft_execute: NULL field pointer");
+    const size_t need = hx_mft_workspace_bytes(p, direction, batch);
+    HX_CHECK_ARG(ws != nullptr && ws_bytes >= need, "hx_mft_execute: workspace of %zu bytes needed, %zu given", need,
+                 ws_bytes);
+    HX_CHECK_ARG(epilogue == HX_EPI_NONE || epilogue == HX_EPI_MUL || epilogue == HX_EPI_BABINET,
+                 "hx_mft_execute_ex: unknown epilogue %d", epilogue);
+    HX_CHECK_ARG(epilogue != HX_EPI_MUL || mask != nullptr, "hx_mft_execute_ex: HX_EPI_MUL needs a mask");
+    HX_CHECK_ARG(epilogue != HX_EPI_BABINET || src != nullptr, "hx_mft_execute_ex: HX_EPI_BABINET needs src");
+    if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
+    cudaStream_t stream = (cudaStream_t)stream_;
+    if (p->precision == HX_PREC_SPLIT)
+        return hx::split_mft_execute(p->split, direction, batch, (const float2*)in, (float2*)out, are, aim, epilogue,
+                                     (const float2*)mask, (const float2*)src, ws, ws_bytes, stream);
+    if (p->dtype == HX_C64)
+        return execute_t<float>(p, direction, batch, in, out, are, aim, epilogue, mask, src, ws, stream);
+    return execute_t<double>(p, direction, batch, in, out, are, aim, epilogue, mask, src, ws, stream);
+}
+
+int hx_mft_plan_destroy(hx_mft_plan* p) {
+    free_plan(p);
+    return HX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,241 @@
+"""Wavefronts and optical elements on the device (hcipy/optics).
+
+``Wavefront`` mirrors hcipy/optics/wavefront.py:15-361 for scalar fields:
+the electric field is cast to complex of the input bit depth, ``copy`` is a
+device copy, ``intensity`` / ``power`` / ``total_power`` are computed on the
+GPU.  ``AgnosticOpticalElement`` keeps the reference's instance cache
+(hcipy/optics/optical_element.py:261-790): instances keyed by input grid,
+output grid and a logarithmic wavelength key, at most 11, first in first out.
+"""
+import collections
+import itertools
+import math
+
+import numpy as np
+import torch
+
+from .field import Field, as_tensor, grid_key
+
+
+class Wavefront(object):
+    """A scalar wavefront: a device Field of the electric field and a wavelength."""
+
+    def __init__(self, electric_field, wavelength=1, input_stokes_vector=None):
+        if input_stokes_vector is not None:
+            raise NotImplementedError('Polarised wavefronts are not part of the GPU diffraction path.')
+        self.electric_field = electric_field
+        self.wavelength = wavelength
+        self._input_stokes_vector = None
+
+    @property
+    def electric_field(self):
+        return self._electric_field
+
+    @electric_field.setter
+    def electric_field(self, field):
+        # hcipy/optics/wavefront.py:77-88: complex of the same bit depth.
+        if not hasattr(field, 'grid'):
+            raise ValueError('The electric field must be a Field.')
+        grid = field.grid
+        t = as_tensor(field)
+        dt = torch.complex64 if t.dtype in (torch.float32, torch.complex64) else torch.complex128
+        if t.dtype != dt:
+            t = t.to(dt)
+        self._electric_field = Field(t, grid)
+
+    @property
+    def input_stokes_vector(self):
+        return self._input_stokes_vector
+
+    @property
+    def wavenumber(self):
+        return 2 * np.pi / self.wavelength
+
+    @property
+    def grid(self):
+        return self._electric_field.grid
+
+    def copy(self):
+        return Wavefront(self._electric_field.copy(), self.wavelength)
+
+    @property
+    def intensity(self):
+        e = self._electric_field.data
+        return Field(e.real * e.real + e.imag * e.imag, self.grid)
+
+    I = intensity  # noqa: E741
+
+    @property
+    def amplitude(self):
+        return Field(self._electric_field.data.abs(), self.grid)
+
+    @property
+    def phase(self):
+        return Field(torch.angle(self._electric_field.data), self.grid)
+
+    @property
+    def power(self):
+        w = self.grid.weights
+        w = torch.as_tensor(w, device=self._electric_field.data.device) if not np.isscalar(w) else w
+        return Field(self.intensity.data * w, self.grid)
+
+    @property
+    def total_power(self):
+        return self.power.data.sum(-1)
+
+
+class OpticalElement(object):
+    """Base class: forward/backward map a Wavefront to a Wavefront (hcipy/optics/optical_element.py:6-151)."""
+
+    def __call__(self, wavefront):
+        return self.forward(wavefront)
+
+    def forward(self, wavefront):
+        raise NotImplementedError()
+
+    def backward(self, wavefront):
+        raise NotImplementedError()
+
+
+class InstanceData(object):
+    def __init__(self, input_grid, output_grid, wavelength):
+        self.input_grid = input_grid
+        self.output_grid = output_grid
+        self.wavelength = wavelength
+
+
+def _wavelength_key(wavelength):
+    # hcipy/optics/optical_element.py:333.
+    return int(np.round(np.log(wavelength) / np.log(1 + 1e-9)))
+
+
+class AgnosticOpticalElement(OpticalElement):
+    """Optical element whose device state depends on the grids and the wavelength it is used with."""
+
+    def __init__(self, grid_dependent=True, wavelength_dependent=True, max_in_cache=11):
+        self._grid_dependent = grid_dependent
+        self._wavelength_dependent = wavelength_dependent
+        self._max_in_cache = max_in_cache
+        self.clear_cache()
+
+    def clear_cache(self):
+        self._cache = collections.OrderedDict()
+        self._instances = collections.OrderedDict()
+
+    def _keys(self, input_grid, output_grid, wavelength):
+        grid_parts = [(None, None)]
+        if self._grid_dependent:
+            ki = None if input_grid is None else grid_key(input_grid)
+            ko = None if output_grid is None else grid_key(output_grid)
+            if ki is None and ko is None:
+                raise ValueError('Grid dependent, but no grids are given for lookup.')
+            if ki is None or ko is None:
+                grid_parts = [(ki, ko)]
+            else:
+                grid_parts = [(ki, ko), (ki, None), (None, ko)]
+        wl_part = (None,)
+        if self._wavelength_dependent:
+            if wavelength is None:
+                raise ValueError('Wavelength dependent, but no wavelength is given for lookup.')
+            wl_part = (_wavelength_key(wavelength),)
+        return [g + wl_part for g in grid_parts]
+
+    def get_instance_data(self, input_grid, output_grid, wavelength):
+        for key in self._keys(input_grid, output_grid, wavelength):
+            if key in self._cache:
+                return self._cache[key]
+        if input_grid is None:
+            input_grid = self.get_input_grid(output_grid, wavelength)
+        if output_grid is None:
+            output_grid = self.get_output_grid(input_grid, wavelength)
+        keys = self._keys(input_grid, output_grid, wavelength)
+        for key in keys:
+            if key in self._cache:
+                return self._cache[key]
+        inst = InstanceData(input_grid, output_grid, wavelength)
+        self.make_instance(inst, input_grid, output_grid, wavelength)
+        if len(self._instances) >= self._max_in_cache:
+            _, (old, old_keys) = self._instances.popitem(last=False)
+            for k in old_keys:
+                self._cache.pop(k, None)
+        self._instances[id(inst)] = (inst, keys)
+        for key in keys:
+            self._cache[key] = inst
+        return inst
+
+    def make_instance(self, instance_data, input_grid, output_grid, wavelength):
+        pass
+
+    def get_input_grid(self, output_grid, wavelength):
+        raise ValueError('This optical element cannot infer its input grid.')
+
+    def get_output_grid(self, input_grid, wavelength):
+        raise ValueError('This optical element cannot infer its output grid.')
+
+    def evaluate_parameter(self, parameter, input_grid, output_grid, wavelength):
+        if callable(parameter):
+            return parameter(wavelength)
+        return parameter
+
+
+def make_agnostic_forward(forward):
+    def res(self, wavefront, *args, **kwargs):
+        inst = self.get_instance_data(wavefront.grid, None, wavefront.wavelength)
+        return forward(self, inst, wavefront, *args, **kwargs)
+    return res
+
+
+def make_agnostic_backward(backward):
+    def res(self, wavefront, *args, **kwargs):
+        inst = self.get_instance_data(None, wavefront.grid, wavefront.wavelength)
+        return backward(self, inst, wavefront, *args, **kwargs)
+    return res
+
+
+def _apodization_tensor(a, wavelength, like):
+    if callable(a):
+        a = a(wavelength)
+    if np.isscalar(a):
+        return a
+    return as_tensor(a, like.device)
+
+
+class Apodizer(OpticalElement):
+    """A thin apodizer: E * a forward, E * conj(a) backward (hcipy/optics/apodization.py:6-35)."""
+
+    def __init__(self, apodization):
+        self.apodization = apodization
+
+    def forward(self, wavefront):
+        e = wavefront.electric_field
+        a = _apodization_tensor(self.apodization, wavefront.wavelength, e.data)
+        return Wavefront(Field(e.data * a, e.grid), wavefront.wavelength)
+
+    def backward(self, wavefront):
+        e = wavefront.electric_field
+        a = _apodization_tensor(self.apodization, wavefront.wavelength, e.data)
+        a = a.conj() if isinstance(a, torch.Tensor) else np.conj(a)
+        return Wavefront(Field(e.data * a, e.grid), wavefront.wavelength)
+
+
+class PhaseApodizer(OpticalElement):
+    """E * exp(+-i phase) (hcipy/optics/apodization.py:37-62)."""
+
+    def __init__(self, phase):
+        self._phase = phase
+
+    @property
+    def phase(self):
+        return self._phase
+
+    def _apply(self, wavefront, sign):
+        from .kernels import apply_phase
+        e = wavefront.electric_field
+        return Wavefront(Field(apply_phase(e.data, as_tensor(self._phase, e.data.device), sign), e.grid),
+                         wavefront.wavelength)
+
+    def forward(self, wavefront):
+        return self._apply(wavefront, 1.0)
+
+    def backward(self, wavefront):
+        return self._apply(wavefront, -1.0)

@@ -1,0 +1,87 @@
+"""Seeded synthetic inputs of the benchmark configurations (host-side, float64 numpy).
+
+Stand-ins for the reference's input generators, with the same shapes and value
+distributions: a circular aperture (hcipy/aperture/generic.py:11-46), Noll-indexed
+Zernike modes on the unit disk (hcipy/mode_basis/zernike.py:455-506) and
+random coefficients scaled to a stated RMS inside the aperture.  These run once
+per workload on the host; the propagation itself runs on the device.
+"""
+import math
+
+import numpy as np
+
+from .field import make_pupil_grid, make_focal_grid
+
+
+def circular_aperture(grid, diameter, center=(0.0, 0.0)):
+    """1 inside the circle of ``diameter`` (boundary inclusive), else 0, as in generic.py:31-44."""
+    x, y = grid.points_list()
+    return ((x - center[0])**2 + (y - center[1])**2 <= (diameter / 2)**2).astype(np.float64)
+
+
+def noll_to_zernike(j):
+    """Noll index (1-based) -> (n, m)."""
+    n = 0
+    j1 = j - 1
+    while j1 > n:
+        n += 1
+        j1 -= n
+    m = (-1)**j * ((n % 2) + 2 * int((j1 + ((n + 1) % 2)) / 2))
+    return n, m
+
+
+def zernike(n, m, r, theta):
+    """Orthonormal (unit RMS over the unit disk) Zernike polynomial."""
+    mm = abs(m)
+    rad = np.zeros_like(r)
+    for k in range((n - mm) // 2 + 1):
+        c = (-1)**k * math.factorial(n - k) / (math.factorial(k) * math.factorial((n + mm) // 2 - k)
+                                                * math.factorial((n - mm) // 2 - k))
+        rad += c * r**(n - 2 * k)
+    if m == 0:
+        return math.sqrt(n + 1) * rad
+    if m > 0:
+        return math.sqrt(2 * (n + 1)) * rad * np.cos(mm * theta)
+    return math.sqrt(2 * (n + 1)) * rad * np.sin(mm * theta)
+
+
+def zernike_phase(grid, diameter, first, last, rms, seed):
+    """sum_{j=first..last} c_j Z_j with c ~ N(0,1), scaled to ``rms`` inside the aperture."""
+    x, y = grid.points_list()
+    r = np.hypot(x, y) / (diameter / 2)
+    theta = np.arctan2(y, x)
+    rng = np.random.default_rng(seed)
+    coeffs = rng.standard_normal(last - first + 1)
+    phase = np.zeros_like(r)
+    for c, j in zip(coeffs, range(first, last + 1)):
+        n, m = noll_to_zernike(j)
+        phase += c * zernike(n, m, r, theta)
+    inside = r <= 1
+    phase -= phase[inside].mean()
+    phase *= rms / np.std(phase[inside])
+    return phase
+
+
+def lyot_workload(pupil_n=2048, fpm_q=8, fpm_num_airy=32, occulter_radius=4.0, stop_diameter=0.9,
+                  final_q=8, final_num_airy=32, rms_rad=2 * np.pi * 1e-3, seed=3, nmodes=(2, 100)):
+    """The precision-form coronagraph workload: aberrated circular pupil, occulting FPM, Lyot stop.
+
+    Defaults: 2048^2 pupil, FPM radius 4 lambda/D on a q=8, num_airy=32 grid
+    (512^2), Lyot stop 0.9 D, final focal grid q=8, num_airy=32 (512^2),
+    Zernike 2-100 at 1 nm RMS (2 pi 1e-3 rad at lambda0 = 1 um).
+    """
+    pupil = make_pupil_grid(pupil_n, 1)
+    aperture = circular_aperture(pupil, 1.0)
+    phase = zernike_phase(pupil, 1.0, nmodes[0], nmodes[1], rms_rad, seed)
+    e = aperture * np.exp(1j * phase)
+    fpm_grid = make_focal_grid(fpm_q, fpm_num_airy)
+    fpm = 1 - circular_aperture(fpm_grid, 2 * occulter_radius)
+    stop = circular_aperture(pupil, stop_diameter)
+    focal = make_focal_grid(final_q, final_num_airy)
+    return dict(pupil=pupil, aperture=aperture, E=e, fpm_grid=fpm_grid, fpm=fpm, stop=stop, focal=focal)
+
+
+def dark_hole_mask(focal, r_in=3.0, r_out=15.0):
+    x, y = focal.points_list()
+    r = np.hypot(x, y)
+    return (r >= r_in) & (r <= r_out)

@@ -1,0 +1,120 @@
+/*
+ * hcipy_gb300 -- C ABI of the GB300 (sm_103a) diffraction kernels.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, and
+ * returns an int status (HX_OK = 0, negative on failure; hx_last_error()
+ * gives the message of the last failure on the calling thread).  Device
+ * buffers are owned by the caller; a plan owns only its constant tables
+ * (phase matrices, twiddles, chirps, transfer functions).  `stream` is a
+ * cudaStream_t passed as void* (NULL = the legacy default stream).  All
+ * execute calls are asynchronous on that stream.
+ *
+ * Complex data are interleaved (re, im) pairs: HX_C64 = 2 x float32,
+ * HX_C128 = 2 x float64, the layouts of numpy complex64 / complex128.
+ * Two-dimensional fields are y-major: element (iy, ix) at iy * nx + ix,
+ * the order of HCIPy's flat Field on a 2-D CartesianGrid
+ * (hcipy/field/field.py:52-65, Field.shaped).
+ *
+ * Each declaration names the reference interface it replaces
+ * (paths relative to the HCIPy source tree).
+ */
+#ifndef HCIPY_GB300_H
+#define HCIPY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define HX_API __attribute__((visibility("default")))
+#else
+#define HX_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define HX_OK 0
+#define HX_ERR_INVALID (-1)     /* bad argument; the reference raises ValueError */
+#define HX_ERR_CUDA (-2)        /* a CUDA runtime call or launch failed */
+#define HX_ERR_UNSUPPORTED (-3) /* valid request that this build does not implement */
+#define HX_ERR_TIMEOUT (-4)     /* a bounded device-side wait gave up */
+#define HX_ERR_ALLOC (-5)       /* device allocation failed */
+#define HX_ERR_INJECTED (-6)    /* host-side fault injection (HX_FAULT=alloc|plan|launch) */
+
+/* Element types. */
+#define HX_C64 0
+#define HX_C128 1
+
+/* Directions of a Fourier operator. */
+#define HX_FORWARD 0  /* FourierTransform.forward */
+#define HX_BACKWARD 1 /* FourierTransform.backward (the inverse transform, with output weights) */
+#define HX_ADJOINT 2  /* the conjugate transpose of forward (input weights); used by gradients */
+
+/* Arithmetic of the MFT GEMMs. */
+#define HX_PREC_FP32 0  /* FP32 CUDA-core complex GEMM (HX_C64) or FP64 (HX_C128) */
+#define HX_PREC_SPLIT 1 /* split-operand tensor-core GEMM on tcgen05 */
+
+/* Message of the last failure on this thread ("" if none). */
+HX_API const char* hx_last_error(void);
+/* Library version as major*10000 + minor*100 + patch. */
+HX_API int hx_version(void);
+/* Number of kernels this library has launched in this process. */
+HX_API long long hx_launch_count(void);
+
+/* ------------------------------------------------------------------------
+ * Matrix Fourier transform.
+ * Replaces MatrixFourierTransform (hcipy/fourier/matrix_fourier_transform.py:42-224):
+ *   forward : out = alpha * M1 . diag(wy) . in . diag(wx) . M2          (:133-176)
+ *   backward: in  = alpha * M1^H . diag(wv) . out . diag(wu) . M2^H     (:179-224)
+ *   adjoint : in  = alpha * M1^H . out . M2^H  (weights applied by alpha)
+ * with M1[v,y] = exp(-i v y) (nv x ny) and M2[x,u] = exp(-i x u) (nx x nu)
+ * built in float64 on the device (:67-111).  x,y,u,v are the separated
+ * coordinates of the input and output grids (host arrays of float64).
+ * w_in_x/w_in_y/w_out_u/w_out_v are the separable weights of non-uniform
+ * separated grids, or NULL for uniform grids, whose scalar weight the caller
+ * folds into alpha as the reference folds it into the GEMM alpha (:161-172).
+ * A 1-D transform is the case ny = nv = 1, y = v = {0}.
+ * ------------------------------------------------------------------------ */
+typedef struct hx_mft_plan hx_mft_plan;
+
+HX_API int hx_mft_plan_create(int nx, int ny, int nu, int nv,
+                       const double* x, const double* y, const double* u, const double* v,
+                       const double* w_in_x, const double* w_in_y,
+                       const double* w_out_u, const double* w_out_v,
+                       int dtype, int precision, void* stream, hx_mft_plan** plan);
+
+/* Bytes of caller-provided scratch that hx_mft_execute needs for `batch` fields. */
+HX_API size_t hx_mft_workspace_bytes(const hx_mft_plan* plan, int direction, int batch);
+
+/* `in` holds `batch` contiguous fields of the source plane, `out` receives
+ * `batch` fields of the destination plane (both device pointers of the plan's dtype). */
+HX_API int hx_mft_execute(const hx_mft_plan* plan, int direction, int batch,
+                   const void* in, void* out, double alpha_re, double alpha_im,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
+/* Epilogues fused into the last GEMM of hx_mft_execute_ex (replacing the
+ * element-wise steps of the Lyot chain, hcipy/coronagraphy/lyot.py:79-90):
+ *   HX_EPI_MUL     : out = (alpha * T) * mask            -- Apodizer.forward on the destination plane
+ *                                                           (hcipy/optics/apodization.py:25-29)
+ *   HX_EPI_BABINET : out = mask * (src - alpha * T)      -- Babinet subtraction E - P^-1[...] followed
+ *                                                           by the Lyot stop; mask may be NULL (no stop)
+ * mask has one field of the destination plane (broadcast over the batch);
+ * src has `batch` fields of the destination plane. */
+#define HX_EPI_NONE 0
+#define HX_EPI_MUL 1
+#define HX_EPI_BABINET 2
+
+HX_API int hx_mft_execute_ex(const hx_mft_plan* plan, int direction, int batch,
+                      const void* in, void* out, double alpha_re, double alpha_im,
+                      int epilogue, const void* mask, const void* src,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+HX_API int hx_mft_plan_destroy(hx_mft_plan* plan);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HCIPY_GB300_H */

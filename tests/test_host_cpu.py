@@ -1,0 +1,85 @@
+"""Host-side logic that runs without a GPU: grids, FFT-grid algebra, the instance cache."""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from oracle import grids as ogrids
+
+import hcipy_gb300 as hg
+
+
+def test_pupil_and_focal_grids_match_reference():
+    g = load_golden('fraunhofer_cfg1')
+    pupil = hg.make_pupil_grid(256, 1)
+    focal = hg.make_focal_grid(q=4, num_airy=16)
+    np.testing.assert_array_equal(pupil.dims, g['pupil_dims'])
+    np.testing.assert_allclose(pupil.delta, g['pupil_delta'], rtol=0)
+    np.testing.assert_allclose(pupil.zero, g['pupil_zero'], rtol=1e-15)
+    np.testing.assert_array_equal(focal.dims, g['focal_dims'])
+    np.testing.assert_allclose(focal.zero, g['focal_zero'], rtol=1e-15)
+    assert pupil.weights == pytest.approx(g['pupil_weights'][0], rel=1e-15)
+    assert pupil.shape == (256, 256)
+
+
+@pytest.mark.parametrize('case', ['fft_0', 'fft_1', 'fft_2', 'fft_3'])
+def test_fft_grid_algebra(case):
+    g = load_golden(case)
+    pupil = hg.make_pupil_grid(tuple(g['ingrid_dims']), tuple(g['ingrid_dims'] * g['ingrid_delta']))
+    out = hg.make_fft_grid(pupil, float(g['q']), float(g['fov']), tuple(g['shift']))
+    np.testing.assert_array_equal(out.dims, g['outgrid_dims'])
+    np.testing.assert_allclose(out.delta, g['outgrid_delta'], rtol=1e-14)
+    np.testing.assert_allclose(out.zero, g['outgrid_zero'], rtol=1e-12, atol=1e-14)
+    q, fov, shift = hg.get_fft_parameters(out, pupil)
+    again = hg.make_fft_grid(pupil, q, fov, shift)
+    np.testing.assert_array_equal(again.dims, out.dims)
+    np.testing.assert_allclose(again.zero, out.zero, rtol=1e-12, atol=1e-14)
+
+
+def test_non_fft_grid_detected():
+    pupil = hg.make_pupil_grid(64, 1)
+    focal = hg.make_focal_grid(3.3, 8).scaled(2 * np.pi)
+    assert not hg.is_fft_grid(focal, pupil)
+    assert hg.is_fft_grid(hg.make_fft_grid(pupil, 2, 0.5), pupil)
+
+
+def test_mft_supported_grids():
+    pupil = hg.make_pupil_grid(16, 1)
+    assert hg.MatrixFourierTransform.is_supported(pupil, hg.make_focal_grid(2, 4))
+    un = hg.CartesianGrid(hg.UnstructuredCoords([np.zeros(3), np.ones(3)]))
+    assert not hg.MatrixFourierTransform.is_supported(un, pupil)
+    with pytest.raises(ValueError):
+        hg.MatrixFourierTransform.check_if_supported(pupil, hg.make_uniform_grid(5, 1))
+
+
+def test_separated_weights_match_reference_formula():
+    g = hg.CartesianGrid(hg.SeparatedCoords([np.array([0.0, 0.1, 0.3, 0.6]), np.array([1.0, 1.5, 2.5])]))
+    w = g.weights
+    wx = np.array([0.1, 0.15, 0.25, 0.3])
+    wy = np.array([0.5, 0.75, 1.0])
+    np.testing.assert_allclose(w, (wy[:, None] * wx[None, :]).ravel())
+
+
+def test_agnostic_cache_fifo():
+    made = []
+
+    class Probe(hg.AgnosticOpticalElement):
+        def make_instance(self, inst, ig, og, wl):
+            made.append(wl)
+
+        def get_output_grid(self, ig, wl):
+            return ig
+
+    p = Probe(max_in_cache=3)
+    g = hg.make_pupil_grid(8)
+    for wl in [1.0, 1.1, 1.2, 1.0, 1.3, 1.0]:
+        p.get_instance_data(g, None, wl)
+    # 1.0 hit once, evicted by 1.3 (FIFO of 3), then rebuilt.
+    assert made == [1.0, 1.1, 1.2, 1.3, 1.0]
+    assert len(p._instances) == 3
+
+
+def test_oracle_grid_factories_agree_with_package():
+    a = hg.make_focal_grid(2.5, (5, 7))
+    b = ogrids.make_focal_grid(2.5, (5, 7))
+    np.testing.assert_array_equal(a.dims, b.dims)
+    np.testing.assert_allclose(a.zero, b.zero)
