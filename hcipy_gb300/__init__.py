@@ -10,7 +10,8 @@ from .fourier import (FourierTransform, ComputationalComplexity, MatrixFourierTr
                       make_fft_grid, get_fft_parameters, is_fft_grid)
 from .optics import (Wavefront, OpticalElement, AgnosticOpticalElement, Apodizer, PhaseApodizer,
                      make_agnostic_forward, make_agnostic_backward)
-from .propagation import FraunhoferPropagator
+from .propagation import FraunhoferPropagator, AngularSpectrumPropagator
+from .fft import FastFourierTransform, ChirpZTransform, ZoomFastFourierTransform, FourierFilter
 from .coronagraphy import LyotCoronagraph
 from ._lib import HXError, launch_count
 
@@ -21,5 +22,6 @@ __all__ = [
     'make_fft_grid', 'get_fft_parameters', 'is_fft_grid',
     'Wavefront', 'OpticalElement', 'AgnosticOpticalElement', 'Apodizer', 'PhaseApodizer',
     'make_agnostic_forward', 'make_agnostic_backward',
-    'FraunhoferPropagator', 'LyotCoronagraph', 'HXError', 'launch_count',
+    'FraunhoferPropagator', 'AngularSpectrumPropagator', 'LyotCoronagraph', 'HXError', 'launch_count',
+    'FastFourierTransform', 'ChirpZTransform', 'ZoomFastFourierTransform', 'FourierFilter',
 ]

@@ -52,6 +52,24 @@ SIGNATURES = {
     'hx_mft_execute_ex': (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_double, c_double, c_int, c_void_p,
                                   c_void_p, c_void_p, c_size_t, c_void_p]),
     'hx_mft_plan_destroy': (c_int, [c_void_p]),
+    'hx_fft_plan_create': (c_int, [c_int, P(c_int), P(c_int), P(c_int), P(c_int), P(c_int), P(P(c_double)),
+                                   P(P(c_double)), c_double, c_double, c_int, c_void_p, P(c_void_p)]),
+    'hx_fft_workspace_bytes': (c_size_t, [c_void_p, c_int, c_int]),
+    'hx_fft_execute': (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    'hx_fft_plan_destroy': (c_int, [c_void_p]),
+    'hx_filter_plan_create': (c_int, [c_int, P(c_int), P(c_int), P(c_int), c_void_p, c_int, c_void_p, P(c_void_p)]),
+    'hx_filter_workspace_bytes': (c_size_t, [c_void_p, c_int]),
+    'hx_filter_execute': (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    'hx_filter_plan_destroy': (c_int, [c_void_p]),
+    'hx_czt_plan_create': (c_int, [c_int, c_int, c_double, c_double, c_double, c_double, P(c_double), P(c_double),
+                                   c_int, c_void_p, P(c_void_p)]),
+    'hx_czt_execute': (c_int, [c_void_p, c_int, c_int, c_void_p, c_ll, c_ll, c_ll, c_void_p, c_ll, c_ll, c_ll,
+                               c_void_p]),
+    'hx_czt_plan_destroy': (c_int, [c_void_p]),
+    'hx_asp_transfer_function': (c_int, [c_int, c_int, c_double, c_double, c_double, c_double, c_double, c_double,
+                                         c_int, c_int, c_void_p, c_void_p]),
+    'hx_asp_impulse_response': (c_int, [c_int, c_int, c_double, c_double, c_double, c_double, c_double, c_double,
+                                        c_int, c_int, c_void_p, c_void_p]),
 }
 
 _lib = None
@@ -116,6 +134,39 @@ def darr(a):
         return None, None
     buf = np.ascontiguousarray(a, dtype=np.float64)
     return buf, buf.ctypes.data_as(P(c_double))
+
+
+def iarr(values):
+    """A host int array as a ctypes pointer; returns (buffer, pointer)."""
+    buf = (ctypes.c_int * len(values))(*[int(v) for v in values])
+    return buf, ctypes.cast(buf, P(c_int))
+
+
+def carr(values):
+    """A host complex array as interleaved float64 (buffer, pointer); None -> (None, None)."""
+    import numpy as np
+    if values is None:
+        return None, None
+    buf = np.ascontiguousarray(np.asarray(values, dtype=np.complex128)).view(np.float64)
+    return buf, buf.ctypes.data_as(P(c_double))
+
+
+def ptr_array(ptrs):
+    """An array of double* (None -> NULL) for the per-axis factor arguments."""
+    arr = (P(c_double) * len(ptrs))(*[p if p is not None else P(c_double)() for p in ptrs])
+    return arr, ctypes.cast(arr, P(P(c_double)))
+
+
+def workspace(nbytes, device):
+    return torch.empty(max(int(nbytes), 16), dtype=torch.uint8, device=device)
+
+
+def dtype_code(dt):
+    if dt == torch.complex64:
+        return HX_C64
+    if dt == torch.complex128:
+        return HX_C128
+    raise ValueError('unsupported dtype %s' % dt)
 
 
 def launch_count():

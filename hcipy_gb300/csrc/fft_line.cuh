@@ -1,0 +1,381 @@
+// Batched 1-D FFTs along one axis of a strided array, in shared memory, with
+// zero-padding, index shifts, cropping, phase factors and (optionally) a
+// spectrum multiply plus inverse transform fused into the same launch.
+//
+// Each CTA owns `lines_per_cta` lines of length M (the shared-memory FFT
+// length).  The transform is a mixed-radix Stockham autosort over radices
+// {2,3,4,5,7,8}: stage s with radix R and accumulated size Ns reads
+// v[r] = buf[j + r M/R], multiplies by the twiddles exp(-+2 pi i r (j mod Ns)/(Ns R)),
+// does an R-point DFT in registers and writes buf[(j/Ns) Ns R + j mod Ns + r Ns].
+// Every thread keeps its butterflies of a stage in registers across one
+// __syncthreads, so the stage runs in place in one shared buffer.  Twiddles
+// come from a float64-accurate table exp(-2 pi i t/M), t < M.
+//
+// Load of line l, FFT index j < M:
+//   j >= n_log                      -> 0
+//   p = (j + load_add) mod n_log - in_offset   (index shift and zero-pad)
+//   value = in[l, p] * pre[l, p] * chirp_in[j] if 0 <= p < in_count, else 0
+// Optional conv stage (CONV): forward FFT, times mid[l, k], inverse FFT.
+// Store of output kk < out_count:
+//   src = (out_offset + kk + store_add) mod out_mod
+//   out[l, kk] = buf[src] * chirp_out[src] * post[l, kk] * scale
+// This one kernel serves the zero-padded FFT with fftshifts and crop, the
+// chirp-Z transform (Bluestein), Bluestein for lengths that are not
+// 2,3,5,7-smooth, and the column pass of the Fourier filter.
+#pragma once
+
+#include "hx_common.cuh"
+
+namespace hx {
+
+template <typename T>
+struct LineArgs {
+    using Cx = typename cplx<T>::type;
+    int M;                // shared-memory FFT length
+    int n_log;            // logical input length (load wrap / zero beyond)
+    int nlines;           // lines per field
+    int lines_per_cta;
+    int pitch;            // shared-memory stride between lines (>= M)
+    int nstages;
+    unsigned long long radix_code;  // radix of stage s in bits [4s, 4s+4)
+    const Cx* tw;         // M entries, exp(-2 pi i t / M)
+    // load
+    const Cx* in;
+    long long in_ls, in_es, in_bs;
+    int in_count, in_offset, load_add;
+    const Cx* pre;        // indexed [l*pre_ls + p], or null
+    long long pre_ls;
+    const Cx* chirp_in;   // indexed [j], or null
+    // spectrum multiply (CONV)
+    const Cx* mid;        // indexed [l*mid_ls + k*mid_es]
+    long long mid_ls, mid_es;
+    int mid_conj;
+    // store
+    Cx* out;
+    long long out_ls, out_es, out_bs;
+    int out_count, out_offset, store_add, out_mod;
+    const Cx* chirp_out;  // indexed [src], or null
+    const Cx* post;       // indexed [l*post_ls + kk*post_es], or null
+    long long post_ls, post_es;
+    Cx scale;
+};
+
+template <typename Cx>
+__device__ __forceinline__ Cx c_add(Cx a, Cx b) { Cx r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename Cx>
+__device__ __forceinline__ Cx c_sub(Cx a, Cx b) { Cx r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename Cx>
+__device__ __forceinline__ Cx c_mul(Cx a, Cx b) {
+    Cx r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+template <typename Cx>
+__device__ __forceinline__ Cx c_conj(Cx a) { a.y = -a.y; return a; }
+// Multiply by SIGN * i.
+template <int SIGN, typename Cx>
+__device__ __forceinline__ Cx c_rot(Cx z) {
+    Cx r;
+    if (SIGN < 0) { r.x = z.y; r.y = -z.x; } else { r.x = -z.y; r.y = z.x; }
+    return r;
+}
+template <typename Cx, typename T>
+__device__ __forceinline__ Cx c_scale(Cx a, T s) { a.x *= s; a.y *= s; return a; }
+
+// R-point DFTs with W = exp(SIGN 2 pi i / R): y_m = sum_r v_r W^(r m).
+template <typename T, int R, int SIGN>
+struct Dft;
+
+template <typename T, int SIGN>
+struct Dft<T, 2, SIGN> {
+    template <typename Cx>
+    __device__ __forceinline__ static void run(Cx* v) {
+        Cx a = v[0], b = v[1];
+        v[0] = c_add(a, b);
+        v[1] = c_sub(a, b);
+    }
+};
+
+template <typename T, int SIGN>
+struct Dft<T, 4, SIGN> {
+    template <typename Cx>
+    __device__ __forceinline__ static void run(Cx* v) {
+        Cx t0 = c_add(v[0], v[2]), t1 = c_sub(v[0], v[2]);
+        Cx t2 = c_add(v[1], v[3]), t3 = c_rot<SIGN>(c_sub(v[1], v[3]));
+        v[0] = c_add(t0, t2);
+        v[2] = c_sub(t0, t2);
+        v[1] = c_add(t1, t3);
+        v[3] = c_sub(t1, t3);
+    }
+};
+
+template <typename T, int SIGN>
+struct Dft<T, 8, SIGN> {
+    template <typename Cx>
+    __device__ __forceinline__ static void run(Cx* v) {
+        const T h = T(0.70710678118654752440);
+        Cx a[4], b[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            a[k] = c_add(v[k], v[k + 4]);
+            b[k] = c_sub(v[k], v[k + 4]);
+        }
+        // b_k *= W8^k, W8 = h (1 + SIGN i)
+        {
+            Cx z = b[1];
+            Cx r;
+            r.x = h * (z.x - SIGN * z.y);
+            r.y = h * (z.y + SIGN * z.x);
+            b[1] = r;
+        }
+        b[2] = c_rot<SIGN>(b[2]);
+        {
+            Cx z = b[3];
+            Cx r;  // W8^3 = h (-1 + SIGN i)
+            r.x = h * (-z.x - SIGN * z.y);
+            r.y = h * (-z.y + SIGN * z.x);
+            b[3] = r;
+        }
+        Dft<T, 4, SIGN>::run(a);
+        Dft<T, 4, SIGN>::run(b);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            v[2 * m] = a[m];
+            v[2 * m + 1] = b[m];
+        }
+    }
+};
+
+template <typename T, int SIGN>
+struct Dft<T, 3, SIGN> {
+    template <typename Cx>
+    __device__ __forceinline__ static void run(Cx* v) {
+        const T c = T(-0.5);
+        const T s = T(0.86602540378443864676);
+        Cx sum = c_add(v[1], v[2]);
+        Cx dif = c_sub(v[1], v[2]);
+        Cx base;
+        base.x = v[0].x + c * sum.x;
+        base.y = v[0].y + c * sum.y;
+        Cx rot = c_scale(c_rot<SIGN>(dif), s);
+        v[0] = c_add(v[0], sum);
+        v[1] = c_add(base, rot);
+        v[2] = c_sub(base, rot);
+    }
+};
+
+template <typename T, int SIGN>
+struct Dft<T, 5, SIGN> {
+    template <typename Cx>
+    __device__ __forceinline__ static void run(Cx* v) {
+        const T c1 = T(0.30901699437494742410), c2 = T(-0.80901699437494742410);
+        const T s1 = T(0.95105651629515357212), s2 = T(0.58778525229247312917);
+        Cx p1 = c_add(v[1], v[4]), m1 = c_sub(v[1], v[4]);
+        Cx p2 = c_add(v[2], v[3]), m2 = c_sub(v[2], v[3]);
+        Cx b1, b2, q1, q2;
+        b1.x = v[0].x + c1 * p1.x + c2 * p2.x;
+        b1.y = v[0].y + c1 * p1.y + c2 * p2.y;
+        b2.x = v[0].x + c2 * p1.x + c1 * p2.x;
+        b2.y = v[0].y + c2 * p1.y + c1 * p2.y;
+        Cx d1, d2;
+        d1.x = s1 * m1.x + s2 * m2.x;
+        d1.y = s1 * m1.y + s2 * m2.y;
+        d2.x = s2 * m1.x - s1 * m2.x;
+        d2.y = s2 * m1.y - s1 * m2.y;
+        q1 = c_rot<SIGN>(d1);
+        q2 = c_rot<SIGN>(d2);
+        v[0] = c_add(v[0], c_add(p1, p2));
+        v[1] = c_add(b1, q1);
+        v[4] = c_sub(b1, q1);
+        v[2] = c_add(b2, q2);
+        v[3] = c_sub(b2, q2);
+    }
+};
+
+template <typename T, int SIGN>
+struct Dft<T, 7, SIGN> {
+    template <typename Cx>
+    __device__ __forceinline__ static void run(Cx* v) {
+        const T C[3] = {T(0.62348980185873353053), T(-0.22252093395631440429), T(-0.90096886790241912624)};
+        const T S[3] = {T(0.78183148246802980871), T(0.97492791218182360702), T(0.43388373911755812048)};
+        Cx p[3], m[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            p[j] = c_add(v[j + 1], v[6 - j]);
+            m[j] = c_sub(v[j + 1], v[6 - j]);
+        }
+        Cx y0 = v[0];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) y0 = c_add(y0, p[j]);
+        Cx out[7];
+        out[0] = y0;
+#pragma unroll
+        for (int k = 1; k <= 3; ++k) {
+            Cx b = v[0], d;
+            d.x = T(0);
+            d.y = T(0);
+#pragma unroll
+            for (int j = 1; j <= 3; ++j) {
+                const int idx = (j * k) % 7;  // cos/sin of 2 pi j k / 7
+                const int q = idx <= 3 ? idx : 7 - idx;
+                const T cs = C[q - 1];
+                const T sn = idx <= 3 ? S[q - 1] : -S[q - 1];
+                b.x += cs * p[j - 1].x;
+                b.y += cs * p[j - 1].y;
+                d.x += sn * m[j - 1].x;
+                d.y += sn * m[j - 1].y;
+            }
+            Cx r = c_rot<SIGN>(d);
+            out[k] = c_add(b, r);
+            out[7 - k] = c_sub(b, r);
+        }
+#pragma unroll
+        for (int k = 0; k < 7; ++k) v[k] = out[k];
+    }
+};
+
+// Points each thread holds per stage: 16 for power-of-two lengths, 8 when the
+// radices 3, 5 and 7 are in use (their register arrays share one allocation);
+// half of that in float64.
+template <typename T, bool MIXED>
+struct Ppt { static constexpr int value = MIXED ? 8 : 16; };
+template <bool MIXED>
+struct Ppt<double, MIXED> { static constexpr int value = MIXED ? 4 : 8; };
+
+constexpr int kFftThreads = 512;
+
+// One Stockham stage of radix R over all lines in shared memory.
+template <typename T, int R, int SIGN, bool MIXED>
+__device__ __forceinline__ void fft_stage(typename cplx<T>::type* buf, int M, int pitch, int lines, int Ns,
+                                          const typename cplx<T>::type* __restrict__ tw) {
+    using Cx = typename cplx<T>::type;
+    constexpr int BPT = Ppt<T, MIXED>::value / R > 0 ? Ppt<T, MIXED>::value / R : 1;
+    const int nb = M / R;
+    const int total = lines * nb;
+    const int stride = M / (Ns * R);
+    Cx v[BPT][R];
+    int dst[BPT];
+#pragma unroll
+    for (int i = 0; i < BPT; ++i) {
+        const int b = threadIdx.x + i * blockDim.x;
+        dst[i] = -1;
+        if (b < total) {
+            const int line = b / nb;
+            const int j = b - line * nb;
+            const int base = line * pitch;
+            const int k = j % Ns;
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[i][r] = buf[base + j + r * nb];
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                Cx w = tw[r * k * stride];
+                if (SIGN > 0) w.y = -w.y;
+                v[i][r] = c_mul(v[i][r], w);
+            }
+            Dft<T, R, SIGN>::run(v[i]);
+            dst[i] = base + (j / Ns) * Ns * R + k;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < BPT; ++i) {
+        if (dst[i] >= 0) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) buf[dst[i] + r * Ns] = v[i][r];
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, int SIGN, bool MIXED>
+__device__ __forceinline__ void fft_smem(typename cplx<T>::type* buf, const LineArgs<T>& a, int lines) {
+    int Ns = 1;
+    unsigned long long code = a.radix_code;
+#pragma unroll 1
+    for (int s = 0; s < a.nstages; ++s) {
+        const int R = (int)(code & 15ull);
+        code >>= 4;
+        if (R == 8) fft_stage<T, 8, SIGN, MIXED>(buf, a.M, a.pitch, lines, Ns, a.tw);
+        else if (R == 4) fft_stage<T, 4, SIGN, MIXED>(buf, a.M, a.pitch, lines, Ns, a.tw);
+        else if (R == 2) fft_stage<T, 2, SIGN, MIXED>(buf, a.M, a.pitch, lines, Ns, a.tw);
+        else if (MIXED) {
+            if (R == 3) fft_stage<T, 3, SIGN, MIXED>(buf, a.M, a.pitch, lines, Ns, a.tw);
+            else if (R == 5) fft_stage<T, 5, SIGN, MIXED>(buf, a.M, a.pitch, lines, Ns, a.tw);
+            else if (R == 7) fft_stage<T, 7, SIGN, MIXED>(buf, a.M, a.pitch, lines, Ns, a.tw);
+        }  // radices are validated at plan time
+        Ns *= R;
+    }
+}
+
+// grid: x = line blocks, y = batch.  SIGN = -1 forward, +1 inverse (of the main FFT).
+template <typename T, int SIGN, bool CONV, bool MIXED>
+__global__ void __launch_bounds__(kFftThreads) fft_line_kernel(const __grid_constant__ LineArgs<T> a) {
+    using Cx = typename cplx<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Cx* buf = reinterpret_cast<Cx*>(smem_raw);
+
+    const int l0 = blockIdx.x * a.lines_per_cta;
+    const int lines = min(a.lines_per_cta, a.nlines - l0);
+    if (lines <= 0) return;
+    const Cx* in = a.in + a.in_bs * blockIdx.y;
+    Cx* out = a.out + a.out_bs * blockIdx.y;
+    const Cx zero = make_c<T>(T(0), T(0));
+
+    // ---- load ----
+    const int nload = lines * a.M;
+    const bool line_fast = (a.in_es != 1);
+    for (int i = threadIdx.x; i < nload; i += blockDim.x) {
+        int ll, j;
+        if (line_fast) { ll = i % lines; j = i / lines; }
+        else { ll = i / a.M; j = i - ll * a.M; }
+        Cx val = zero;
+        if (j < a.n_log) {
+            int pa = j + a.load_add;
+            pa %= a.n_log;
+            if (pa < 0) pa += a.n_log;
+            const int p = pa - a.in_offset;
+            if (p >= 0 && p < a.in_count) {
+                const long long l = l0 + ll;
+                val = in[l * a.in_ls + (long long)p * a.in_es];
+                if (a.pre) val = c_mul(val, a.pre[l * a.pre_ls + p]);
+                if (a.chirp_in) val = c_mul(val, a.chirp_in[j]);
+            }
+        }
+        buf[ll * a.pitch + j] = val;
+    }
+    __syncthreads();
+
+    fft_smem<T, SIGN, MIXED>(buf, a, lines);
+
+    if (CONV) {
+        const int n = lines * a.M;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int ll = i / a.M;
+            const int k = i - ll * a.M;
+            Cx m = a.mid[(long long)(l0 + ll) * a.mid_ls + (long long)k * a.mid_es];
+            if (a.mid_conj) m.y = -m.y;
+            buf[ll * a.pitch + k] = c_mul(buf[ll * a.pitch + k], m);
+        }
+        __syncthreads();
+        fft_smem<T, -SIGN, MIXED>(buf, a, lines);
+    }
+
+    // ---- store ----
+    const int nstore = lines * a.out_count;
+    const bool line_fast_out = (a.out_es != 1);
+    for (int i = threadIdx.x; i < nstore; i += blockDim.x) {
+        int ll, kk;
+        if (line_fast_out) { ll = i % lines; kk = i / lines; }
+        else { ll = i / a.out_count; kk = i - ll * a.out_count; }
+        int src = (a.out_offset + kk + a.store_add) % a.out_mod;
+        if (src < 0) src += a.out_mod;
+        Cx val = c_mul(buf[ll * a.pitch + src], a.scale);
+        if (a.chirp_out) val = c_mul(val, a.chirp_out[src]);
+        const long long l = l0 + ll;
+        if (a.post) val = c_mul(val, a.post[l * a.post_ls + (long long)kk * a.post_es]);
+        out[l * a.out_ls + (long long)kk * a.out_es] = val;
+    }
+}
+
+}  // namespace hx

@@ -287,22 +287,24 @@ class _CostModel(object):
     """Predicted device time of each method; replaces the CPU-fitted coefficients of the reference
     planner (hcipy/fourier/fourier_transform.py:159-183, hcipy/config/default_config.yaml:10-44).
 
-    ``t = launch_overhead * launches + work / rate``; the rates are sustained
-    figures of this package's kernels on a GB300 and can be refreshed by
-    ``make_fourier_transform(..., planner='measure')``.
+    ``t = launches * launch_s + max(bytes / hbm_bytes, flops / rate)``: the MFT is
+    two complex GEMM launches at the FP32 CUDA-core rate measured on a GB300; a
+    zero-padded FFT or a zoom FFT is one line-FFT launch per axis, bound by the
+    HBM traffic of its source, intermediate and destination planes or by the
+    shared-memory butterflies.
     """
-    launch_s = 4e-6
-    mft_flops = 45e12       # FP32 CUDA-core complex GEMM
-    fft_bytes = 3.0e12      # bandwidth-bound Stockham passes
-    fft_flops = 20e12
+    launch_s = 3e-6
+    mft_flops = 30e12
+    fft_flops = 15e12
+    hbm_bytes = 5e12
 
     def mft_seconds(self, ops):
         return 2 * self.launch_s + ops / self.mft_flops
 
-    def fft_seconds(self, n_internal, n_in, n_out, itemsize=8):
-        traffic = (2 * n_internal + n_in + n_out) * itemsize * 2
-        flops = 5 * n_internal * max(math.log2(max(n_internal, 2)), 1)
-        return 3 * self.launch_s + max(traffic / self.fft_bytes, flops / self.fft_flops)
+    def fft_seconds(self, n_internal, n_in, n_out, passes=2, n_mid=0, itemsize=8):
+        traffic = (n_in + n_out + 2 * n_mid) * itemsize
+        flops = 5.0 * n_internal * max(math.log2(max(n_internal, 2)), 1)
+        return passes * self.launch_s + max(traffic / self.hbm_bytes, flops / self.fft_flops)
 
 
 cost_model = _CostModel()

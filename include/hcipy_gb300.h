@@ -113,6 +113,86 @@ HX_API int hx_mft_execute_ex(const hx_mft_plan* plan, int direction, int batch,
 
 HX_API int hx_mft_plan_destroy(hx_mft_plan* plan);
 
+/* ------------------------------------------------------------------------
+ * Zero-padded FFT with index fftshifts, crop and separable phase factors.
+ * Replaces FastFourierTransform (hcipy/fourier/fast_fourier_transform.py:223-406):
+ *   forward : out = crop_out( fftshift( FFT_N( ifftshift( pad_in(in * pre) ) ) ) ) * post * scale
+ *   backward: in  = crop_in( fftshift( IFFT_N( ifftshift( pad_out(out / post) ) ) ) ) / pre / scale
+ * per axis d (axis 0 = x, contiguous): the source is placed at offset in_offsets[d]
+ * of the padded length internal_dims[d] and the result is read from out_offsets[d]
+ * (the reference's cutouts, :261-275).  pre[d] (length in_dims[d]) and post[d]
+ * (length out_dims[d]) are host arrays of interleaved complex float64 or NULL:
+ * the per-axis factors of shift_output and shift_input (:277-321), whose product
+ * over the axes is the reference's phase array.  Lengths that are not products
+ * of 2, 3, 5 and 7 run Bluestein's algorithm.  ndim is 1 or 2.
+ * ------------------------------------------------------------------------ */
+typedef struct hx_fft_plan hx_fft_plan;
+
+HX_API int hx_fft_plan_create(int ndim, const int* in_dims, const int* internal_dims, const int* out_dims,
+                       const int* in_offsets, const int* out_offsets,
+                       const double* const* pre, const double* const* post,
+                       double scale_re, double scale_im, int dtype, void* stream, hx_fft_plan** plan);
+HX_API size_t hx_fft_workspace_bytes(const hx_fft_plan* plan, int direction, int batch);
+/* direction HX_FORWARD (input plane -> output plane) or HX_BACKWARD. */
+HX_API int hx_fft_execute(const hx_fft_plan* plan, int direction, int batch, const void* in, void* out,
+                   void* workspace, size_t workspace_bytes, void* stream);
+HX_API int hx_fft_plan_destroy(hx_fft_plan* plan);
+
+/* ------------------------------------------------------------------------
+ * Fourier filter: zero-pad to internal_dims, FFT, multiply by the transfer
+ * function (conjugated when adjoint != 0), inverse FFT, crop.
+ * Replaces FourierFilter.forward/backward (hcipy/fourier/fourier_operations.py:59-151).
+ * transfer_function is a DEVICE array of the plan's dtype in FFT order (the
+ * reference's ifftshifted transfer function, :47-48), copied into the plan.
+ * The 2-D form is three launches: row FFTs, column FFT x TF x inverse FFT,
+ * inverse row FFTs of the kept rows.
+ * ------------------------------------------------------------------------ */
+typedef struct hx_filter_plan hx_filter_plan;
+
+HX_API int hx_filter_plan_create(int ndim, const int* in_dims, const int* internal_dims, const int* in_offsets,
+                          const void* transfer_function, int dtype, void* stream, hx_filter_plan** plan);
+HX_API size_t hx_filter_workspace_bytes(const hx_filter_plan* plan, int batch);
+HX_API int hx_filter_execute(const hx_filter_plan* plan, int adjoint, int batch, const void* in, void* out,
+                      void* workspace, size_t workspace_bytes, void* stream);
+HX_API int hx_filter_plan_destroy(hx_filter_plan* plan);
+
+/* ------------------------------------------------------------------------
+ * Chirp-Z transform X_k = sum_n x_n (a w^-k)^-n, k < m, along lines of a
+ * strided array, by Bluestein's algorithm in one launch.
+ * Replaces ChirpZTransform (hcipy/fourier/chirp_z_transform.py:39-105); the
+ * optional host arrays pre (length n) and post (length m, interleaved complex
+ * float64) multiply the input and output, which is how ZoomFastFourierTransform
+ * (hcipy/fourier/zoom_fast_fourier_transform.py:69-119) folds its weights and shifts in.
+ * ------------------------------------------------------------------------ */
+typedef struct hx_czt_plan hx_czt_plan;
+
+HX_API int hx_czt_plan_create(int n, int m, double w_re, double w_im, double a_re, double a_im,
+                       const double* pre, const double* post, int dtype, void* stream, hx_czt_plan** plan);
+HX_API int hx_czt_execute(const hx_czt_plan* plan, int nlines, int batch,
+                   const void* in, long long in_line_stride, long long in_elem_stride, long long in_batch_stride,
+                   void* out, long long out_line_stride, long long out_elem_stride, long long out_batch_stride,
+                   void* stream);
+HX_API int hx_czt_plan_destroy(hx_czt_plan* plan);
+
+/* ------------------------------------------------------------------------
+ * Angular-spectrum transfer function exp(i sqrt(k^2 - kx^2 - ky^2 + 0j) d),
+ * averaged over oversampling^2 dithered sub-samples, evaluated in float64 on
+ * the padded FFT grid (zero, delta per axis) and written in FFT order.
+ * Replaces transfer_function_native with evaluate_supersampled
+ * (hcipy/propagation/angular_spectrum.py:159-166, hcipy/field/util.py:655-692).
+ * ------------------------------------------------------------------------ */
+HX_API int hx_asp_transfer_function(int nx, int ny, double zero_x, double zero_y, double delta_x, double delta_y,
+                             double wavenumber, double distance, int oversampling, int dtype, void* out,
+                             void* stream);
+
+/* Impulse response cos(theta)/(2 pi) exp(i k r) (1/r^2 - i k/r), r^2 = x^2 + y^2 + d^2,
+ * averaged over oversampling^2 dithers, on a regular grid (zero, delta), grid order;
+ * the transfer function of the other branch is its FFT
+ * (hcipy/propagation/angular_spectrum.py:143-157). */
+HX_API int hx_asp_impulse_response(int nx, int ny, double zero_x, double zero_y, double delta_x, double delta_y,
+                            double wavenumber, double distance, int oversampling, int dtype, void* out,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -185,7 +185,8 @@ def make_asp_cases(hp, out):
     rng = np.random.default_rng(44)
     recs = {}
     # The native transfer-function branch (large distance relative to sampling is the other branch).
-    for i, (n, diam, wl, d) in enumerate([(64, 8.0, 1.6e-6, 0.5), (48, 8.0, 1.6e-6, 5.0), (40, 2e-3, 500e-9, 0.05)]):
+    for i, (n, diam, wl, d) in enumerate([(64, 8.0, 1.6e-6, 0.5), (48, 8.0, 1.6e-6, 5.0), (40, 2e-3, 500e-9, 0.05),
+                                          (32, 1e-3, 1e-6, 1.0)]):
         pupil = hp.make_pupil_grid(n, diam)
         aperture = hp.make_circular_aperture(diam * 0.9)(pupil)
         e = aperture * np.exp(1j * rng.standard_normal(pupil.size) * 0.3)

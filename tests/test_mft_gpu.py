@@ -172,7 +172,8 @@ def test_errors_and_fault_injection(monkeypatch):
     with pytest.raises(hg.HXError):
         mft.forward(torch.zeros(256, dtype=torch.complex64, device='cuda'))
     monkeypatch.delenv('HX_FAULT')
-    assert mft.forward(torch.ones(256, dtype=torch.complex64, device='cuda')).shape == (64,)
+    # make_focal_grid(2, 4) is 16 x 16.
+    assert mft.forward(torch.ones(256, dtype=torch.complex64, device='cuda')).shape == (256,)
 
 
 def test_inputs_are_not_modified():

@@ -94,7 +94,7 @@ def test_fourier_filter_oracle():
     assert rel_err(plan.apply(g['E'], adjoint=True), g['bwd_c128']) < 1e-13
 
 
-@pytest.mark.parametrize('case', ['asp_0', 'asp_1', 'asp_2'])
+@pytest.mark.parametrize('case', ['asp_0', 'asp_1', 'asp_2', 'asp_3'])
 def test_asp_oracle(case):
     g = load_golden(case)
     pupil = grids.make_pupil_grid(int(g['n']), float(g['diam']))
