@@ -14,7 +14,7 @@ import torch
 from . import _lib
 from .field import Field, as_tensor, complex_dtype_for
 from .fourier import (FourierTransform, ComputationalComplexity, make_fft_grid, get_fft_parameters, _is_cartesian,
-                      _prepare_input, cost_model, _as_tuple)
+                      _prepare_input, cost_model, reference_seconds)
 
 
 def _grid_axes(grid):
@@ -166,10 +166,16 @@ class FastFourierTransform(FourierTransform):
         cadd = n_int * math.log2(n_int)
         mults = 4 * cmul
         adds = 2 * cmul + 2 * cadd
+        return ComputationalComplexity(mults, adds, reference_seconds('fft', mults + adds))
+
+    @classmethod
+    def gpu_execution_time(cls, input_grid, output_grid):
+        """GB300 estimate: one line-FFT launch per axis, bound by HBM traffic or butterflies."""
+        q, _, _ = get_fft_parameters(output_grid, input_grid)
+        n_int = math.prod(n * qq for n, qq in zip(input_grid.dims, q))
         ndim = input_grid.ndim
-        n_mid = input_grid.shape[0] * output_grid.dims[0] if ndim == 2 else 0
-        secs = cost_model.fft_seconds(n_int, n_in, n_out, passes=ndim, n_mid=n_mid)
-        return ComputationalComplexity(mults, adds, secs)
+        n_mid = int(np.asarray(input_grid.dims)[1]) * int(output_grid.dims[0]) if ndim == 2 else 0
+        return cost_model.fft_seconds(n_int, input_grid.size, output_grid.size, passes=ndim, n_mid=n_mid)
 
 
 # ---------------------------------------------------------------------------
@@ -314,10 +320,29 @@ class ZoomFastFourierTransform(FourierTransform):
 
     @classmethod
     def compute_complexity(cls, input_grid, output_grid):
-        """Operation count of zoom_fast_fourier_transform.py:147-219 and a GB300 time estimate."""
+        """Operation count and predicted time as the reference planner computes them
+        (zoom_fast_fourier_transform.py:147-219; its CZT length is scipy's next_fast_len)."""
+        import scipy.fft
         cls.check_if_supported(input_grid, output_grid)
         cmul = input_grid.size
         cadd = 0
+        ins = [int(d) for d in np.asarray(input_grid.shape)]
+        outs = [int(d) for d in np.asarray(output_grid.shape)]
+        for i in range(len(ins)):
+            L = scipy.fft.next_fast_len(ins[i] + outs[i] - 1)
+            per = math.prod(outs[:i]) * math.prod(ins[i + 1:])
+            before = math.prod(outs[:i]) * math.prod(ins[i:])
+            after = math.prod(outs[:i + 1]) * math.prod(ins[i + 1:])
+            cmul += before + 0.5 * L * per * math.log2(L) + L * per + 0.5 * L * per * math.log2(L) + 2 * after
+            cadd += 2 * L * per * math.log2(L)
+        mults = 4 * cmul
+        adds = 2 * cmul + 2 * cadd
+        return ComputationalComplexity(mults, adds, reference_seconds('zfft', mults + adds))
+
+    @classmethod
+    def gpu_execution_time(cls, input_grid, output_grid):
+        """GB300 estimate: one chirp-Z launch per axis (power-of-two Bluestein length)."""
+        cls.check_if_supported(input_grid, output_grid)
         secs = 0
         ins = [int(d) for d in input_grid.dims]
         outs = [int(d) for d in output_grid.dims]
@@ -326,10 +351,8 @@ class ZoomFastFourierTransform(FourierTransform):
             per = math.prod(outs[:i]) * math.prod(ins[i + 1:])
             before = math.prod(outs[:i]) * math.prod(ins[i:])
             after = math.prod(outs[:i + 1]) * math.prod(ins[i + 1:])
-            cmul += before + L * per * (1 + math.log2(L)) + 2 * after
-            cadd += 2 * L * per * math.log2(L)
             secs += cost_model.fft_seconds(2 * L * per, before, after, passes=1)
-        return ComputationalComplexity(4 * cmul, 2 * cmul + 2 * cadd, secs)
+        return secs
 
 
 # ---------------------------------------------------------------------------

@@ -263,19 +263,58 @@ class MatrixFourierTransform(FourierTransform):
 
     @classmethod
     def compute_complexity(cls, input_grid, output_grid):
-        """Operation count of the two GEMMs (matrix_fourier_transform.py:256-310) and a GB300 time estimate."""
+        """Operation count and predicted time as the reference planner computes them
+        (matrix_fourier_transform.py:256-310), so ``planner='estimate'`` makes the reference's choice."""
+        cls.check_if_supported(input_grid, output_grid)
+        mults, adds = _mft_operation_count(input_grid, output_grid)
+        return ComputationalComplexity(mults, adds, reference_seconds('mft', mults + adds))
+
+    @classmethod
+    def gpu_execution_time(cls, input_grid, output_grid):
+        """GB300 time estimate: two complex GEMM launches at the CUDA-core rate."""
         cls.check_if_supported(input_grid, output_grid)
         if input_grid.ndim == 1:
-            cmul = input_grid.size * output_grid.size
-            cadd = (input_grid.size - 1) * output_grid.size
+            cmacs = input_grid.size * output_grid.size
         else:
             nx, ny = (int(d) for d in input_grid.dims)
             nu, nv = (int(d) for d in output_grid.dims)
-            cmul = ny * nx * nu + nv * ny * nu + input_grid.size
-            cadd = nu * ny * (nx - 1) + nv * nu * (ny - 1)
-        mults = 4 * cmul
-        adds = 2 * cmul + 2 * cadd
-        return ComputationalComplexity(mults, adds, cost_model.mft_seconds(mults + adds))
+            cmacs = ny * nx * nu + nv * ny * nu
+        return cost_model.mft_seconds(8 * cmacs)
+
+
+def _mft_operation_count(input_grid, output_grid):
+    """Real multiplications and additions of the MFT as the reference counts them.
+
+    The reference unpacks ``grid.shape`` (which is (Ny, Nx)) into names ordered
+    (x, y), so its count uses Nx_in*Ny_in*Nx_out + Ny_in*Ny_out*Nx_out; that order
+    is kept so that the planner's choices match.
+    """
+    if input_grid.ndim == 1:
+        cmul = input_grid.size * output_grid.size
+        cadd = (input_grid.size - 1) * output_grid.size
+    else:
+        ny_in, nx_in = (int(d) for d in np.asarray(input_grid.dims)[::-1])
+        ny_out, nx_out = (int(d) for d in np.asarray(output_grid.dims)[::-1])
+        a_in, b_in = ny_in, nx_in      # the reference's (N_in_x, N_in_y)
+        a_out, b_out = ny_out, nx_out  # the reference's (N_out_x, N_out_y)
+        cmul = b_in * a_in * b_out + a_in * a_out * b_out + input_grid.size
+        cadd = b_out * a_in * (b_in - 1) + a_out * b_out * (a_in - 1)
+    return 4 * cmul, 2 * cmul + 2 * cadd
+
+
+# Execution-time model of the reference planner, t_ms = exp(a) * GFLOP^b + exp(c), with the
+# coefficients of its default configuration (hcipy/config/default_config.yaml:10-44,
+# fitted by the reference on its CPU; hcipy/fourier/fourier_transform.py:159-183).
+REFERENCE_TIME_COEFFICIENTS = {
+    'fft': (3.746, 0.881, -4.749),
+    'mft': (1.667, 0.716, -4.624),
+    'zfft': (4.093, 0.847, -2.973),
+}
+
+
+def reference_seconds(method, num_operations):
+    a, b, c = REFERENCE_TIME_COEFFICIENTS[method]
+    return (math.exp(a) * (num_operations / 1e9)**b + math.exp(c)) * 1e-3
 
 
 # ---------------------------------------------------------------------------
@@ -385,7 +424,13 @@ def is_fft_grid(grid, input_grid):
 
 
 def make_fourier_transform(input_grid, output_grid=None, q=1, fov=1, shift=0, planner='estimate'):
-    """Choose and construct the fastest Fourier operator (hcipy/fourier/fourier_transform.py:217-300)."""
+    """Choose and construct a Fourier operator (hcipy/fourier/fourier_transform.py:217-300).
+
+    ``planner='estimate'`` (default) ranks the methods with the reference's own
+    operation counts and time model, so a drop-in user gets the method the
+    reference would pick (and its numerical behaviour); ``'gpu'`` ranks them with
+    the GB300 cost model of this package; ``'measure'`` times each on the device.
+    """
     options = {'mft': MatrixFourierTransform}
     try:
         from .fft import FastFourierTransform, ZoomFastFourierTransform
@@ -407,12 +452,14 @@ def make_fourier_transform(input_grid, output_grid=None, q=1, fov=1, shift=0, pl
             continue
         if planner == 'estimate':
             expected[method] = ft.compute_complexity(input_grid, output_grid).expected_execution_time
+        elif planner == 'gpu':
+            expected[method] = ft.gpu_execution_time(input_grid, output_grid)
         elif planner == 'measure':
             obj = ft(input_grid, q, fov, shift) if method == 'fft' else ft(input_grid, output_grid)
             a = torch.zeros(input_grid.size, dtype=torch.complex64, device='cuda')
             expected[method] = _time_device(lambda: obj.forward(a))
         else:
-            raise ValueError('planner must be "estimate" or "measure"')
+            raise ValueError('planner must be "estimate", "gpu" or "measure"')
     if not expected:
         raise ValueError('No Fourier transform supports these grids (unstructured grids need a naive DFT).')
     best = min(expected, key=expected.get)
