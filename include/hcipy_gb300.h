@@ -113,6 +113,20 @@ HX_API int hx_mft_execute_ex(const hx_mft_plan* plan, int direction, int batch,
 
 HX_API int hx_mft_plan_destroy(hx_mft_plan* plan);
 
+/* No counterpart in the reference.  The same transform as hx_mft_execute for
+ * callers that cannot allocate device memory while they run (a real-time loop
+ * that must not stall on an allocator, a host framework or plugin ABI that hands
+ * over only input and output buffers): the intermediate of the two GEMMs lives in
+ * a static device array of HX_MFT_NOALLOC_SCRATCH_BYTES compiled into the library
+ * (one per GPU that loads it, held until exit) instead of a caller workspace.
+ * The call allocates nothing.  Its first call on a device looks up the array's
+ * device address, so make that first call before any stream capture.  A batch
+ * whose scratch need (hx_mft_workspace_bytes) exceeds the array is rejected with
+ * HX_ERR_INVALID.  All calls share the array: calls that overlap on the GPU race. */
+#define HX_MFT_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
+HX_API int hx_mft_execute_noalloc(const hx_mft_plan* plan, int direction, int batch,
+                           const void* in, void* out, double alpha_re, double alpha_im, void* stream);
+
 /* ------------------------------------------------------------------------
  * Zero-padded FFT with index fftshifts, crop and separable phase factors.
  * Replaces FastFourierTransform (hcipy/fourier/fast_fourier_transform.py:223-406):
