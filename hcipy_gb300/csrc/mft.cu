@@ -174,9 +174,7 @@ int hx_mft_plan_create(int nx, int ny, int nu, int nv, const double* x, const do
             if ((rc = gen_matrix(dtype, nu, nx, du, dx, +1.0, nullptr, dwx, &p->m2a, stream))) break;
         }
         if (precision == HX_PREC_SPLIT) {
-            if ((rc = hx::split_mft_create(nx, ny, nu, nv, (const float2*)p->m1f, (const float2*)p->m2f,
-                                           (const float2*)p->m1b, (const float2*)p->m2b, (const float2*)p->m1a,
-                                           (const float2*)p->m2a, stream, &p->split)))
+            if ((rc = hx::split_mft_create(nx, ny, nu, nv, dx, dy, du, dv, dwx, dwy, dwu, dwv, stream, &p->split)))
                 break;
         }
     } while (false);
@@ -225,6 +223,12 @@ int hx_mft_execute_ex(const hx_mft_plan* p, int direction, int batch, const void
     if (p->dtype == HX_C64)
         return execute_t<float>(p, direction, batch, in, out, are, aim, epilogue, mask, src, ws, stream);
     return execute_t<double>(p, direction, batch, in, out, are, aim, epilogue, mask, src, ws, stream);
+}
+
+int hx_mft_plan_status(const hx_mft_plan* p, int reset) {
+    HX_CHECK_ARG(p != nullptr, "hx_mft_plan_status: plan is NULL");
+    if (p->precision != HX_PREC_SPLIT) return HX_OK;
+    return hx::split_mft_status(p->split, reset);
 }
 
 int hx_mft_plan_destroy(hx_mft_plan* p) {

@@ -156,6 +156,10 @@ class _MftPlan(object):
                                         _lib.dptr(workspace), nbytes, _lib.stream_handle())
         _lib.check(rc, 'hx_mft_execute_ex')
 
+    def status(self, reset=True):
+        """Status of the plan's bounded device waits (0 = fine); synchronizes with the device."""
+        return int(self.lib.hx_mft_plan_status(self.handle, 1 if reset else 0))
+
     def __del__(self):
         try:
             if self.handle:

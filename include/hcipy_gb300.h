@@ -113,6 +113,11 @@ HX_API int hx_mft_execute_ex(const hx_mft_plan* plan, int direction, int batch,
 
 HX_API int hx_mft_plan_destroy(hx_mft_plan* plan);
 
+/* Status of the plan's bounded device-side waits since the last reset: HX_OK, or
+ * HX_ERR_TIMEOUT when a wait of the tensor-core GEMM gave up (its CTA then
+ * returned without writing).  Synchronizes with the device; reset != 0 clears it. */
+HX_API int hx_mft_plan_status(const hx_mft_plan* plan, int reset);
+
 /* No counterpart in the reference.  The same transform as hx_mft_execute for
  * callers that cannot allocate device memory while they run (a real-time loop
  * that must not stall on an allocator, a host framework or plugin ABI that hands

@@ -1,0 +1,111 @@
+"""The split-operand tcgen05 MFT (precision='split') against the float64 oracle and its arithmetic model.
+
+The split form cuts every operand into fixed-point slices (6, 11, 11 bits) and
+sums the kept slice products exactly, so its error does not grow with the
+transform length as FP32 accumulation does.  Tolerances:
+  device result vs the numpy model of the split arithmetic : 1e-12 relative (same arithmetic)
+  MFT fields, relative L2 vs float64                       : 1e-7 (~2^-29 per element, then complex64 output)
+  Lyot dark hole (3-15 lambda/D), 512^2 pupil              : max |NI - NI_fp64| < 1.5e-11 and < 1/5 of FP32's
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import load_golden, rel_err
+import split_model
+from oracle import fourier as ofourier, optics as ooptics
+from oracle.grids import RegularGrid
+
+pytestmark = pytest.mark.gpu
+
+hg = pytest.importorskip('hcipy_gb300')
+
+
+def regular(g, prefix):
+    return hg.CartesianGrid(hg.RegularCoords(g[prefix + '_delta'], g[prefix + '_dims'], g[prefix + '_zero']))
+
+
+def og(grid):
+    return RegularGrid(grid.delta, grid.dims, grid.zero)
+
+
+def test_split_mft_forward_small():
+    g = load_golden('mft_0')
+    pupil, focal = regular(g, 'ingrid'), regular(g, 'outgrid')
+    e = torch.from_numpy(g['E'].astype(np.complex64)).cuda()
+    split = hg.MatrixFourierTransform(pupil, focal, precision='split')
+    out = split.forward(e).numpy()
+    ref = ofourier.mft_forward(e.cpu().numpy().astype(complex), g['in_x'], g['in_y'], g['out_x'], g['out_y'],
+                               pupil.weights)
+    assert split._plan(torch.complex64).status() == 0
+    model = split_model.mft_forward(e.cpu().numpy(), g['in_x'], g['in_y'], g['out_x'], g['out_y'], pupil.weights)
+    # The device computes the model's arithmetic; only the complex64 output rounding remains.
+    assert rel_err(out, model.astype(np.complex64)) < 1e-12
+    assert rel_err(out, ref) < 1e-7
+
+
+@pytest.mark.parametrize('case', ['mft_0', 'mft_1', 'mft_2'])
+def test_split_mft_all_directions(case):
+    g = load_golden(case)
+    pupil, focal = regular(g, 'ingrid'), regular(g, 'outgrid')
+    x, y, u, v = g['in_x'], g['in_y'], g['out_x'], g['out_y']
+    e = g['E'].astype(np.complex64)
+    f = g['F'].astype(np.complex64)
+    split = hg.MatrixFourierTransform(pupil, focal, precision='split')
+    plain = hg.MatrixFourierTransform(pupil, focal)
+    checks = [
+        (split.forward(e), plain.forward(e), ofourier.mft_forward(e.astype(complex), x, y, u, v, pupil.weights)),
+        (split.backward(f), plain.backward(f), ofourier.mft_backward(f.astype(complex), x, y, u, v, focal.weights)),
+        (split.adjoint(f), plain.adjoint(f), ofourier.mft_adjoint(f.astype(complex), x, y, u, v, pupil.weights)),
+    ]
+    for got, fp32, ref in checks:
+        assert rel_err(got.numpy(), ref) < 1e-7
+    assert split._plan(torch.complex64).status() == 0
+
+
+def test_split_mft_batched_and_nonuniform():
+    rng = np.random.default_rng(3)
+    xg = np.sort(rng.uniform(-0.5, 0.5, 70))
+    yg = np.sort(rng.uniform(-0.5, 0.5, 66))
+    ug = np.linspace(-30, 30, 90)
+    vg = np.linspace(-25, 28, 71)
+    gi = hg.CartesianGrid(hg.SeparatedCoords([xg, yg]))
+    go = hg.CartesianGrid(hg.SeparatedCoords([ug, vg]))
+    split = hg.MatrixFourierTransform(gi, go, precision='split')
+    e = (rng.standard_normal((2, 3, gi.size)) + 1j * rng.standard_normal((2, 3, gi.size))).astype(np.complex64)
+    out = split.forward(e).numpy()
+    for i in range(2):
+        for j in range(3):
+            ref = ofourier.mft_forward(e[i, j].astype(complex), xg, yg, ug, vg, gi.weights)
+            assert rel_err(out[i, j], ref) < 1e-7
+    f = (rng.standard_normal((4, go.size)) + 1j * rng.standard_normal((4, go.size))).astype(np.complex64)
+    back = split.backward(f).numpy()
+    for i in range(4):
+        ref = ofourier.mft_backward(f[i].astype(complex), xg, yg, ug, vg, go.weights)
+        assert rel_err(back[i], ref) < 1e-7
+    assert split._plan(torch.complex64).status() == 0
+
+
+def _lyot_ni_errors(n):
+    from hcipy_gb300 import workloads
+    w = workloads.lyot_workload(pupil_n=n)
+    pupil, fpm_grid, focal = w['pupil'], w['fpm_grid'], w['focal']
+    chain64 = ooptics.LyotChain(og(pupil), og(fpm_grid), og(focal), w['fpm'], w['stop'])
+    ref = chain64(w['E'])
+    peak = np.abs(chain64.image(w['aperture'].astype(complex))).max()**2
+    mask = workloads.dark_hole_mask(focal)
+    errs = {}
+    for precision in ('fp32', 'split'):
+        lyot = hg.LyotCoronagraph(pupil, hg.Field(w['fpm'], fpm_grid), hg.Field(w['stop'], pupil),
+                                  precision=precision)
+        prop = hg.FraunhoferPropagator(pupil, focal, precision=precision)
+        img = prop(lyot(hg.Wavefront(hg.Field(w['E'].astype(np.complex64), pupil), 1.0))).electric_field.numpy()
+        d = np.abs(np.abs(img.astype(complex))**2 - np.abs(ref)**2)[mask] / peak
+        errs[precision] = (d.max(), d.mean())
+    return errs
+
+
+def test_split_lyot_dark_hole_512():
+    errs = _lyot_ni_errors(512)
+    assert errs['split'][0] < 1.5e-11, errs
+    assert errs['split'][0] < errs['fp32'][0] / 5, errs
