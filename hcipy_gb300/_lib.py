@@ -53,6 +53,12 @@ SIGNATURES = {
                                   c_void_p, c_void_p, c_size_t, c_void_p]),
     'hx_mft_plan_destroy': (c_int, [c_void_p]),
     'hx_mft_plan_status': (c_int, [c_void_p, c_int]),
+    'hx_mft_execute_io': (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_double, c_double, c_int,
+                                  c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
+    'hx_lyot_workspace_bytes': (c_size_t, [c_void_p, c_void_p, c_int]),
+    'hx_lyot_execute': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p, c_double, c_double,
+                                c_double, c_double, c_double, c_double, c_void_p, c_int, c_void_p, c_int, c_void_p,
+                                c_size_t, c_void_p]),
     'hx_mft_execute_noalloc': (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_double, c_double, c_void_p]),
     'hx_fft_plan_create': (c_int, [c_int, P(c_int), P(c_int), P(c_int), P(c_int), P(c_int), P(P(c_double)),
                                    P(P(c_double)), c_double, c_double, c_int, c_void_p, P(c_void_p)]),

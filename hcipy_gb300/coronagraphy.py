@@ -15,11 +15,13 @@ class LyotCoronagraph(OpticalElement):
     forward (lyot.py:66-92):  E_f = P(E);  E_f <- E_f - M E_f;  L = P^-1(E_f);  L <- E - L;  L <- S L.
 
     When the focal-plane mask and the Lyot stop are fields and the propagator
-    uses a matrix Fourier transform, the chain is two MFT launches pairs:
-    the mask product ``E_f (1 - M)`` is the epilogue of the forward MFT's
-    last GEMM, and ``S (E - L)`` is the epilogue of the inverse MFT's last
-    GEMM, so no intermediate field is re-read.  Other masks (optical
-    elements) run the same steps one operator at a time.
+    uses a matrix Fourier transform, the chain is one library call
+    (``hx_lyot_execute``): the mask product ``E_f (1 - M)`` is the epilogue of
+    the forward MFT's last GEMM, and ``S (E - L)`` the epilogue of the inverse
+    MFT's last GEMM.  With ``precision='split'`` the focal-plane field stays in
+    float-float between the transforms and the Lyot plane is returned as
+    complex128.  Other masks (optical elements) run the same steps one
+    operator at a time.
     """
 
     def __init__(self, input_grid, focal_plane_mask, lyot_stop=None, focal_length=1, focal_plane_mask_grid=None,
@@ -44,6 +46,8 @@ class LyotCoronagraph(OpticalElement):
         self._masks = {}
 
     def _fused_masks(self, dtype):
+        if self.prop.precision == 'split':
+            dtype = torch.complex64
         m = self._masks.get(dtype)
         if m is None:
             fpm = as_tensor(self._fpm_field).to(dtype).reshape(-1)
@@ -66,14 +70,24 @@ class LyotCoronagraph(OpticalElement):
         ft = inst.fourier_transform
         e = wavefront.electric_field
         t = as_tensor(e).contiguous()
+        split = ft.precision == 'split'
         one_minus, stop = self._fused_masks(t.dtype)
         a_fwd = complex(ft._w_in_scalar) * inst.norm_factor
         a_bwd = complex(ft._w_out_scalar / (2 * np.pi)**ft.ndim) / inst.norm_factor
-        ef = ft._run(t, ft.input_grid, ft.output_grid, _lib.HX_FORWARD, a_fwd, epilogue=_lib.HX_EPI_MUL,
-                     mask=one_minus)
-        lyot = ft._run(ef.data, ft.output_grid, ft.input_grid, _lib.HX_BACKWARD, a_bwd,
-                       epilogue=_lib.HX_EPI_BABINET, mask=stop, src=t)
-        return Wavefront(Field(lyot.data, e.grid), wavefront.wavelength)
+        lead = tuple(t.shape[:-1])
+        batch = int(np.prod(lead)) if lead else 1
+        out = torch.empty(lead + (t.shape[-1],), dtype=torch.complex128 if split else t.dtype, device=t.device)
+        plan = ft._plan(t.dtype)
+        lib = _lib.lib()
+        nbytes = int(lib.hx_lyot_workspace_bytes(plan.handle, None, batch))
+        ws = _lib.workspace(nbytes, t.device)
+        rc = lib.hx_lyot_execute(plan.handle, None, batch, _lib.dptr(t), _lib.dtype_code(t.dtype),
+                                 _lib.dptr(one_minus), None if stop is None else _lib.dptr(stop),
+                                 a_fwd.real, a_fwd.imag, a_bwd.real, a_bwd.imag, 0.0, 0.0,
+                                 _lib.dptr(out), _lib.dtype_code(out.dtype), None, _lib.HX_C64,
+                                 _lib.dptr(ws), nbytes, _lib.stream_handle())
+        _lib.check(rc, 'hx_lyot_execute')
+        return Wavefront(Field(out, e.grid), wavefront.wavelength)
 
     def _forward_unfused(self, wavefront):
         wf_foc = self.prop.forward(wavefront)

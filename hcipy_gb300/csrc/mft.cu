@@ -12,6 +12,7 @@
 #include "gemm_simt.cuh"
 #include "mft_tc.cuh"
 
+#include <algorithm>
 #include <vector>
 
 struct hx_mft_plan {
@@ -218,11 +219,89 @@ int hx_mft_execute_ex(const hx_mft_plan* p, int direction, int batch, const void
     if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
     cudaStream_t stream = (cudaStream_t)stream_;
     if (p->precision == HX_PREC_SPLIT)
-        return hx::split_mft_execute(p->split, direction, batch, (const float2*)in, (float2*)out, are, aim, epilogue,
-                                     (const float2*)mask, (const float2*)src, ws, ws_bytes, stream);
+        return hx::split_mft_execute(p->split, direction, batch, in, HX_C64, out, HX_C64, are, aim, epilogue,
+                                     (const float2*)mask, src, HX_C64, ws, ws_bytes, stream);
     if (p->dtype == HX_C64)
         return execute_t<float>(p, direction, batch, in, out, are, aim, epilogue, mask, src, ws, stream);
     return execute_t<double>(p, direction, batch, in, out, are, aim, epilogue, mask, src, ws, stream);
+}
+
+int hx_mft_execute_io(const hx_mft_plan* p, int direction, int batch, const void* in, int in_dtype, void* out,
+                      int out_dtype, double are, double aim, int epilogue, const void* mask, const void* src,
+                      int src_dtype, void* ws, size_t ws_bytes, void* stream) {
+    HX_CHECK_ARG(p != nullptr, "hx_mft_execute_io: plan is NULL");
+    const bool ok_t = (in_dtype == HX_C64 || in_dtype == HX_C128) && (out_dtype == HX_C64 || out_dtype == HX_C128) &&
+                      (src_dtype == HX_C64 || src_dtype == HX_C128);
+    HX_CHECK_ARG(ok_t, "hx_mft_execute_io: dtypes must be HX_C64 or HX_C128");
+    if (p->precision != HX_PREC_SPLIT) {
+        HX_CHECK_ARG(in_dtype == p->dtype && out_dtype == p->dtype && src_dtype == p->dtype,
+                     "hx_mft_execute_io: a plain plan reads and writes its own dtype");
+        return hx_mft_execute_ex(p, direction, batch, in, out, are, aim, epilogue, mask, src, ws, ws_bytes, stream);
+    }
+    HX_CHECK_ARG(direction == HX_FORWARD || direction == HX_BACKWARD || direction == HX_ADJOINT,
+                 "hx_mft_execute_io: unknown direction %d", direction);
+    HX_CHECK_ARG(batch >= 1 && in && out, "hx_mft_execute_io: bad batch or NULL field");
+    HX_CHECK_ARG(epilogue != HX_EPI_MUL || mask != nullptr, "hx_mft_execute_io: HX_EPI_MUL needs a mask");
+    HX_CHECK_ARG(epilogue != HX_EPI_BABINET || src != nullptr, "hx_mft_execute_io: HX_EPI_BABINET needs src");
+    const size_t need = hx_mft_workspace_bytes(p, direction, batch);
+    HX_CHECK_ARG(ws != nullptr && ws_bytes >= need, "hx_mft_execute_io: workspace of %zu bytes needed", need);
+    if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
+    return hx::split_mft_execute(p->split, direction, batch, in, in_dtype, out, out_dtype, are, aim, epilogue,
+                                 (const float2*)mask, src, src_dtype, ws, ws_bytes, (cudaStream_t)stream);
+}
+
+size_t hx_lyot_workspace_bytes(const hx_mft_plan* fpm, const hx_mft_plan* img, int batch) {
+    if (!fpm || batch <= 0) return 0;
+    if (fpm->precision == HX_PREC_SPLIT)
+        return hx::split_lyot_workspace_bytes(fpm->split, img ? img->split : nullptr, batch);
+    const size_t es = fpm->esize;
+    size_t mft = std::max(hx_mft_workspace_bytes(fpm, HX_FORWARD, batch), hx_mft_workspace_bytes(fpm, HX_BACKWARD, batch));
+    if (img) mft = std::max(mft, hx_mft_workspace_bytes(img, HX_FORWARD, batch));
+    const size_t focal = es * (size_t)batch * fpm->nu * fpm->nv;
+    const size_t pupil = es * (size_t)batch * fpm->nx * fpm->ny;
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    return up(focal) + up(pupil) + up(mft);
+}
+
+int hx_lyot_execute(const hx_mft_plan* fpm, const hx_mft_plan* img, int batch, const void* e, int e_dtype,
+                    const void* one_minus_fpm, const void* stop, double af_re, double af_im, double ab_re,
+                    double ab_im, double ai_re, double ai_im, void* lyot_out, int lyot_dtype, void* image_out,
+                    int image_dtype, void* ws, size_t ws_bytes, void* stream_) {
+    HX_CHECK_ARG(fpm != nullptr && e != nullptr && one_minus_fpm != nullptr, "hx_lyot_execute: NULL argument");
+    HX_CHECK_ARG(batch >= 1, "hx_lyot_execute: batch must be >= 1");
+    HX_CHECK_ARG(lyot_out != nullptr || (img != nullptr && image_out != nullptr),
+                 "hx_lyot_execute: nothing to write (no Lyot-plane output and no image)");
+    HX_CHECK_ARG(!img || (img->nx == fpm->nx && img->ny == fpm->ny && img->precision == fpm->precision),
+                 "hx_lyot_execute: the image plan must share the pupil grid and the precision of the mask plan");
+    HX_CHECK_ARG(!img || image_out != nullptr, "hx_lyot_execute: image plan given without an image output");
+    const size_t need = hx_lyot_workspace_bytes(fpm, img, batch);
+    HX_CHECK_ARG(ws != nullptr && ws_bytes >= need, "hx_lyot_execute: workspace of %zu bytes needed", need);
+    if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
+    cudaStream_t stream = (cudaStream_t)stream_;
+    if (fpm->precision == HX_PREC_SPLIT)
+        return hx::split_lyot_execute(fpm->split, img ? img->split : nullptr, batch, e, e_dtype,
+                                      (const float2*)one_minus_fpm, (const float2*)stop, af_re, af_im, ab_re, ab_im,
+                                      ai_re, ai_im, lyot_out, lyot_dtype, image_out, image_dtype, ws, stream);
+    HX_CHECK_ARG(e_dtype == fpm->dtype && (!lyot_out || lyot_dtype == fpm->dtype) &&
+                     (!img || image_dtype == fpm->dtype),
+                 "hx_lyot_execute: a plain plan reads and writes its own dtype");
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    uint8_t* w = (uint8_t*)ws;
+    const size_t es = fpm->esize;
+    void* ef = w;
+    w += up(es * (size_t)batch * fpm->nu * fpm->nv);
+    void* lp = lyot_out ? lyot_out : (void*)w;
+    w += up(es * (size_t)batch * fpm->nx * fpm->ny);
+    void* mws = w;
+    const size_t mws_bytes = ws_bytes - (size_t)(w - (uint8_t*)ws);
+    HX_TRY(hx_mft_execute_ex(fpm, HX_FORWARD, batch, e, ef, af_re, af_im, HX_EPI_MUL, one_minus_fpm, nullptr, mws,
+                             mws_bytes, stream));
+    HX_TRY(hx_mft_execute_ex(fpm, HX_BACKWARD, batch, ef, lp, ab_re, ab_im, HX_EPI_BABINET, stop, e, mws, mws_bytes,
+                             stream));
+    if (img)
+        return hx_mft_execute_ex(img, HX_FORWARD, batch, lp, image_out, ai_re, ai_im, HX_EPI_NONE, nullptr, nullptr,
+                                 mws, mws_bytes, stream);
+    return HX_OK;
 }
 
 int hx_mft_plan_status(const hx_mft_plan* p, int reset) {

@@ -11,21 +11,27 @@
 // survive.  The level-0 products are integers of magnitude <= 2^12, so their
 // FP32 sum is exact up to 4096 terms (K' = 2K <= 4096); the other levels carry
 // 2^-11, 2^-22 and 2^-33 of the weight, so their FP32 rounding sits far below
-// 2^-29.  The epilogue combines the levels in float64.  This removes the FP32
-// accumulation error of the plain path, which dominates a coronagraph's dark
-// hole (its normalized-intensity error is ~1e-10 in FP32).
+// 2^-29.  This removes the FP32 accumulation error of the plain path, which
+// dominates a coronagraph's dark hole (its normalized-intensity error is
+// ~1e-9 in FP32).
+//
+// All arithmetic around the tensor cores is FP32: the GB300's float64 rate is a
+// small fraction of its FP32 rate.  The epilogue combines the levels into a
+// float-float pair (hi + lo, ~46 bits) with error-free TwoSum/TwoProduct steps,
+// and applies the scales, alpha, the focal-plane mask and the Babinet
+// subtraction in float-float.  Intermediate fields travel between the two GEMMs
+// of an MFT, and between the MFTs of a coronagraph, as float-float planes
+// (hi and lo of Re and Im); slicing reads them with FP32 operations only.
 //
 // Kernel.  One CTA computes 64 complex rows x 64 columns of C: a 128-row tile of
 // A' (the 64 Cr rows then their 64 Ci rows) times a 64-row tile of B'.
 // warp 0 issues TMA loads (one 3-D box per operand per stage: three slice
 // planes of 64 K-elements, 128-byte swizzle), warp 1 issues tcgen05.mma
 // (8 slice products x 4 K16 steps per stage) into four TMEM accumulators of
-// 128 lanes x 64 columns, warps 2-5 read TMEM, combine the levels in float64,
-// apply the row/column scales, alpha and the fused epilogue, and write the
-// result.  Three pipeline stages of 72 KiB.  All waits are bounded: a wait that
-// runs out records HX_ERR_TIMEOUT in the plan's status word, the CTA drains its
-// own copies and MMAs, frees its TMEM and returns.  A wait is bounded by the
-// global timer (2 s), not by a poll count.
+// 128 lanes x 64 columns, warps 2-5 read TMEM, combine and finish the result.
+// Three pipeline stages of 72 KiB.  All waits are bounded by the global timer:
+// a wait that runs out records HX_ERR_TIMEOUT in the plan's status word, the
+// CTA drains its own copies and MMAs, frees its TMEM and returns.
 #include "hx_common.cuh"
 #include "mft_tc.cuh"
 #include "tc_ptx.cuh"
@@ -34,6 +40,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 
 namespace hx {
@@ -49,43 +56,132 @@ constexpr int B_PLANE_BYTES = BN * BK * 2;
 constexpr int A_STAGE_BYTES = NSLICE * A_PLANE_BYTES;
 constexpr int B_STAGE_BYTES = NSLICE * B_PLANE_BYTES;
 constexpr int STAGE_BYTES = A_STAGE_BYTES + B_STAGE_BYTES;
-constexpr int EPI_PITCH = BN + 1;  // float64 staging row pitch (bank spread)
+constexpr int EPI_PITCH = BN + 1;  // staging row pitch in floats (bank spread)
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr int TMEM_COLS = 256;  // four level accumulators of BN columns
 constexpr int NUM_THREADS = 192;
 constexpr uint64_t WAIT_LIMIT = 2000000000ull;  // 2 s per wait
-constexpr int MAX_KPITCH = 4096;  // exact level-0 sums need K' <= 4096
+constexpr int MAX_KPITCH = 4096;                // exact level-0 sums need K' <= 4096
 
-static_assert(BM * EPI_PITCH * 8 <= STAGES * STAGE_BYTES, "epilogue staging must fit the pipeline buffers");
+static_assert(2 * BM * EPI_PITCH * 4 <= STAGES * STAGE_BYTES, "epilogue staging must fit the pipeline buffers");
 
-enum { OUT_F64_PLANES = 0, OUT_C64 = 1 };
+// ---- float-float arithmetic (error-free transformations in FP32) -------------------------------------
+
+struct ff {
+    float hi, lo;
+};
+
+__device__ __forceinline__ ff two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+
+__device__ __forceinline__ ff two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    const ff s = two_sum(a.hi, b.hi);
+    const float t = __fadd_rn(__fadd_rn(a.lo, b.lo), s.lo);
+    return two_sum(s.hi, t);
+}
+
+__device__ __forceinline__ ff ff_neg(ff a) { return {-a.hi, -a.lo}; }
+
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+    const ff p = two_prod(a.hi, b.hi);
+    const float t = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo));
+    return two_sum(p.hi, t);
+}
+
+__device__ __forceinline__ ff ff_mulf(ff a, float b) {
+    const ff p = two_prod(a.hi, b);
+    return two_sum(p.hi, __fmaf_rn(a.lo, b, p.lo));
+}
+
+// Complex float-float: (a + ib).
+struct cff {
+    ff re, im;
+};
+
+__device__ __forceinline__ cff cff_mul(cff a, cff b) {
+    return {ff_add(ff_mul(a.re, b.re), ff_neg(ff_mul(a.im, b.im))), ff_add(ff_mul(a.re, b.im), ff_mul(a.im, b.re))};
+}
+
+__device__ __forceinline__ cff cff_mul_c64(cff a, float2 b) {
+    return {ff_add(ff_mulf(a.re, b.x), ff_neg(ff_mulf(a.im, b.y))), ff_add(ff_mulf(a.re, b.y), ff_mulf(a.im, b.x))};
+}
+
+// ---- field formats ----------------------------------------------------------------------------------
+
+// A batch of complex values as interleaved complex64, interleaved complex128, or four float-float planes.
+struct FieldIO {
+    const float2* c64 = nullptr;
+    float2* c64_out = nullptr;
+    const double2* c128 = nullptr;
+    double2* c128_out = nullptr;
+    float* re_hi = nullptr;
+    float* re_lo = nullptr;
+    float* im_hi = nullptr;
+    float* im_lo = nullptr;
+};
+
+__device__ __forceinline__ ff split_double(double x) {
+    const float hi = (float)x;
+    return {hi, (float)(x - (double)hi)};
+}
+
+__device__ __forceinline__ cff load_field(const FieldIO& f, long long i) {
+    if (f.re_hi) return {{f.re_hi[i], f.re_lo[i]}, {f.im_hi[i], f.im_lo[i]}};
+    if (f.c128) {
+        const double2 v = f.c128[i];
+        return {split_double(v.x), split_double(v.y)};
+    }
+    const float2 v = f.c64[i];
+    return {{v.x, 0.0f}, {v.y, 0.0f}};
+}
+
+__device__ __forceinline__ void store_field(const FieldIO& f, long long i, cff v) {
+    if (f.re_hi) {
+        f.re_hi[i] = v.re.hi;
+        f.re_lo[i] = v.re.lo;
+        f.im_hi[i] = v.im.hi;
+        f.im_lo[i] = v.im.lo;
+    } else if (f.c128_out) {
+        f.c128_out[i] = make_double2((double)v.re.hi + (double)v.re.lo, (double)v.im.hi + (double)v.im.lo);
+    } else {
+        f.c64_out[i] = make_float2(__fadd_rn(v.re.hi, v.re.lo), __fadd_rn(v.im.hi, v.im.lo));
+    }
+}
+
+// ---- the tensor-core GEMM ----------------------------------------------------------------------------
 
 struct __align__(64) GemmArgs {
     CUtensorMap tmap_a;
     CUtensorMap tmap_b;
-    int m_tiles, n_tiles, ktiles;
+    int ktiles;
     int a_rows_per_z;      // A' row offset per grid z (0: shared A)
     int b_rows_per_z;      // B' row offset per grid z (0: shared B)
     int M, N;              // valid complex rows / columns of the output (per z)
-    const double* row_scale;
+    const float* row_scale;
     long long row_scale_z;
-    const double* col_scale;
+    const float* col_scale;
     long long col_scale_z;
-    double alpha_re, alpha_im;
-    int out_mode;
-    double* out_re;
-    double* out_im;
-    float2* out_c64;
+    float alpha[4];        // Re hi, Re lo, Im hi, Im lo
+    FieldIO out;
     long long ldo, out_z;
     int epi;
     const float2* mask;
-    const float2* src;
+    FieldIO src;           // Babinet source, same indexing as the output
     int rows_per_field;    // mask index = (m % rows_per_field) * N + n
-    unsigned long long* colmax;
+    unsigned int* colmax;  // max(|Re|, |Im|) of the output as float bits, per (field, column)
     long long colmax_z;
-    int colmax_rows_per_field;  // colmax field = m / colmax_rows_per_field (stacked rows), plus z
+    int colmax_rows_per_field;  // field of a stacked row = m / colmax_rows_per_field (0: one field)
     long long colmax_field_stride;
-    unsigned long long* rowmax;
+    unsigned int* rowmax;  // per output row
     long long rowmax_z;
     int* status;
 };
@@ -195,10 +291,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
         }
     } else {
         // ---- epilogue: warps 2..5 ----
-        const int et = threadIdx.x - 64;           // 0..127
-        const int quarter = warp & 3;              // TMEM lane quarter this warp may access
-        const int row = quarter * 32 + lane;       // A' row within the tile = TMEM lane
-        double* stage = reinterpret_cast<double*>(smem);
+        const int et = threadIdx.x - 64;      // 0..127
+        const int quarter = warp & 3;         // TMEM lane quarter this warp may access
+        const int row = quarter * 32 + lane;  // A' row within the tile = TMEM lane
+        float* st_hi = reinterpret_cast<float*>(smem);
+        float* st_lo = st_hi + BM * EPI_PITCH;
         if (!ptx::mbar_wait_bounded(bar_accum, 0, WAIT_LIMIT)) raise_status(g.status, abort_flag);
         ptx::tc_fence_after();
         // Warp-uniform decision: the TMEM loads below are .sync.aligned.
@@ -214,14 +311,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
                 ptx::tmem_ld_16(tmem + lane_base + 3 * BN + c * 16, v3);
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                    const double v = (double)v0[j] * 0x1p-12 + (double)v1[j] * 0x1p-23 + (double)v2[j] * 0x1p-34 +
-                                     (double)v3[j] * 0x1p-45;
-                    stage[row * EPI_PITCH + c * 16 + j] = v;
+                    // level 0 is an exact integer; scaling by powers of two is exact.
+                    ff s = two_sum(v0[j] * 0x1p-12f, v1[j] * 0x1p-23f);
+                    s = two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(v2[j] * 0x1p-34f, v3[j] * 0x1p-45f)));
+                    st_hi[row * EPI_PITCH + c * 16 + j] = s.hi;
+                    st_lo[row * EPI_PITCH + c * 16 + j] = s.lo;
                 }
             }
         }
         ptx::named_barrier(1, 128);
         if (live && !*abort_flag) {
+            const cff alpha = {{g.alpha[0], g.alpha[1]}, {g.alpha[2], g.alpha[3]}};
 #pragma unroll 1
             for (int i = 0; i < (64 * BN) / 128; ++i) {
                 const int idx = et + 128 * i;
@@ -229,42 +329,25 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
                 const int m = m_tile * 64 + ml;
                 const int n = n_tile * BN + nl;
                 if (m >= g.M || n >= g.N) continue;
-                const double sc = g.row_scale[z * g.row_scale_z + m] * g.col_scale[z * g.col_scale_z + n];
-                const double cr = stage[ml * EPI_PITCH + nl] * sc;
-                const double ci = stage[(64 + ml) * EPI_PITCH + nl] * sc;
-                double re = g.alpha_re * cr - g.alpha_im * ci;
-                double im = g.alpha_re * ci + g.alpha_im * cr;
+                const float sc = g.row_scale[z * g.row_scale_z + m] * g.col_scale[z * g.col_scale_z + n];
+                cff v = {ff{st_hi[ml * EPI_PITCH + nl] * sc, st_lo[ml * EPI_PITCH + nl] * sc},
+                         ff{st_hi[(64 + ml) * EPI_PITCH + nl] * sc, st_lo[(64 + ml) * EPI_PITCH + nl] * sc}};
+                v = cff_mul(v, alpha);
                 const long long o = z * g.out_z + (long long)m * g.ldo + n;
                 if (g.epi == HX_EPI_MUL) {
-                    const float2 mk = g.mask[(long long)(m % g.rows_per_field) * g.N + n];
-                    const double r2 = re * mk.x - im * mk.y;
-                    im = re * mk.y + im * mk.x;
-                    re = r2;
+                    v = cff_mul_c64(v, g.mask[(long long)(m % g.rows_per_field) * g.N + n]);
                 } else if (g.epi == HX_EPI_BABINET) {
-                    const float2 e = g.src[o];
-                    re = (double)e.x - re;
-                    im = (double)e.y - im;
-                    if (g.mask) {
-                        const float2 mk = g.mask[(long long)(m % g.rows_per_field) * g.N + n];
-                        const double r2 = re * mk.x - im * mk.y;
-                        im = re * mk.y + im * mk.x;
-                        re = r2;
-                    }
+                    const cff e = load_field(g.src, o);
+                    v = {ff_add(e.re, ff_neg(v.re)), ff_add(e.im, ff_neg(v.im))};
+                    if (g.mask) v = cff_mul_c64(v, g.mask[(long long)(m % g.rows_per_field) * g.N + n]);
                 }
-                if (g.out_mode == OUT_F64_PLANES) {
-                    g.out_re[o] = re;
-                    g.out_im[o] = im;
-                } else {
-                    g.out_c64[o] = make_float2((float)re, (float)im);
-                }
-                const double mag = fmax(fabs(re), fabs(im));
+                store_field(g.out, o, v);
+                const float mag = fmaxf(fabsf(v.re.hi), fabsf(v.im.hi));
                 if (g.colmax) {
                     const long long f = g.colmax_rows_per_field > 0 ? m / g.colmax_rows_per_field : 0;
-                    atomicMax(&g.colmax[z * g.colmax_z + f * g.colmax_field_stride + n],
-                              (unsigned long long)__double_as_longlong(mag));
+                    atomicMax(&g.colmax[z * g.colmax_z + f * g.colmax_field_stride + n], __float_as_uint(mag));
                 }
-                if (g.rowmax)
-                    atomicMax(&g.rowmax[z * g.rowmax_z + m], (unsigned long long)__double_as_longlong(mag));
+                if (g.rowmax) atomicMax(&g.rowmax[z * g.rowmax_z + m], __float_as_uint(mag));
             }
         }
     }
@@ -276,78 +359,66 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
     }
 }
 
-// ---- slicing --------------------------------------------------------------------------------------
+// ---- slicing (FP32 only) ------------------------------------------------------------------------------
 
-__device__ __forceinline__ double pow2_scale(double mx) {
-    if (!(mx > 0.0) || !isfinite(mx)) return 1.0;
+// Power of two strictly above the largest magnitude of a row/column (1 for zero rows).
+__device__ __forceinline__ float pow2_above(float mx) {
+    if (!(mx > 0.0f) || !isfinite(mx)) return 1.0f;
     int e;
-    frexp(mx, &e);  // mx = f 2^e, f in [0.5, 1)
-    return ldexp(1.0, e);
+    frexpf(mx, &e);  // mx = f 2^e, f in [0.5, 1)
+    return ldexpf(1.0f, e);
 }
 
-// x in [-1, 1] -> a0 + 2^-11 a1 + 2^-22 a2 (times 2^-6), rounded to nearest at each step.
-__device__ __forceinline__ void slice3(double t, __half& h0, __half& h1, __half& h2) {
-    double u = t * 64.0;
-    const double a0 = rint(u);
-    u = (u - a0) * 2048.0;
-    const double a1 = rint(u);
-    u = (u - a1) * 2048.0;
-    const double a2 = rint(u);
-    h0 = __double2half(a0);
-    h1 = __double2half(a1);
-    h2 = __double2half(a2);
-}
-
-__device__ __forceinline__ void load_cplx(const float2* c64, const double* re, const double* im, long long i,
-                                          double& xr, double& xi) {
-    if (c64) {
-        const float2 v = c64[i];
-        xr = v.x;
-        xi = v.y;
-    } else {
-        xr = re[i];
-        xi = im[i];
-    }
+// hi + lo scaled into [-1, 1) -> a0 + 2^-11 a1 + 2^-22 a2 (times 2^-6); every step is exact except the
+// single addition of the scaled low word, whose rounding is below 2^-31 of the scale.
+__device__ __forceinline__ void slice3(ff x, float inv, __half& h0, __half& h1, __half& h2) {
+    const float th = x.hi * inv * 64.0f;
+    const float tl = x.lo * inv * 64.0f;
+    const float a0 = rintf(th);
+    const float r = __fadd_rn(__fsub_rn(th, a0), tl) * 2048.0f;
+    const float a1 = rintf(r);
+    const float a2 = rintf(__fsub_rn(r, a1) * 2048.0f);
+    h0 = __float2half_rn(a0);
+    h1 = __float2half_rn(a1);
+    h2 = __float2half_rn(a2);
 }
 
 // One CTA per complex row m of X (M x K, row stride ld): writes the Cr and Ci rows of A'.
-__global__ void slice_rows_kernel(const float2* src_c64, const double* src_re, const double* src_im, long long ld,
-                                  int K, int Kp, const unsigned long long* rowmax, __half* planes,
-                                  long long plane_stride, int kpitch, double* scale_out) {
+__global__ void slice_rows_kernel(FieldIO src, long long ld, int K, int Kp, const unsigned int* rowmax,
+                                  __half* planes, long long plane_stride, int kpitch, float* scale_out) {
     const int m = blockIdx.x;
-    __shared__ double red[32];
-    __shared__ double s_scale;
-    double mx = 0.0;
+    __shared__ float red[32];
+    __shared__ float s_scale;
+    float mx = 0.0f;
     if (rowmax) {
-        mx = __longlong_as_double((long long)rowmax[m]);
+        mx = __uint_as_float(rowmax[m]);
     } else {
         for (int k = threadIdx.x; k < K; k += blockDim.x) {
-            double xr, xi;
-            load_cplx(src_c64, src_re, src_im, (long long)m * ld + k, xr, xi);
-            mx = fmax(mx, fmax(fabs(xr), fabs(xi)));
+            const cff v = load_field(src, (long long)m * ld + k);
+            mx = fmaxf(mx, fmaxf(fabsf(v.re.hi), fabsf(v.im.hi)));
         }
-        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
         __syncthreads();
         if (threadIdx.x < 32) {
-            mx = threadIdx.x < (int)(blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-            for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            mx = threadIdx.x < (int)(blockDim.x >> 5) ? red[threadIdx.x] : 0.0f;
+            for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         }
     }
     if (threadIdx.x == 0) {
-        s_scale = pow2_scale(mx);
+        s_scale = pow2_above(mx);
         scale_out[m] = s_scale;
     }
     __syncthreads();
-    const double inv = 1.0 / s_scale;
+    const float inv = 1.0f / s_scale;
     const long long r_cr = (long long)(m / 64) * 128 + (m % 64);
     const long long r_ci = r_cr + 64;
     for (int k = threadIdx.x; k < Kp; k += blockDim.x) {
-        double xr = 0.0, xi = 0.0;
-        if (k < K) load_cplx(src_c64, src_re, src_im, (long long)m * ld + k, xr, xi);
+        cff v = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+        if (k < K) v = load_field(src, (long long)m * ld + k);
         __half r0, r1, r2, i0, i1, i2;
-        slice3(xr * inv, r0, r1, r2);
-        slice3(xi * inv, i0, i1, i2);
+        slice3(v.re, inv, r0, r1, r2);
+        slice3(v.im, inv, i0, i1, i2);
         const __half rs[3] = {r0, r1, r2};
         const __half is[3] = {i0, i1, i2};
 #pragma unroll
@@ -361,53 +432,51 @@ __global__ void slice_rows_kernel(const float2* src_c64, const double* src_re, c
     }
 }
 
-// Column maxima max(|Re|, |Im|) of per-field K x N matrices (fields along grid z), as float64 bits.
-__global__ void colmax_kernel(const float2* src_c64, const double* src_re, const double* src_im, int K, int N,
-                              long long field_stride, unsigned long long* colmax, long long colmax_stride) {
+// Column maxima max(|Re|, |Im|) of per-field K x N matrices (fields along grid z), as float bits.
+__global__ void colmax_kernel(FieldIO src, int K, int N, long long field_stride, unsigned int* colmax,
+                              long long colmax_stride) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const int z = blockIdx.z;
     if (n >= N) return;
     const int k0 = blockIdx.y * 64;
     const int k1 = min(K, k0 + 64);
-    double mx = 0.0;
+    float mx = 0.0f;
     for (int k = k0; k < k1; ++k) {
-        double xr, xi;
-        load_cplx(src_c64, src_re, src_im, z * field_stride + (long long)k * N + n, xr, xi);
-        mx = fmax(mx, fmax(fabs(xr), fabs(xi)));
+        const cff v = load_field(src, z * field_stride + (long long)k * N + n);
+        mx = fmaxf(mx, fmaxf(fabsf(v.re.hi), fabsf(v.im.hi)));
     }
-    atomicMax(&colmax[z * colmax_stride + n], (unsigned long long)__double_as_longlong(mx));
+    atomicMax(&colmax[z * colmax_stride + n], __float_as_uint(mx));
 }
 
 // Per-field K x N matrix Y -> B' rows (z*n_rows_per_field + n): [slices of Re Y[:, n] | slices of Im Y[:, n]].
-__global__ void slice_cols_kernel(const float2* src_c64, const double* src_re, const double* src_im, int K, int N,
-                                  int Kp, long long field_stride, const unsigned long long* colmax,
-                                  long long colmax_stride, __half* planes, long long plane_stride, int kpitch,
-                                  int n_rows_per_field, double* scale_out) {
-    __shared__ double tr[32][33], ti[32][33];
-    __shared__ double sc[32];
+__global__ void slice_cols_kernel(FieldIO src, int K, int N, int Kp, long long field_stride,
+                                  const unsigned int* colmax, long long colmax_stride, __half* planes,
+                                  long long plane_stride, int kpitch, int n_rows_per_field, float* scale_out) {
+    __shared__ ff tr[32][33], ti[32][33];
+    __shared__ float sc[32];
     const int n0 = blockIdx.x * 32, k0 = blockIdx.y * 32, z = blockIdx.z;
     const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
     if (ty == 0) {
         const int n = n0 + tx;
-        const double mx = n < N ? __longlong_as_double((long long)colmax[z * colmax_stride + n]) : 0.0;
-        sc[tx] = pow2_scale(mx);
+        const float mx = n < N ? __uint_as_float(colmax[z * colmax_stride + n]) : 0.0f;
+        sc[tx] = pow2_above(mx);
         if (k0 == 0 && n < N) scale_out[(long long)z * n_rows_per_field + n] = sc[tx];
     }
     for (int r = ty; r < 32; r += 8) {
         const int k = k0 + r, n = n0 + tx;
-        double xr = 0.0, xi = 0.0;
-        if (k < K && n < N) load_cplx(src_c64, src_re, src_im, z * field_stride + (long long)k * N + n, xr, xi);
-        tr[r][tx] = xr;
-        ti[r][tx] = xi;
+        cff v = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+        if (k < K && n < N) v = load_field(src, z * field_stride + (long long)k * N + n);
+        tr[r][tx] = v.re;
+        ti[r][tx] = v.im;
     }
     __syncthreads();
     for (int r = ty; r < 32; r += 8) {
         const int n = n0 + r, k = k0 + tx;
         if (n >= N || k >= Kp) continue;
-        const double inv = 1.0 / sc[r];
+        const float inv = 1.0f / sc[r];
         __half r0, r1, r2, i0, i1, i2;
-        slice3(tr[tx][r] * inv, r0, r1, r2);
-        slice3(ti[tx][r] * inv, i0, i1, i2);
+        slice3(tr[tx][r], inv, r0, r1, r2);
+        slice3(ti[tx][r], inv, i0, i1, i2);
         const __half rs[3] = {r0, r1, r2};
         const __half is[3] = {i0, i1, i2};
         const long long row = (long long)z * n_rows_per_field + n;
@@ -420,9 +489,11 @@ __global__ void slice_cols_kernel(const float2* src_c64, const double* src_re, c
     }
 }
 
-// Phase matrix in float64 planes: M[r, c] = wr[r] wc[c] exp(sign i a[r] b[c]).
+// Phase matrix as float-float planes: M[r, c] = wr[r] wc[c] exp(sign i a[r] b[c]), evaluated in float64
+// once per plan.
 __global__ void phase_planes_kernel(int rows, int cols, const double* a, const double* b, double sign,
-                                    const double* wr, const double* wc, double* re, double* im) {
+                                    const double* wr, const double* wc, float* re_hi, float* re_lo, float* im_hi,
+                                    float* im_lo) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)rows * cols) return;
     const int r = (int)(idx / cols), c = (int)(idx % cols);
@@ -431,8 +502,18 @@ __global__ void phase_planes_kernel(int rows, int cols, const double* a, const d
     double w = 1.0;
     if (wr) w *= wr[r];
     if (wc) w *= wc[c];
-    re[idx] = w * co;
-    im[idx] = w * sign * s;
+    const double re = w * co, im = w * sign * s;
+    re_hi[idx] = (float)re;
+    re_lo[idx] = (float)(re - (double)(float)re);
+    im_hi[idx] = (float)im;
+    im_lo[idx] = (float)(im - (double)(float)im);
+}
+
+// Copy between field formats (float-float planes -> complex64 / complex128).
+__global__ void field_copy_kernel(FieldIO src, FieldIO dst, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    store_field(dst, i, load_field(src, i));
 }
 
 // ---- host side ------------------------------------------------------------------------------------
@@ -456,7 +537,7 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 // A sliced operand in global memory: three fp16 planes of rows x kpitch (K-major) and one scale per logical row.
 struct SliceMat {
     __half* planes = nullptr;
-    double* scale = nullptr;
+    float* scale = nullptr;
     long long rows = 0;
     int kpitch = 0;
     int Kp = 0;
@@ -502,34 +583,50 @@ void carve_slices(Carver& c, SliceMat& s, long long rows, int K, long long scale
     s.kpitch = 2 * s.Kp;
     s.rows = rows;
     s.planes = (__half*)c.take(s.plane_bytes());
-    s.scale = (double*)c.take(sizeof(double) * scales);
+    s.scale = (float*)c.take(sizeof(float) * scales);
 }
 
-int launch_slice_rows(const float2* c64, const double* re, const double* im, long long ld, long long M, int K,
-                      const unsigned long long* rowmax, SliceMat& s, cudaStream_t st) {
+FieldIO carve_ff(Carver& c, long long n) {
+    FieldIO f;
+    f.re_hi = (float*)c.take(sizeof(float) * n);
+    f.re_lo = (float*)c.take(sizeof(float) * n);
+    f.im_hi = (float*)c.take(sizeof(float) * n);
+    f.im_lo = (float*)c.take(sizeof(float) * n);
+    return f;
+}
+
+int launch_slice_rows(const FieldIO& src, long long ld, long long M, int K, const unsigned int* rowmax,
+                      SliceMat& s, cudaStream_t st) {
     if (M > 2147483647LL) return HX_ERR_UNSUPPORTED;
-    slice_rows_kernel<<<(unsigned)M, 256, 0, st>>>(c64, re, im, ld, K, s.Kp, rowmax, s.planes, s.plane_stride(),
-                                                   s.kpitch, s.scale);
+    slice_rows_kernel<<<(unsigned)M, 256, 0, st>>>(src, ld, K, s.Kp, rowmax, s.planes, s.plane_stride(), s.kpitch,
+                                                   s.scale);
     return launch_status("slice_rows_kernel");
 }
 
-int launch_colmax(const float2* c64, const double* re, const double* im, int K, int N, int fields,
-                  long long field_stride, unsigned long long* colmax, long long colmax_stride, cudaStream_t st) {
+int launch_colmax(const FieldIO& src, int K, int N, int fields, long long field_stride, unsigned int* colmax,
+                  long long colmax_stride, cudaStream_t st) {
     dim3 grid(ceil_div(N, 128), ceil_div(K, 64), fields);
-    colmax_kernel<<<grid, 128, 0, st>>>(c64, re, im, K, N, field_stride, colmax, colmax_stride);
+    colmax_kernel<<<grid, 128, 0, st>>>(src, K, N, field_stride, colmax, colmax_stride);
     return launch_status("colmax_kernel");
 }
 
-int launch_slice_cols(const float2* c64, const double* re, const double* im, int K, int N, int fields,
-                      long long field_stride, const unsigned long long* colmax, long long colmax_stride,
-                      SliceMat& s, int n_rows_per_field, cudaStream_t st) {
+int launch_slice_cols(const FieldIO& src, int K, int N, int fields, long long field_stride,
+                      const unsigned int* colmax, long long colmax_stride, SliceMat& s, int n_rows_per_field,
+                      cudaStream_t st) {
     dim3 grid(ceil_div(N, 32), ceil_div(s.Kp, 32), fields);
-    slice_cols_kernel<<<grid, dim3(32, 8), 0, st>>>(c64, re, im, K, N, s.Kp, field_stride, colmax, colmax_stride,
-                                                    s.planes, s.plane_stride(), s.kpitch, n_rows_per_field, s.scale);
+    slice_cols_kernel<<<grid, dim3(32, 8), 0, st>>>(src, K, N, s.Kp, field_stride, colmax, colmax_stride, s.planes,
+                                                    s.plane_stride(), s.kpitch, n_rows_per_field, s.scale);
     return launch_status("slice_cols_kernel");
 }
 
-int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, long long a_tiles_rows, int grid_z,
+void set_alpha(GemmArgs& g, double re, double im) {
+    g.alpha[0] = (float)re;
+    g.alpha[1] = (float)(re - (double)g.alpha[0]);
+    g.alpha[2] = (float)im;
+    g.alpha[3] = (float)(im - (double)g.alpha[2]);
+}
+
+int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, long long a_tile_rows, int grid_z,
                 cudaStream_t st) {
     if (A.kpitch != B.kpitch) {
         set_error("internal: split GEMM K mismatch (%d vs %d)", A.kpitch, B.kpitch);
@@ -538,8 +635,8 @@ int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, long long a_t
     HX_TRY(encode_map(&g.tmap_a, A, BM));
     HX_TRY(encode_map(&g.tmap_b, B, BN));
     g.ktiles = A.kpitch / BK;
-    g.m_tiles = (int)(a_tiles_rows / BM);
-    g.n_tiles = ceil_div(g.N, BN);
+    const long long m_tiles = a_tile_rows / BM;
+    const int n_tiles = ceil_div(g.N, BN);
     static bool configured = false;
     if (!configured) {
         HX_TRY(cuda_status(cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -547,11 +644,11 @@ int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, long long a_t
                            "cudaFuncSetAttribute(split_gemm_kernel)"));
         configured = true;
     }
-    if (g.m_tiles > 65535 || grid_z > 65535) {
+    if (m_tiles > 65535 || grid_z > 65535) {
         set_error("split GEMM grid too large");
         return HX_ERR_UNSUPPORTED;
     }
-    dim3 grid(g.n_tiles, g.m_tiles, grid_z);
+    dim3 grid(n_tiles, (unsigned)m_tiles, grid_z);
     split_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, st>>>(g);
     return launch_status("split_gemm_kernel");
 }
@@ -559,7 +656,7 @@ int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, long long a_t
 GemmArgs base_args(int* status) {
     GemmArgs g;
     memset(&g, 0, sizeof(g));
-    g.alpha_re = 1.0;
+    set_alpha(g, 1.0, 0.0);
     g.rows_per_field = 1;
     g.status = status;
     return g;
@@ -580,35 +677,156 @@ struct SplitMftPlan {
 
 namespace {
 
-// Slice a float64 phase matrix (rows x cols, generated on the device) as an A (row) or B (column) operand.
+// Slice a phase matrix (rows x cols, evaluated on the device) as an A (row) or B (column) operand.
 int slice_phase(int rows, int cols, const double* a, const double* b, double sign, const double* wr,
                 const double* wc, bool as_rows, SliceMat& out, cudaStream_t st) {
-    double *re = nullptr, *im = nullptr;
-    unsigned long long* mx = nullptr;
+    void* tmp = nullptr;
     const long long n = (long long)rows * cols;
-    int rc = cuda_status(cudaMalloc(&re, sizeof(double) * n), "cudaMalloc(phase re)");
-    if (rc == HX_OK) rc = cuda_status(cudaMalloc(&im, sizeof(double) * n), "cudaMalloc(phase im)");
+    Carver count(nullptr);
+    carve_ff(count, n);
+    count.take(sizeof(unsigned int) * round_up(cols, 64));
+    int rc = cuda_status(cudaMalloc(&tmp, count.off), "cudaMalloc(phase matrix)");
     if (rc == HX_OK) {
-        phase_planes_kernel<<<ceil_div(n, 256), 256, 0, st>>>(rows, cols, a, b, sign, wr, wc, re, im);
+        Carver c(tmp);
+        FieldIO f = carve_ff(c, n);
+        unsigned int* mx = (unsigned int*)c.take(sizeof(unsigned int) * round_up(cols, 64));
+        phase_planes_kernel<<<ceil_div(n, 256), 256, 0, st>>>(rows, cols, a, b, sign, wr, wc, f.re_hi, f.re_lo,
+                                                              f.im_hi, f.im_lo);
         rc = launch_status("phase_planes_kernel");
-    }
-    if (rc == HX_OK) {
-        if (as_rows) {
-            rc = launch_slice_rows(nullptr, re, im, cols, rows, cols, nullptr, out, st);
-        } else {
-            rc = cuda_status(cudaMalloc(&mx, sizeof(unsigned long long) * round_up(cols, 64)), "cudaMalloc(colmax)");
-            if (rc == HX_OK)
-                rc = cuda_status(cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * round_up(cols, 64), st),
-                                 "memset colmax");
-            if (rc == HX_OK) rc = launch_colmax(nullptr, re, im, rows, cols, 1, 0, mx, 0, st);
-            if (rc == HX_OK) rc = launch_slice_cols(nullptr, re, im, rows, cols, 1, 0, mx, 0, out, 0, st);
+        if (rc == HX_OK) {
+            if (as_rows) {
+                rc = launch_slice_rows(f, cols, rows, cols, nullptr, out, st);
+            } else {
+                rc = cuda_status(cudaMemsetAsync(mx, 0, sizeof(unsigned int) * round_up(cols, 64), st), "memset");
+                if (rc == HX_OK) rc = launch_colmax(f, rows, cols, 1, 0, mx, 0, st);
+                if (rc == HX_OK) rc = launch_slice_cols(f, rows, cols, 1, 0, mx, 0, out, 0, st);
+            }
         }
     }
     cudaStreamSynchronize(st);
-    cudaFree(re);
-    cudaFree(im);
-    cudaFree(mx);
+    cudaFree(tmp);
     return rc;
+}
+
+// Workspace of one direction: operand slices, the float-float intermediate and the max arrays.
+struct Ws {
+    unsigned int* in_max = nullptr;  // input column maxima (backward only)
+    SliceMat s1;                     // sliced input operand of the first GEMM
+    FieldIO t;                       // float-float intermediate
+    unsigned int* t_max = nullptr;   // its column (forward) or row (backward) maxima
+    SliceMat s2;                     // sliced intermediate for the second GEMM
+};
+
+void carve_ws(Carver& c, const SplitMftPlan* p, int direction, int batch, Ws& w) {
+    const long long rows = (long long)batch * p->ny;
+    const long long nu64 = round_up(p->nu, 64);
+    if (direction == HX_FORWARD) {
+        carve_slices(c, w.s1, 2 * round_up(rows, 64), p->nx, rows);
+        w.t = carve_ff(c, rows * p->nu);
+        w.t_max = (unsigned int*)c.take(sizeof(unsigned int) * batch * nu64);
+        carve_slices(c, w.s2, (long long)batch * nu64, p->ny, (long long)batch * nu64);
+    } else {
+        w.in_max = (unsigned int*)c.take(sizeof(unsigned int) * batch * nu64);
+        carve_slices(c, w.s1, (long long)batch * nu64, p->nv, (long long)batch * nu64);
+        w.t = carve_ff(c, rows * p->nu);
+        w.t_max = (unsigned int*)c.take(sizeof(unsigned int) * rows);
+        carve_slices(c, w.s2, 2 * round_up(rows, 64), p->nu, rows);
+    }
+}
+
+// in/out: c64 or float-float fields.  in_max: optional precomputed maxima of the input in the orientation the
+// first GEMM slices it (forward: per stacked row; backward: per field and column, stride nu64).  out_rowmax /
+// out_colmax: optional maxima of the output for a following transform (zeroed by the caller).
+int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO& in, const unsigned int* in_max,
+                  const FieldIO& out, double are, double aim, int epilogue, const float2* mask, const FieldIO& src,
+                  unsigned int* out_rowmax, unsigned int* out_colmax, void* ws, cudaStream_t st) {
+    const int nx = p->nx, ny = p->ny, nu = p->nu, nv = p->nv;
+    const long long nu64 = round_up(nu, 64);
+    const long long rows = (long long)batch * ny;
+    Carver c(ws);
+    Ws w;
+    carve_ws(c, p, direction, batch, w);
+    if (direction == HX_FORWARD) {
+        HX_TRY(cuda_status(cudaMemsetAsync(w.t_max, 0, sizeof(unsigned int) * batch * nu64, st), "memset"));
+        // G1: T = E . M2f, stacked over the batch; column maxima of T per field for the next slicing.
+        HX_TRY(launch_slice_rows(in, nx, rows, nx, in_max, w.s1, st));
+        GemmArgs g1 = base_args(p->status);
+        g1.M = (int)rows;
+        g1.N = nu;
+        g1.row_scale = w.s1.scale;
+        g1.col_scale = p->m2f.scale;
+        g1.out = w.t;
+        g1.ldo = nu;
+        g1.colmax = w.t_max;
+        g1.colmax_rows_per_field = ny;
+        g1.colmax_field_stride = nu64;
+        HX_TRY(launch_gemm(g1, w.s1, p->m2f, w.s1.rows, 1, st));
+        // G2: out[b] = alpha M1f . T[b] with the fused epilogue.
+        HX_TRY(launch_slice_cols(w.t, ny, nu, batch, (long long)ny * nu, w.t_max, nu64, w.s2, (int)nu64, st));
+        GemmArgs g2 = base_args(p->status);
+        g2.M = nv;
+        g2.N = nu;
+        g2.b_rows_per_z = (int)nu64;
+        g2.row_scale = p->m1f.scale;
+        g2.col_scale = w.s2.scale;
+        g2.col_scale_z = nu64;
+        set_alpha(g2, are, aim);
+        g2.out = out;
+        g2.ldo = nu;
+        g2.out_z = (long long)nv * nu;
+        g2.epi = epilogue;
+        g2.mask = mask;
+        g2.src = src;
+        g2.rows_per_field = nv;
+        g2.rowmax = out_rowmax;
+        g2.rowmax_z = nv;
+        g2.colmax = out_colmax;
+        g2.colmax_z = nu64;
+        return launch_gemm(g2, p->m1f, w.s2, p->m1f.rows, batch, st);
+    }
+    const SliceMat& m1 = direction == HX_BACKWARD ? p->m1b : p->m1a;
+    const SliceMat& m2 = direction == HX_BACKWARD ? p->m2b : p->m2a;
+    HX_TRY(cuda_status(cudaMemsetAsync(w.t_max, 0, sizeof(unsigned int) * rows, st), "memset"));
+    // G1: T[b] = M1 . F[b]  (F sliced by columns), row maxima of T for the next slicing.
+    const unsigned int* fmax = in_max;
+    if (!fmax) {
+        HX_TRY(cuda_status(cudaMemsetAsync(w.in_max, 0, sizeof(unsigned int) * batch * nu64, st), "memset"));
+        HX_TRY(launch_colmax(in, nv, nu, batch, (long long)nv * nu, w.in_max, nu64, st));
+        fmax = w.in_max;
+    }
+    HX_TRY(launch_slice_cols(in, nv, nu, batch, (long long)nv * nu, fmax, nu64, w.s1, (int)nu64, st));
+    GemmArgs g1 = base_args(p->status);
+    g1.M = ny;
+    g1.N = nu;
+    g1.b_rows_per_z = (int)nu64;
+    g1.row_scale = m1.scale;
+    g1.col_scale = w.s1.scale;
+    g1.col_scale_z = nu64;
+    g1.out = w.t;
+    g1.ldo = nu;
+    g1.out_z = (long long)ny * nu;
+    g1.rowmax = w.t_max;
+    g1.rowmax_z = ny;
+    HX_TRY(launch_gemm(g1, m1, w.s1, m1.rows, batch, st));
+    // G2: out = alpha T . M2, stacked over the batch, with the fused epilogue.
+    HX_TRY(launch_slice_rows(w.t, nu, rows, nu, w.t_max, w.s2, st));
+    GemmArgs g2 = base_args(p->status);
+    g2.M = (int)rows;
+    g2.N = nx;
+    g2.row_scale = w.s2.scale;
+    g2.col_scale = m2.scale;
+    set_alpha(g2, are, aim);
+    g2.out = out;
+    g2.ldo = nx;
+    g2.epi = epilogue;
+    g2.mask = mask;
+    g2.src = src;
+    g2.rows_per_field = ny;
+    g2.rowmax = out_rowmax;
+    g2.colmax = out_colmax;
+    g2.colmax_rows_per_field = ny;
+    g2.colmax_field_stride = round_up(nx, 64);
+    return launch_gemm(g2, w.s2, m2, w.s2.rows, 1, st);
 }
 
 }  // namespace
@@ -624,7 +842,6 @@ int split_mft_create(int nx, int ny, int nu, int nv, const double* x, const doub
     SplitMftPlan* p = new SplitMftPlan();
     p->nx = nx; p->ny = ny; p->nu = nu; p->nv = nv;
     const bool own_adj = wx || wy || wu || wv;
-    // Layout pass (sizes), then one allocation, then the real pass.
     auto layout = [&](Carver& c) {
         carve_slices(c, p->m2f, round_up(nu, 64), nx, round_up(nu, 64));
         carve_slices(c, p->m1f, 2 * round_up(nv, 64), ny, nv);
@@ -666,154 +883,86 @@ int split_mft_create(int nx, int ny, int nu, int nv, const double* x, const doub
     return HX_OK;
 }
 
-namespace {
-
-struct FwdWs {
-    SliceMat a1;            // input rows (batch*ny) x K nx
-    double *t_re, *t_im;    // (batch*ny) x nu
-    unsigned long long* tmax;  // batch x nu64
-    SliceMat b2;            // batch*nu64 rows, K ny
-};
-struct BwdWs {
-    unsigned long long* fmax;  // batch x nu64
-    SliceMat b1;            // batch*nu64 rows, K nv
-    double *t_re, *t_im;    // batch x ny x nu
-    unsigned long long* tmax;  // batch*ny
-    SliceMat a2;            // rows 2 (batch*ny)64, K nu
-};
-
-void carve_fwd(Carver& c, const SplitMftPlan* p, int batch, FwdWs& w) {
-    const long long rows = (long long)batch * p->ny;
-    const long long nu64 = round_up(p->nu, 64);
-    carve_slices(c, w.a1, 2 * round_up(rows, 64), p->nx, rows);
-    w.t_re = (double*)c.take(sizeof(double) * rows * p->nu);
-    w.t_im = (double*)c.take(sizeof(double) * rows * p->nu);
-    w.tmax = (unsigned long long*)c.take(sizeof(unsigned long long) * batch * nu64);
-    carve_slices(c, w.b2, (long long)batch * nu64, p->ny, (long long)batch * nu64);
-}
-
-void carve_bwd(Carver& c, const SplitMftPlan* p, int batch, BwdWs& w) {
-    const long long rows = (long long)batch * p->ny;
-    const long long nu64 = round_up(p->nu, 64);
-    w.fmax = (unsigned long long*)c.take(sizeof(unsigned long long) * batch * nu64);
-    carve_slices(c, w.b1, (long long)batch * nu64, p->nv, (long long)batch * nu64);
-    w.t_re = (double*)c.take(sizeof(double) * rows * p->nu);
-    w.t_im = (double*)c.take(sizeof(double) * rows * p->nu);
-    w.tmax = (unsigned long long*)c.take(sizeof(unsigned long long) * rows);
-    carve_slices(c, w.a2, 2 * round_up(rows, 64), p->nu, rows);
-}
-
-}  // namespace
-
 size_t split_mft_workspace_bytes(const SplitMftPlan* p, int direction, int batch) {
     if (!p || batch <= 0) return 0;
     Carver c(nullptr);
-    if (direction == HX_FORWARD) {
-        FwdWs w;
-        carve_fwd(c, p, batch, w);
-    } else {
-        BwdWs w;
-        carve_bwd(c, p, batch, w);
-    }
+    Ws w;
+    carve_ws(c, p, direction, batch, w);
     return c.off + 256;
 }
 
-int split_mft_execute(const SplitMftPlan* p, int direction, int batch, const float2* in, float2* out, double are,
-                      double aim, int epilogue, const float2* mask, const float2* src, void* ws, size_t ws_bytes,
-                      cudaStream_t st) {
+namespace {
+FieldIO input_field(const void* p, int dtype) {
+    FieldIO f;
+    if (dtype == HX_C128) f.c128 = (const double2*)p;
+    else f.c64 = (const float2*)p;
+    return f;
+}
+FieldIO output_field(void* p, int dtype) {
+    FieldIO f;
+    if (dtype == HX_C128) f.c128_out = (double2*)p;
+    else f.c64_out = (float2*)p;
+    return f;
+}
+}  // namespace
+
+int split_mft_execute(const SplitMftPlan* p, int direction, int batch, const void* in, int in_dtype, void* out,
+                      int out_dtype, double are, double aim, int epilogue, const float2* mask, const void* src,
+                      int src_dtype, void* ws, size_t ws_bytes, cudaStream_t st) {
     if (!p) {
         set_error("the split tensor-core MFT plan is missing");
         return HX_ERR_INVALID;
     }
-    const int nx = p->nx, ny = p->ny, nu = p->nu, nv = p->nv;
-    const long long nu64 = round_up(nu, 64);
-    if (direction == HX_FORWARD) {
-        Carver c(ws);
-        FwdWs w;
-        carve_fwd(c, p, batch, w);
-        const long long rows = (long long)batch * ny;
-        HX_TRY(cuda_status(cudaMemsetAsync(w.tmax, 0, sizeof(unsigned long long) * batch * nu64, st), "memset"));
-        // G1: T = E . M2f, stacked over the batch; column maxima of T per field for the next slicing.
-        HX_TRY(launch_slice_rows(in, nullptr, nullptr, nx, rows, nx, nullptr, w.a1, st));
-        GemmArgs g1 = base_args(p->status);
-        g1.M = (int)rows;
-        g1.N = nu;
-        g1.row_scale = w.a1.scale;
-        g1.col_scale = p->m2f.scale;
-        g1.out_mode = OUT_F64_PLANES;
-        g1.out_re = w.t_re;
-        g1.out_im = w.t_im;
-        g1.ldo = nu;
-        g1.colmax = w.tmax;
-        g1.colmax_rows_per_field = ny;
-        g1.colmax_field_stride = nu64;
-        HX_TRY(launch_gemm(g1, w.a1, p->m2f, w.a1.rows, 1, st));
-        // G2: out[b] = alpha M1f . T[b]
-        HX_TRY(launch_slice_cols(nullptr, w.t_re, w.t_im, ny, nu, batch, (long long)ny * nu, w.tmax, nu64, w.b2,
-                                 (int)nu64, st));
-        GemmArgs g2 = base_args(p->status);
-        g2.M = nv;
-        g2.N = nu;
-        g2.b_rows_per_z = (int)nu64;
-        g2.row_scale = p->m1f.scale;
-        g2.col_scale = w.b2.scale;
-        g2.col_scale_z = nu64;
-        g2.alpha_re = are;
-        g2.alpha_im = aim;
-        g2.out_mode = OUT_C64;
-        g2.out_c64 = out;
-        g2.ldo = nu;
-        g2.out_z = (long long)nv * nu;
-        g2.epi = epilogue;
-        g2.mask = mask;
-        g2.src = src;
-        g2.rows_per_field = nv;
-        return launch_gemm(g2, p->m1f, w.b2, p->m1f.rows, batch, st);
-    }
-    const SliceMat& m1 = direction == HX_BACKWARD ? p->m1b : p->m1a;
-    const SliceMat& m2 = direction == HX_BACKWARD ? p->m2b : p->m2a;
+    return split_mft_run(p, direction, batch, input_field(in, in_dtype), nullptr, output_field(out, out_dtype), are,
+                         aim, epilogue, mask, input_field(src, src_dtype), nullptr, nullptr, ws, st);
+}
+
+// Lyot coronagraph (and final image) with float-float fields between the transforms.
+size_t split_lyot_workspace_bytes(const SplitMftPlan* fpm, const SplitMftPlan* img, int batch) {
+    const long long pupil = (long long)fpm->nx * fpm->ny, focal = (long long)fpm->nu * fpm->nv;
+    Carver c(nullptr);
+    carve_ff(c, batch * focal);
+    carve_ff(c, batch * pupil);
+    c.take(sizeof(unsigned int) * batch * round_up(fpm->nu, 64));
+    c.take(sizeof(unsigned int) * batch * fpm->ny);
+    const size_t own = c.off + 256;
+    size_t inner = std::max(split_mft_workspace_bytes(fpm, HX_FORWARD, batch),
+                            split_mft_workspace_bytes(fpm, HX_BACKWARD, batch));
+    if (img) inner = std::max(inner, split_mft_workspace_bytes(img, HX_FORWARD, batch));
+    return own + inner + 256;
+}
+
+int split_lyot_execute(const SplitMftPlan* fpm, const SplitMftPlan* img, int batch, const void* e, int e_dtype,
+                       const float2* one_minus_fpm, const float2* stop, double af_re, double af_im, double ab_re,
+                       double ab_im, double ai_re, double ai_im, void* lyot_out, int lyot_dtype, void* img_out,
+                       int img_dtype, void* ws, cudaStream_t st) {
+    const long long pupil = (long long)fpm->nx * fpm->ny, focal = (long long)fpm->nu * fpm->nv;
     Carver c(ws);
-    BwdWs w;
-    carve_bwd(c, p, batch, w);
-    const long long rows = (long long)batch * ny;
-    HX_TRY(cuda_status(cudaMemsetAsync(w.fmax, 0, sizeof(unsigned long long) * batch * nu64, st), "memset"));
-    HX_TRY(cuda_status(cudaMemsetAsync(w.tmax, 0, sizeof(unsigned long long) * rows, st), "memset"));
-    // G1: T[b] = M1 . F[b]  (F sliced by columns), row maxima of T for the next slicing.
-    HX_TRY(launch_colmax(in, nullptr, nullptr, nv, nu, batch, (long long)nv * nu, w.fmax, nu64, st));
-    HX_TRY(launch_slice_cols(in, nullptr, nullptr, nv, nu, batch, (long long)nv * nu, w.fmax, nu64, w.b1, (int)nu64,
-                             st));
-    GemmArgs g1 = base_args(p->status);
-    g1.M = ny;
-    g1.N = nu;
-    g1.b_rows_per_z = (int)nu64;
-    g1.row_scale = m1.scale;
-    g1.col_scale = w.b1.scale;
-    g1.col_scale_z = nu64;
-    g1.out_mode = OUT_F64_PLANES;
-    g1.out_re = w.t_re;
-    g1.out_im = w.t_im;
-    g1.ldo = nu;
-    g1.out_z = (long long)ny * nu;
-    g1.rowmax = w.tmax;
-    g1.rowmax_z = ny;
-    HX_TRY(launch_gemm(g1, m1, w.b1, m1.rows, batch, st));
-    // G2: out = alpha T . M2, stacked over the batch, with the fused epilogue.
-    HX_TRY(launch_slice_rows(nullptr, w.t_re, w.t_im, nu, rows, nu, w.tmax, w.a2, st));
-    GemmArgs g2 = base_args(p->status);
-    g2.M = (int)rows;
-    g2.N = nx;
-    g2.row_scale = w.a2.scale;
-    g2.col_scale = m2.scale;
-    g2.alpha_re = are;
-    g2.alpha_im = aim;
-    g2.out_mode = OUT_C64;
-    g2.out_c64 = out;
-    g2.ldo = nx;
-    g2.epi = epilogue;
-    g2.mask = mask;
-    g2.src = src;
-    g2.rows_per_field = ny;
-    return launch_gemm(g2, w.a2, m2, w.a2.rows, 1, st);
+    FieldIO ef = carve_ff(c, batch * focal);
+    FieldIO lp = carve_ff(c, batch * pupil);
+    const long long nu64 = round_up(fpm->nu, 64);
+    unsigned int* ef_colmax = (unsigned int*)c.take(sizeof(unsigned int) * batch * nu64);
+    unsigned int* lp_rowmax = (unsigned int*)c.take(sizeof(unsigned int) * batch * fpm->ny);
+    void* inner = c.take(0);
+    HX_TRY(cuda_status(cudaMemsetAsync(ef_colmax, 0, sizeof(unsigned int) * batch * nu64, st), "memset"));
+    HX_TRY(cuda_status(cudaMemsetAsync(lp_rowmax, 0, sizeof(unsigned int) * batch * fpm->ny, st), "memset"));
+    FieldIO fe = input_field(e, e_dtype), none;
+    // E_f = P(E) (1 - M), kept in float-float with its column maxima.
+    HX_TRY(split_mft_run(fpm, HX_FORWARD, batch, fe, nullptr, ef, af_re, af_im, HX_EPI_MUL, one_minus_fpm, none,
+                         nullptr, ef_colmax, inner, st));
+    // L = S (E - P^-1(E_f)), in float-float with its row maxima.
+    HX_TRY(split_mft_run(fpm, HX_BACKWARD, batch, ef, ef_colmax, lp, ab_re, ab_im, HX_EPI_BABINET, stop, fe,
+                         lp_rowmax, nullptr, inner, st));
+    if (lyot_out) {
+        const long long n = batch * pupil;
+        field_copy_kernel<<<ceil_div(n, 256), 256, 0, st>>>(lp, output_field(lyot_out, lyot_dtype), n);
+        HX_TRY(launch_status("field_copy_kernel"));
+    }
+    if (img) {
+        HX_TRY(split_mft_run(img, HX_FORWARD, batch, lp, lp_rowmax, output_field(img_out, img_dtype), ai_re, ai_im,
+                             HX_EPI_NONE, nullptr, none, nullptr, nullptr, inner, st));
+    }
+    return HX_OK;
 }
 
 int split_mft_status(const SplitMftPlan* p, int reset) {

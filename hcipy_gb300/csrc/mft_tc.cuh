@@ -12,9 +12,18 @@ int split_mft_create(int nx, int ny, int nu, int nv, const double* x, const doub
                      const double* v, const double* wx, const double* wy, const double* wu, const double* wv,
                      cudaStream_t stream, SplitMftPlan** out);
 size_t split_mft_workspace_bytes(const SplitMftPlan* p, int direction, int batch);
-int split_mft_execute(const SplitMftPlan* p, int direction, int batch, const float2* in, float2* out, double are,
-                      double aim, int epilogue, const float2* mask, const float2* src, void* ws, size_t ws_bytes,
-                      cudaStream_t stream);
+// Fields are complex64 or complex128 (dtype HX_C64 / HX_C128), independently for input, output and the
+// Babinet source; the mask is complex64.
+int split_mft_execute(const SplitMftPlan* p, int direction, int batch, const void* in, int in_dtype, void* out,
+                      int out_dtype, double are, double aim, int epilogue, const float2* mask, const void* src,
+                      int src_dtype, void* ws, size_t ws_bytes, cudaStream_t stream);
+// Lyot coronagraph and (if img != NULL) its final image, with the focal-plane and Lyot-plane fields in
+// float-float between the transforms.
+size_t split_lyot_workspace_bytes(const SplitMftPlan* fpm, const SplitMftPlan* img, int batch);
+int split_lyot_execute(const SplitMftPlan* fpm, const SplitMftPlan* img, int batch, const void* e, int e_dtype,
+                       const float2* one_minus_fpm, const float2* stop, double af_re, double af_im, double ab_re,
+                       double ab_im, double ai_re, double ai_im, void* lyot_out, int lyot_dtype, void* img_out,
+                       int img_dtype, void* ws, cudaStream_t stream);
 // Status word of the bounded device waits (HX_OK or HX_ERR_TIMEOUT); synchronizes with the device.
 int split_mft_status(const SplitMftPlan* p, int reset);
 void split_mft_destroy(SplitMftPlan* p);

@@ -156,6 +156,18 @@ class _MftPlan(object):
                                         _lib.dptr(workspace), nbytes, _lib.stream_handle())
         _lib.check(rc, 'hx_mft_execute_ex')
 
+    def execute_io(self, direction, batch, inp, out, alpha, epilogue=_lib.HX_EPI_NONE, mask=None, src=None):
+        """Split plans: complex64 or complex128 input, output and Babinet source (dtype taken from the tensors)."""
+        nbytes = self.workspace_bytes(direction, batch)
+        workspace = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=inp.device)
+        rc = self.lib.hx_mft_execute_io(self.handle, direction, batch, _lib.dptr(inp), _lib.dtype_code(inp.dtype),
+                                        _lib.dptr(out), _lib.dtype_code(out.dtype), float(alpha.real),
+                                        float(alpha.imag), epilogue, None if mask is None else _lib.dptr(mask),
+                                        None if src is None else _lib.dptr(src),
+                                        _lib.dtype_code(src.dtype) if src is not None else _lib.HX_C64,
+                                        _lib.dptr(workspace), nbytes, _lib.stream_handle())
+        _lib.check(rc, 'hx_mft_execute_io')
+
     def status(self, reset=True):
         """Status of the plan's bounded device waits (0 = fine); synchronizes with the device."""
         return int(self.lib.hx_mft_plan_status(self.handle, 1 if reset else 0))
@@ -173,8 +185,9 @@ class MatrixFourierTransform(FourierTransform):
 
     ``precision`` selects the GEMM arithmetic: ``'fp32'`` (default) is the plain
     drop-in (complex64 fields on FP32 CUDA cores, complex128 fields in FP64);
-    ``'split'`` runs complex64 fields on tcgen05 tensor cores with split
-    operands (see ``hx_mft_plan_create``).  ``precompute_matrices`` and
+    ``'split'`` runs on tcgen05 tensor cores with fixed-point fp16 slices and
+    exact sums (~29-bit operands), takes complex64 or complex128 fields and
+    returns complex128, since its results hold more than a complex64 can.  ``precompute_matrices`` and
     ``allocate_intermediate`` are accepted for API compatibility: the phase
     matrices are always kept on the device and the intermediate is scratch from
     torch's caching allocator.
@@ -214,7 +227,9 @@ class MatrixFourierTransform(FourierTransform):
     # -- plans ---------------------------------------------------------------
     def _plan(self, cdt):
         code = _lib.HX_C64 if cdt == torch.complex64 else _lib.HX_C128
-        prec = PRECISIONS[self.precision] if code == _lib.HX_C64 else _lib.HX_PREC_FP32
+        prec = PRECISIONS[self.precision]
+        if prec == _lib.HX_PREC_SPLIT:
+            code = _lib.HX_C64  # split plans take either field dtype
         key = (code, prec)
         plan = self._plans.get(key)
         if plan is None:
@@ -227,16 +242,22 @@ class MatrixFourierTransform(FourierTransform):
         t = _prepare_input(field, src_grid)
         batch_shape = tuple(t.shape[:-1])
         batch = int(np.prod(batch_shape)) if batch_shape else 1
+        split = self.precision == 'split'
         if out is None:
-            out = torch.empty(batch_shape + (dst_grid.size,), dtype=t.dtype, device=t.device)
+            out_dtype = torch.complex128 if split else t.dtype
+            out = torch.empty(batch_shape + (dst_grid.size,), dtype=out_dtype, device=t.device)
         if mask is not None:
-            mask = _broadcast_mask(mask, dst_grid, t.dtype)
+            mask = _broadcast_mask(mask, dst_grid, torch.complex64 if split else t.dtype)
         if src is not None:
-            src = src.to(t.dtype).contiguous()
+            src = src.contiguous() if split else src.to(t.dtype).contiguous()
             if tuple(src.shape) != tuple(out.shape):
                 src = src.expand(out.shape).contiguous()
         if batch > 0:
-            self._plan(t.dtype).execute(direction, batch, t, out, alpha, epilogue=epilogue, mask=mask, src=src)
+            plan = self._plan(t.dtype)
+            if self.precision == 'split':
+                plan.execute_io(direction, batch, t, out, alpha, epilogue=epilogue, mask=mask, src=src)
+            else:
+                plan.execute(direction, batch, t, out, alpha, epilogue=epilogue, mask=mask, src=src)
         return Field(out, dst_grid)
 
     # -- operator API ----------------------------------------------------------

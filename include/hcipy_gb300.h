@@ -113,6 +113,39 @@ HX_API int hx_mft_execute_ex(const hx_mft_plan* plan, int direction, int batch,
 
 HX_API int hx_mft_plan_destroy(hx_mft_plan* plan);
 
+/* hx_mft_execute_ex with independent element types (HX_C64 / HX_C128) for the
+ * input, the output and the Babinet source.  Plain plans (HX_PREC_FP32) accept
+ * only their own dtype.  Split plans take complex64 or complex128 fields; their
+ * results carry ~29-bit operands through exact sums, so writing complex128
+ * keeps what a complex64 store would round away.  The mask is complex64 for
+ * split plans and the plan's dtype otherwise. */
+HX_API int hx_mft_execute_io(const hx_mft_plan* plan, int direction, int batch,
+                      const void* in, int in_dtype, void* out, int out_dtype,
+                      double alpha_re, double alpha_im, int epilogue, const void* mask,
+                      const void* src, int src_dtype, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Lyot coronagraph and its final image in one call.
+ * Replaces LyotCoronagraph.forward (hcipy/coronagraphy/lyot.py:66-92) followed by
+ * FraunhoferPropagator.forward (hcipy/propagation/fraunhofer.py:56-71):
+ *   E_f   = alpha_fwd * MFT_fpm(E) * (1 - M)
+ *   lyot  = stop * (E - alpha_bwd * MFT_fpm^-1(E_f))
+ *   image = alpha_img * MFT_img(lyot)
+ * fpm_plan maps the pupil to the focal-plane-mask grid, img_plan (or NULL) the
+ * pupil to the image grid; both share the pupil and the precision.  lyot_out
+ * and/or image_out receive the results (either may be NULL, not both).  With
+ * split plans E_f and lyot stay in float-float between the transforms.
+ * one_minus_fpm and stop are complex64 for split plans and the plan dtype
+ * otherwise; stop may be NULL (no Lyot stop).
+ * ------------------------------------------------------------------------ */
+HX_API size_t hx_lyot_workspace_bytes(const hx_mft_plan* fpm_plan, const hx_mft_plan* img_plan, int batch);
+HX_API int hx_lyot_execute(const hx_mft_plan* fpm_plan, const hx_mft_plan* img_plan, int batch,
+                    const void* e, int e_dtype, const void* one_minus_fpm, const void* stop,
+                    double alpha_fwd_re, double alpha_fwd_im, double alpha_bwd_re, double alpha_bwd_im,
+                    double alpha_img_re, double alpha_img_im,
+                    void* lyot_out, int lyot_dtype, void* image_out, int image_dtype,
+                    void* workspace, size_t workspace_bytes, void* stream);
+
 /* Status of the plan's bounded device-side waits since the last reset: HX_OK, or
  * HX_ERR_TIMEOUT when a wait of the tensor-core GEMM gave up (its CTA then
  * returned without writing).  Synchronizes with the device; reset != 0 clears it. */

@@ -3,9 +3,12 @@
 The split form cuts every operand into fixed-point slices (6, 11, 11 bits) and
 sums the kept slice products exactly, so its error does not grow with the
 transform length as FP32 accumulation does.  Tolerances:
-  device result vs the numpy model of the split arithmetic : 1e-12 relative (same arithmetic)
-  MFT fields, relative L2 vs float64                       : 1e-7 (~2^-29 per element, then complex64 output)
-  Lyot dark hole (3-15 lambda/D), 512^2 pupil              : max |NI - NI_fp64| < 1.5e-11 and < 1/5 of FP32's
+  device result vs the numpy model of the split arithmetic : 2e-8 relative (same slices of the inputs; the device
+                                                             slices the float-float intermediate in FP32, which
+                                                             can move the last slice of an element by one unit;
+                                                             a wrong level or scale shows at 1e-4 or worse)
+  MFT fields (complex128 results), relative L2 vs float64  : 2e-8 (~2^-29 per operand element)
+  Lyot dark hole (3-15 lambda/D), 512^2 pupil              : max |NI - NI_fp64| < 5e-12 and < 1/20 of FP32's
 """
 import numpy as np
 import pytest
@@ -39,9 +42,9 @@ def test_split_mft_forward_small():
                                pupil.weights)
     assert split._plan(torch.complex64).status() == 0
     model = split_model.mft_forward(e.cpu().numpy(), g['in_x'], g['in_y'], g['out_x'], g['out_y'], pupil.weights)
-    # The device computes the model's arithmetic; only the complex64 output rounding remains.
-    assert rel_err(out, model.astype(np.complex64)) < 1e-12
-    assert rel_err(out, ref) < 1e-7
+    assert out.dtype == np.complex128
+    assert rel_err(out, model) < 2e-8
+    assert rel_err(out, ref) < 2e-8
 
 
 @pytest.mark.parametrize('case', ['mft_0', 'mft_1', 'mft_2'])
@@ -59,7 +62,7 @@ def test_split_mft_all_directions(case):
         (split.adjoint(f), plain.adjoint(f), ofourier.mft_adjoint(f.astype(complex), x, y, u, v, pupil.weights)),
     ]
     for got, fp32, ref in checks:
-        assert rel_err(got.numpy(), ref) < 1e-7
+        assert rel_err(got.numpy(), ref) < 2e-8
     assert split._plan(torch.complex64).status() == 0
 
 
@@ -77,12 +80,12 @@ def test_split_mft_batched_and_nonuniform():
     for i in range(2):
         for j in range(3):
             ref = ofourier.mft_forward(e[i, j].astype(complex), xg, yg, ug, vg, gi.weights)
-            assert rel_err(out[i, j], ref) < 1e-7
+            assert rel_err(out[i, j], ref) < 2e-8
     f = (rng.standard_normal((4, go.size)) + 1j * rng.standard_normal((4, go.size))).astype(np.complex64)
     back = split.backward(f).numpy()
     for i in range(4):
         ref = ofourier.mft_backward(f[i].astype(complex), xg, yg, ug, vg, go.weights)
-        assert rel_err(back[i], ref) < 1e-7
+        assert rel_err(back[i], ref) < 2e-8
     assert split._plan(torch.complex64).status() == 0
 
 
@@ -107,5 +110,5 @@ def _lyot_ni_errors(n):
 
 def test_split_lyot_dark_hole_512():
     errs = _lyot_ni_errors(512)
-    assert errs['split'][0] < 1.5e-11, errs
-    assert errs['split'][0] < errs['fp32'][0] / 5, errs
+    assert errs['split'][0] < 5e-12, errs
+    assert errs['split'][0] < errs['fp32'][0] / 20, errs
