@@ -23,15 +23,21 @@
 // of an MFT, and between the MFTs of a coronagraph, as float-float planes
 // (hi and lo of Re and Im); slicing reads them with FP32 operations only.
 //
-// Kernel.  One CTA computes 64 complex rows x 64 columns of C: a 128-row tile of
-// A' (the 64 Cr rows then their 64 Ci rows) times a 64-row tile of B'.
-// warp 0 issues TMA loads (one 3-D box per operand per stage: three slice
-// planes of 64 K-elements, 128-byte swizzle), warp 1 issues tcgen05.mma
-// (8 slice products x 4 K16 steps per stage) into four TMEM accumulators of
-// 128 lanes x 64 columns, warps 2-5 read TMEM, combine and finish the result.
-// Three pipeline stages of 72 KiB.  All waits are bounded by the global timer:
-// a wait that runs out records HX_ERR_TIMEOUT in the plan's status word, the
-// CTA drains its own copies and MMAs, frees its TMEM and returns.
+// Kernel.  One CTA computes 64 complex rows x BN columns of C (BN = 64 or 128):
+// a 128-row tile of A' (the 64 Cr rows then their 64 Ci rows) times a BN-row
+// tile of B'.  warp 0 issues TMA loads (one 3-D box per operand per stage:
+// three slice planes of 64 K-elements, 128-byte swizzle), warp 1 issues
+// tcgen05.mma (8 slice products x 4 K16 steps per stage) into four TMEM
+// accumulators of 128 lanes x BN columns, warps 2-9 read TMEM, combine and
+// finish the result.  Three stages of 72 KiB (BN = 64) or two of 96 KiB
+// (BN = 128).  GEMMs with too few tiles to fill the GPU split K across CTAs:
+// each CTA combines its levels into a float-float partial (level 0 exactly),
+// and the last CTA of a tile (counted with an atomic) adds the partials in
+// split order with float-float additions (error ~2^-47 of a partial, far below
+// the 2^-29 slice truncation) and runs the epilogue.  All waits are
+// bounded by the global timer: a wait that runs out records HX_ERR_TIMEOUT in
+// the plan's status word, the CTA drains its own copies and MMAs, frees its
+// TMEM and returns.
 #include "hx_common.cuh"
 #include "mft_tc.cuh"
 #include "tc_ptx.cuh"
@@ -41,29 +47,35 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <mutex>
 
 namespace hx {
 namespace {
 
 constexpr int BM = 128;  // A' rows per tile (64 complex rows)
-constexpr int BN = 64;   // output columns per tile
 constexpr int BK = 64;   // K' elements per stage (128 bytes of fp16)
-constexpr int STAGES = 3;
 constexpr int NSLICE = 3;
 constexpr int A_PLANE_BYTES = BM * BK * 2;
-constexpr int B_PLANE_BYTES = BN * BK * 2;
 constexpr int A_STAGE_BYTES = NSLICE * A_PLANE_BYTES;
-constexpr int B_STAGE_BYTES = NSLICE * B_PLANE_BYTES;
-constexpr int STAGE_BYTES = A_STAGE_BYTES + B_STAGE_BYTES;
-constexpr int EPI_PITCH = BN + 1;  // staging row pitch in floats (bank spread)
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-constexpr int TMEM_COLS = 256;  // four level accumulators of BN columns
-constexpr int NUM_THREADS = 192;
+constexpr int NUM_THREADS = 320;  // TMA warp, MMA warp, 8 epilogue warps
 constexpr uint64_t WAIT_LIMIT = 2000000000ull;  // 2 s per wait
 constexpr int MAX_KPITCH = 4096;                // exact level-0 sums need K' <= 4096
+constexpr int EXTRA_BYTES = 1024 + 1280;        // alignment slack, barriers, flags, per-row tables
 
-static_assert(2 * BM * EPI_PITCH * 4 <= STAGES * STAGE_BYTES, "epilogue staging must fit the pipeline buffers");
+// Tile of BN output columns: four level accumulators of BN TMEM columns each, so BN = 128 takes all
+// 512 columns of the SM.  Stage count fills the shared memory.
+template <int BN> struct Tile {
+    static constexpr int B_PLANE_BYTES = BN * BK * 2;
+    static constexpr int STAGE_BYTES = A_STAGE_BYTES + NSLICE * B_PLANE_BYTES;
+    static constexpr int STAGES = BN == 64 ? 3 : 2;
+    static constexpr int PIPE_BYTES = STAGES * STAGE_BYTES;
+    static constexpr int SMEM_BYTES = PIPE_BYTES + EXTRA_BYTES;
+    static constexpr int TMEM_COLS = 4 * BN;
+    static constexpr int PITCH = BN + 1;  // epilogue staging row pitch in floats (bank spread)
+    static_assert(2 * BM * PITCH * 4 <= PIPE_BYTES, "epilogue staging must fit the pipeline buffers");
+    static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
+};
 
 // ---- float-float arithmetic (error-free transformations in FP32) -------------------------------------
 
@@ -162,7 +174,9 @@ __device__ __forceinline__ void store_field(const FieldIO& f, long long i, cff v
 struct __align__(64) GemmArgs {
     CUtensorMap tmap_a;
     CUtensorMap tmap_b;
-    int ktiles;
+    int ktiles;            // K' / BK
+    int ksplit;            // CTAs along K per output tile
+    int n_tiles;           // output column tiles (grid x = n_tiles * ksplit)
     int a_rows_per_z;      // A' row offset per grid z (0: shared A)
     int b_rows_per_z;      // B' row offset per grid z (0: shared B)
     int M, N;              // valid complex rows / columns of the output (per z)
@@ -183,6 +197,8 @@ struct __align__(64) GemmArgs {
     long long colmax_field_stride;
     unsigned int* rowmax;  // per output row
     long long rowmax_z;
+    float* partial;        // split K: float-float partial of every split of every tile
+    unsigned int* counters;  // split K: finished splits per tile (zero before the launch)
     int* status;
 };
 
@@ -191,18 +207,37 @@ __device__ __forceinline__ void raise_status(int* status, volatile int* abort_fl
     if (status) atomicExch(status, HX_ERR_TIMEOUT);
 }
 
+// The four level sums of one element as float-float: level 0 is an exact integer and the level weights are
+// powers of two, so only the additions round.
+__device__ __forceinline__ ff combine_levels(float v0, float v1, float v2, float v3) {
+    const ff s = two_sum(v0 * 0x1p-12f, v1 * 0x1p-23f);
+    return two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(v2 * 0x1p-34f, v3 * 0x1p-45f)));
+}
+
+template <int BN>
 __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid_constant__ GemmArgs g) {
+    using T = Tile<BN>;
+    constexpr int STAGES = T::STAGES;
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     const uint32_t raw_addr = ptx::smem_addr(smem_raw);
     uint8_t* smem = smem_raw + ((1024 - (raw_addr & 1023)) & 1023);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+    uint8_t* extra = smem + T::PIPE_BYTES;
     // bars[0..S): full, bars[S..2S): empty, bars[2S]: accumulators ready
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 2);
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(extra);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(extra + 64);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(extra + 68);
+    volatile int* last_flag = reinterpret_cast<volatile int*>(extra + 72);
+    unsigned int* s_rowmax = reinterpret_cast<unsigned int*>(extra + 128);  // per tile row (64)
+    float* s_rscale = reinterpret_cast<float*>(extra + 384);                // row scales
+    int* s_maskrow = reinterpret_cast<int*>(extra + 640);                   // m % rows_per_field
+    int* s_field = reinterpret_cast<int*>(extra + 896);                     // m / colmax_rows_per_field
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const int n_tile = blockIdx.x, m_tile = blockIdx.y, z = blockIdx.z;
+    const int n_tile = blockIdx.x % g.n_tiles, ks = blockIdx.x / g.n_tiles;
+    const int m_tile = blockIdx.y, z = blockIdx.z;
+    const int kt0 = (int)((long long)g.ktiles * ks / g.ksplit);
+    const int nkt = (int)((long long)g.ktiles * (ks + 1) / g.ksplit) - kt0;
 
     auto bar_full = [&](int s) { return ptx::smem_addr(&bars[s]); };
     auto bar_empty = [&](int s) { return ptx::smem_addr(&bars[STAGES + s]); };
@@ -215,10 +250,20 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
         }
         ptx::mbar_init(bar_accum, 1);
         *abort_flag = 0;
+        *last_flag = 0;
         ptx::fence_mbar_init();
     }
+    if (threadIdx.x >= 64 && threadIdx.x < 128) {
+        const int r = threadIdx.x - 64;
+        const int m = m_tile * 64 + r;
+        const bool ok = m < g.M;
+        s_rowmax[r] = 0u;
+        s_rscale[r] = ok ? g.row_scale[z * g.row_scale_z + m] : 0.0f;
+        s_maskrow[r] = ok ? m % g.rows_per_field : 0;
+        s_field[r] = (ok && g.colmax_rows_per_field > 0) ? m / g.colmax_rows_per_field : 0;
+    }
     if (warp == 1) {
-        ptx::tmem_alloc(ptx::smem_addr(tmem_slot), TMEM_COLS);
+        ptx::tmem_alloc(ptx::smem_addr(tmem_slot), T::TMEM_COLS);
         ptx::tmem_relinquish();
     }
     ptx::tc_fence_before();
@@ -232,19 +277,19 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
             for (int s = 0; s < STAGES; ++s) last_use[s] = -1;
             const int a_row0 = m_tile * BM + z * g.a_rows_per_z;
             const int b_row0 = n_tile * BN + z * g.b_rows_per_z;
-            for (int kt = 0; kt < g.ktiles; ++kt) {
+            for (int i = 0; i < nkt; ++i) {
                 if (*abort_flag) break;
-                const int s = kt % STAGES;
-                const int u = kt / STAGES;
+                const int s = i % STAGES;
+                const int u = i / STAGES;
                 if (u > 0 && !ptx::mbar_wait_bounded(bar_empty(s), (u - 1) & 1, WAIT_LIMIT)) {
                     raise_status(g.status, abort_flag);
                     break;
                 }
-                uint8_t* sa = smem + s * STAGE_BYTES;
+                uint8_t* sa = smem + s * T::STAGE_BYTES;
                 uint8_t* sb = sa + A_STAGE_BYTES;
-                ptx::mbar_arrive_expect_tx(bar_full(s), STAGE_BYTES);
-                ptx::tma_load_3d(ptx::smem_addr(sa), &g.tmap_a, kt * BK, a_row0, 0, bar_full(s));
-                ptx::tma_load_3d(ptx::smem_addr(sb), &g.tmap_b, kt * BK, b_row0, 0, bar_full(s));
+                ptx::mbar_arrive_expect_tx(bar_full(s), T::STAGE_BYTES);
+                ptx::tma_load_3d(ptx::smem_addr(sa), &g.tmap_a, (kt0 + i) * BK, a_row0, 0, bar_full(s));
+                ptx::tma_load_3d(ptx::smem_addr(sb), &g.tmap_b, (kt0 + i) * BK, b_row0, 0, bar_full(s));
                 last_use[s] = u;
             }
             // No copy may land in shared memory after this CTA exits.
@@ -261,24 +306,24 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
             const int pb[NPROD] = {0, 1, 0, 2, 1, 0, 2, 1};
             const int pl[NPROD] = {0, 1, 1, 2, 2, 2, 3, 3};
             const int first[NPROD] = {1, 1, 0, 1, 0, 0, 1, 0};
-            for (int kt = 0; kt < g.ktiles; ++kt) {
+            for (int i = 0; i < nkt; ++i) {
                 if (*abort_flag) break;
-                const int s = kt % STAGES;
-                const int u = kt / STAGES;
+                const int s = i % STAGES;
+                const int u = i / STAGES;
                 if (!ptx::mbar_wait_bounded(bar_full(s), u & 1, WAIT_LIMIT)) {
                     raise_status(g.status, abort_flag);
                     break;
                 }
                 ptx::tc_fence_after();
-                const uint32_t a0 = ptx::smem_addr(smem + s * STAGE_BYTES);
+                const uint32_t a0 = ptx::smem_addr(smem + s * T::STAGE_BYTES);
                 const uint32_t b0 = a0 + A_STAGE_BYTES;
 #pragma unroll
                 for (int kk = 0; kk < BK / 16; ++kk) {
 #pragma unroll
                     for (int p = 0; p < NPROD; ++p) {
                         const uint64_t ad = ptx::umma_desc_sw128(a0 + pa[p] * A_PLANE_BYTES + kk * 32);
-                        const uint64_t bd = ptx::umma_desc_sw128(b0 + pb[p] * B_PLANE_BYTES + kk * 32);
-                        const uint32_t acc = (kt > 0 || kk > 0 || !first[p]) ? 1u : 0u;
+                        const uint64_t bd = ptx::umma_desc_sw128(b0 + pb[p] * T::B_PLANE_BYTES + kk * 32);
+                        const uint32_t acc = (i > 0 || kk > 0 || !first[p]) ? 1u : 0u;
                         ptx::umma_f16(tmem + pl[p] * BN, ad, bd, idesc, acc);
                     }
                 }
@@ -290,72 +335,195 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
             if (!ptx::mbar_wait_bounded(bar_accum, 0, WAIT_LIMIT)) raise_status(g.status, abort_flag);
         }
     } else {
-        // ---- epilogue: warps 2..5 ----
-        const int et = threadIdx.x - 64;      // 0..127
-        const int quarter = warp & 3;         // TMEM lane quarter this warp may access
-        const int row = quarter * 32 + lane;  // A' row within the tile = TMEM lane
+        // ---- epilogue: warps 2..9, two per TMEM lane quarter (each takes every other 16-column chunk) ----
+        constexpr int EPI = NUM_THREADS - 64;
+        const int et = threadIdx.x - 64;         // 0..EPI-1
+        const int quarter = warp & 3;            // TMEM lane quarter this warp may access
+        const int half = (warp - 2) >> 2;        // 0 or 1
+        const int row = quarter * 32 + lane;     // A' row within the tile = TMEM lane
         float* st_hi = reinterpret_cast<float*>(smem);
-        float* st_lo = st_hi + BM * EPI_PITCH;
+        float* st_lo = st_hi + BM * T::PITCH;
         if (!ptx::mbar_wait_bounded(bar_accum, 0, WAIT_LIMIT)) raise_status(g.status, abort_flag);
         ptx::tc_fence_after();
         // Warp-uniform decision: the TMEM loads below are .sync.aligned.
         const bool live = __shfl_sync(0xffffffffu, (int)(*abort_flag == 0), 0) != 0;
-        if (live) {
-            const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+        const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+        // Split K: float-float partial per split, [split][hi/lo][column / 4][row][column % 4] (float4 per thread).
+        constexpr long long PART = 2LL * BN * BM;
+        const long long tile = ((long long)z * gridDim.y + m_tile) * g.n_tiles + n_tile;
+        float* part_base = g.ksplit > 1 ? g.partial + tile * g.ksplit * PART : nullptr;
+        auto part_at = [&](int s, int plane, int c4) {
+            return reinterpret_cast<float4*>(part_base + s * PART + ((long long)(plane * (BN / 4) + c4) * BM + row) * 4);
+        };
+        auto own_chunk = [&](int c, ff* r) {
+            float v0[16], v1[16], v2[16], v3[16];
+            ptx::tmem_ld_16(tmem + lane_base + 0 * BN + c * 16, v0);
+            ptx::tmem_ld_16(tmem + lane_base + 1 * BN + c * 16, v1);
+            ptx::tmem_ld_16(tmem + lane_base + 2 * BN + c * 16, v2);
+            ptx::tmem_ld_16(tmem + lane_base + 3 * BN + c * 16, v3);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) r[j] = combine_levels(v0[j], v1[j], v2[j], v3[j]);
+        };
+        bool finish = true;
+        if (g.ksplit > 1) {
+            if (live) {
 #pragma unroll 1
-            for (int c = 0; c < BN / 16; ++c) {
-                float v0[16], v1[16], v2[16], v3[16];
-                ptx::tmem_ld_16(tmem + lane_base + 0 * BN + c * 16, v0);
-                ptx::tmem_ld_16(tmem + lane_base + 1 * BN + c * 16, v1);
-                ptx::tmem_ld_16(tmem + lane_base + 2 * BN + c * 16, v2);
-                ptx::tmem_ld_16(tmem + lane_base + 3 * BN + c * 16, v3);
+                for (int c = half; c < BN / 16; c += 2) {
+                    ff r[16];
+                    own_chunk(c, r);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        __stcg(part_at(ks, 0, c * 4 + q), make_float4(r[4 * q].hi, r[4 * q + 1].hi, r[4 * q + 2].hi, r[4 * q + 3].hi));
+                        __stcg(part_at(ks, 1, c * 4 + q), make_float4(r[4 * q].lo, r[4 * q + 1].lo, r[4 * q + 2].lo, r[4 * q + 3].lo));
+                    }
+                }
+            }
+            __threadfence();
+            ptx::named_barrier(1, EPI);
+            if (et == 0) *last_flag = atomicAdd(&g.counters[tile], 1u) == (unsigned)(g.ksplit - 1) ? 1 : 0;
+            ptx::named_barrier(1, EPI);
+            finish = *last_flag != 0;
+            if (finish && live) {
+                __threadfence();
+#pragma unroll 1
+                for (int c = half; c < BN / 16; c += 2) {
+                    ff own[16], acc[16];
+                    own_chunk(c, own);
+                    // Splits in index order (the sum does not depend on which CTA finishes last); two at a time.
+#pragma unroll 1
+                    for (int s0 = 0; s0 < g.ksplit; s0 += 2) {
+                        float4 ph[2][4], pl[2][4];
+#pragma unroll
+                        for (int d = 0; d < 2; ++d) {
+                            const int s = s0 + d;
+                            if (s < g.ksplit && s != ks) {
+#pragma unroll
+                                for (int q = 0; q < 4; ++q) {
+                                    ph[d][q] = __ldcg(part_at(s, 0, c * 4 + q));
+                                    pl[d][q] = __ldcg(part_at(s, 1, c * 4 + q));
+                                }
+                            }
+                        }
+#pragma unroll
+                        for (int d = 0; d < 2; ++d) {
+                            const int s = s0 + d;
+                            if (s >= g.ksplit) continue;
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) {
+                                ff p = own[j];
+                                if (s != ks) {
+                                    const float4 h = ph[d][j >> 2], l = pl[d][j >> 2];
+                                    const int w = j & 3;
+                                    p = {w == 0 ? h.x : w == 1 ? h.y : w == 2 ? h.z : h.w,
+                                         w == 0 ? l.x : w == 1 ? l.y : w == 2 ? l.z : l.w};
+                                }
+                                acc[j] = s == 0 ? p : ff_add(acc[j], p);
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        st_hi[row * T::PITCH + c * 16 + j] = acc[j].hi;
+                        st_lo[row * T::PITCH + c * 16 + j] = acc[j].lo;
+                    }
+                }
+            }
+        } else if (live) {
+#pragma unroll 1
+            for (int c = half; c < BN / 16; c += 2) {
+                ff r[16];
+                own_chunk(c, r);
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                    // level 0 is an exact integer; scaling by powers of two is exact.
-                    ff s = two_sum(v0[j] * 0x1p-12f, v1[j] * 0x1p-23f);
-                    s = two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(v2[j] * 0x1p-34f, v3[j] * 0x1p-45f)));
-                    st_hi[row * EPI_PITCH + c * 16 + j] = s.hi;
-                    st_lo[row * EPI_PITCH + c * 16 + j] = s.lo;
+                    st_hi[row * T::PITCH + c * 16 + j] = r[j].hi;
+                    st_lo[row * T::PITCH + c * 16 + j] = r[j].lo;
                 }
             }
         }
-        ptx::named_barrier(1, 128);
-        if (live && !*abort_flag) {
+        ptx::named_barrier(1, EPI);
+        const bool run = finish && live && !*abort_flag;
+        if (run) {
             const cff alpha = {{g.alpha[0], g.alpha[1]}, {g.alpha[2], g.alpha[3]}};
+            const bool real_alpha = g.alpha[2] == 0.0f && g.alpha[3] == 0.0f;
+            const bool unit_alpha = real_alpha && g.alpha[0] == 1.0f && g.alpha[1] == 0.0f;
+            const bool babinet = g.epi == HX_EPI_BABINET;
+            const float2* mask = (g.epi == HX_EPI_MUL || babinet) ? g.mask : nullptr;
+            const bool want_mag = g.colmax || g.rowmax;
+            // Each thread keeps one column; a warp covers 32 consecutive columns of one row.
+            const int nl = et % BN;
+            const int n = n_tile * BN + nl;
+            const bool nok = n < g.N;
+            const float csc = nok ? g.col_scale[z * g.col_scale_z + n] : 0.0f;
+            constexpr int RSTEP = EPI / BN;       // rows per iteration
+            constexpr int ITER = 64 / RSTEP;
+            constexpr int U = 4;                  // rows per batch: loads issued before any store
+            const int r0 = et / BN;
+            int cfield = -1;
+            float cmax = 0.0f;
 #pragma unroll 1
-            for (int i = 0; i < (64 * BN) / 128; ++i) {
-                const int idx = et + 128 * i;
-                const int ml = idx / BN, nl = idx % BN;
-                const int m = m_tile * 64 + ml;
-                const int n = n_tile * BN + nl;
-                if (m >= g.M || n >= g.N) continue;
-                const float sc = g.row_scale[z * g.row_scale_z + m] * g.col_scale[z * g.col_scale_z + n];
-                cff v = {ff{st_hi[ml * EPI_PITCH + nl] * sc, st_lo[ml * EPI_PITCH + nl] * sc},
-                         ff{st_hi[(64 + ml) * EPI_PITCH + nl] * sc, st_lo[(64 + ml) * EPI_PITCH + nl] * sc}};
-                v = cff_mul(v, alpha);
-                const long long o = z * g.out_z + (long long)m * g.ldo + n;
-                if (g.epi == HX_EPI_MUL) {
-                    v = cff_mul_c64(v, g.mask[(long long)(m % g.rows_per_field) * g.N + n]);
-                } else if (g.epi == HX_EPI_BABINET) {
-                    const cff e = load_field(g.src, o);
-                    v = {ff_add(e.re, ff_neg(v.re)), ff_add(e.im, ff_neg(v.im))};
-                    if (g.mask) v = cff_mul_c64(v, g.mask[(long long)(m % g.rows_per_field) * g.N + n]);
+            for (int i0 = 0; i0 < ITER; i0 += U) {
+                cff e[U];
+                float2 mk[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int ml = r0 + RSTEP * (i0 + u);
+                    const int m = m_tile * 64 + ml;
+                    const bool ok = nok && m < g.M;
+                    e[u] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+                    mk[u] = make_float2(1.0f, 0.0f);
+                    if (ok && babinet) e[u] = load_field(g.src, z * g.out_z + (long long)m * g.ldo + n);
+                    if (ok && mask) mk[u] = __ldg(&mask[(long long)s_maskrow[ml] * g.N + n]);
                 }
-                store_field(g.out, o, v);
-                const float mag = fmaxf(fabsf(v.re.hi), fabsf(v.im.hi));
-                if (g.colmax) {
-                    const long long f = g.colmax_rows_per_field > 0 ? m / g.colmax_rows_per_field : 0;
-                    atomicMax(&g.colmax[z * g.colmax_z + f * g.colmax_field_stride + n], __float_as_uint(mag));
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int ml = r0 + RSTEP * (i0 + u);
+                    const int m = m_tile * 64 + ml;
+                    float mag = 0.0f;
+                    if (nok && m < g.M) {
+                        const float sc = s_rscale[ml] * csc;  // product of powers of two: exact
+                        cff v = {ff{st_hi[ml * T::PITCH + nl] * sc, st_lo[ml * T::PITCH + nl] * sc},
+                                 ff{st_hi[(64 + ml) * T::PITCH + nl] * sc, st_lo[(64 + ml) * T::PITCH + nl] * sc}};
+                        if (!unit_alpha) v = real_alpha ? cff{ff_mul(v.re, alpha.re), ff_mul(v.im, alpha.re)}
+                                                        : cff_mul(v, alpha);
+                        if (babinet) v = {ff_add(e[u].re, ff_neg(v.re)), ff_add(e[u].im, ff_neg(v.im))};
+                        if (mask) v = mk[u].y == 0.0f ? cff{ff_mulf(v.re, mk[u].x), ff_mulf(v.im, mk[u].x)}
+                                                      : cff_mul_c64(v, mk[u]);
+                        store_field(g.out, z * g.out_z + (long long)m * g.ldo + n, v);
+                        if (want_mag) mag = fmaxf(fabsf(v.re.hi), fabsf(v.im.hi));
+                        if (g.colmax) {
+                            const int f = s_field[ml];
+                            if (f != cfield) {
+                                if (cfield >= 0 && cmax > 0.0f)
+                                    atomicMax(&g.colmax[z * g.colmax_z + cfield * g.colmax_field_stride + n],
+                                              __float_as_uint(cmax));
+                                cfield = f;
+                                cmax = 0.0f;
+                            }
+                            cmax = fmaxf(cmax, mag);
+                        }
+                    }
+                    if (g.rowmax) {
+                        float wm = mag;
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+                        if (lane == 0 && wm > 0.0f) atomicMax(&s_rowmax[ml], __float_as_uint(wm));
+                    }
                 }
-                if (g.rowmax) atomicMax(&g.rowmax[z * g.rowmax_z + m], __float_as_uint(mag));
             }
+            if (g.colmax && cfield >= 0 && cmax > 0.0f)
+                atomicMax(&g.colmax[z * g.colmax_z + cfield * g.colmax_field_stride + n], __float_as_uint(cmax));
+        }
+        ptx::named_barrier(1, EPI);
+        if (run && g.rowmax && et < 64) {
+            const int m = m_tile * 64 + et;
+            if (m < g.M && s_rowmax[et] != 0u) atomicMax(&g.rowmax[z * g.rowmax_z + m], s_rowmax[et]);
         }
     }
     ptx::tc_fence_before();
     __syncthreads();
     if (warp == 1) {
         ptx::tc_fence_after();
-        ptx::tmem_dealloc(tmem, TMEM_COLS);
+        ptx::tmem_dealloc(tmem, T::TMEM_COLS);
     }
 }
 
@@ -413,21 +581,30 @@ __global__ void slice_rows_kernel(FieldIO src, long long ld, int K, int Kp, cons
     const float inv = 1.0f / s_scale;
     const long long r_cr = (long long)(m / 64) * 128 + (m % 64);
     const long long r_ci = r_cr + 64;
-    for (int k = threadIdx.x; k < Kp; k += blockDim.x) {
-        cff v = {{0.0f, 0.0f}, {0.0f, 0.0f}};
-        if (k < K) v = load_field(src, (long long)m * ld + k);
-        __half r0, r1, r2, i0, i1, i2;
-        slice3(v.re, inv, r0, r1, r2);
-        slice3(v.im, inv, i0, i1, i2);
-        const __half rs[3] = {r0, r1, r2};
-        const __half is[3] = {i0, i1, i2};
+    // Four consecutive K-elements per thread: 8-byte stores into each plane (Kp and kpitch are multiples of 32).
+    for (int k0 = 4 * threadIdx.x; k0 < Kp; k0 += 4 * blockDim.x) {
+        __half rs[3][4], is[3][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            cff v = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+            if (k0 + j < K) v = load_field(src, (long long)m * ld + k0 + j);
+            slice3(v.re, inv, rs[0][j], rs[1][j], rs[2][j]);
+            slice3(v.im, inv, is[0][j], is[1][j], is[2][j]);
+        }
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
             __half* pl = planes + p * plane_stride;
-            pl[r_cr * kpitch + k] = rs[p];
-            pl[r_cr * kpitch + Kp + k] = __hneg(is[p]);
-            pl[r_ci * kpitch + k] = is[p];
-            pl[r_ci * kpitch + Kp + k] = rs[p];
+            __half2 re01 = __halves2half2(rs[p][0], rs[p][1]), re23 = __halves2half2(rs[p][2], rs[p][3]);
+            __half2 im01 = __halves2half2(is[p][0], is[p][1]), im23 = __halves2half2(is[p][2], is[p][3]);
+            __half2 ni01 = __hneg2(im01), ni23 = __hneg2(im23);
+            *reinterpret_cast<uint2*>(pl + r_cr * kpitch + k0) =
+                make_uint2(*reinterpret_cast<uint32_t*>(&re01), *reinterpret_cast<uint32_t*>(&re23));
+            *reinterpret_cast<uint2*>(pl + r_cr * kpitch + Kp + k0) =
+                make_uint2(*reinterpret_cast<uint32_t*>(&ni01), *reinterpret_cast<uint32_t*>(&ni23));
+            *reinterpret_cast<uint2*>(pl + r_ci * kpitch + k0) =
+                make_uint2(*reinterpret_cast<uint32_t*>(&im01), *reinterpret_cast<uint32_t*>(&im23));
+            *reinterpret_cast<uint2*>(pl + r_ci * kpitch + Kp + k0) =
+                make_uint2(*reinterpret_cast<uint32_t*>(&re01), *reinterpret_cast<uint32_t*>(&re23));
         }
     }
 }
@@ -509,11 +686,16 @@ __global__ void phase_planes_kernel(int rows, int cols, const double* a, const d
     im_lo[idx] = (float)(im - (double)(float)im);
 }
 
-// Copy between field formats (float-float planes -> complex64 / complex128).
+// Copy between field formats (float-float planes -> complex64 / complex128), two elements per thread.
 __global__ void field_copy_kernel(FieldIO src, FieldIO dst, long long n) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    store_field(dst, i, load_field(src, i));
+    const long long i = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+    if (i + 1 < n) {
+        const cff a = load_field(src, i), b = load_field(src, i + 1);
+        store_field(dst, i, a);
+        store_field(dst, i + 1, b);
+    } else if (i < n) {
+        store_field(dst, i, load_field(src, i));
+    }
 }
 
 // ---- host side ------------------------------------------------------------------------------------
@@ -626,31 +808,88 @@ void set_alpha(GemmArgs& g, double re, double im) {
     g.alpha[3] = (float)(im - (double)g.alpha[2]);
 }
 
-int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, long long a_tile_rows, int grid_z,
-                cudaStream_t st) {
+int sm_count() {
+    static int cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+    if (cache[dev] == 0) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev] = n > 0 ? n : 148;
+    }
+    return cache[dev];
+}
+
+// Tile width and K split of one GEMM.
+struct TileChoice {
+    int bn = 128;
+    int ksplit = 1;
+    int n_tiles = 1;
+    long long tiles = 0;  // output tiles over all grid z
+    size_t partial_floats() const { return ksplit > 1 ? (size_t)tiles * ksplit * 2 * bn * BM : 0; }
+};
+
+// BN = 128 halves the A traffic per product against BN = 64; a GEMM with fewer output tiles than SMs splits
+// K so that the grid fills the GPU, keeping at least four K-steps per CTA.  HX_SPLIT_TILE="bn[,ksplit]"
+// overrides the choice (tuning).
+TileChoice choose_tile(long long m_tiles, int N, int grid_z, int ktiles) {
+    static int forced_bn = 0, forced_split = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const char* e = getenv("HX_SPLIT_TILE");
+        int bn = 0, ks = 0;
+        const int n = e ? sscanf(e, "%d,%d", &bn, &ks) : 0;
+        if (n >= 1 && (bn == 64 || bn == 128)) forced_bn = bn;
+        if (n == 2 && ks >= 1) forced_split = ks;
+    });
+    TileChoice c;
+    c.bn = forced_bn ? forced_bn : (N <= 64 ? 64 : 128);
+    c.n_tiles = (int)ceil_div(N, c.bn);
+    c.tiles = m_tiles * c.n_tiles * grid_z;
+    const int sms = sm_count();
+    if (forced_split) c.ksplit = forced_split;
+    else if (c.tiles < sms) c.ksplit = (int)(sms / c.tiles);
+    c.ksplit = std::max(1, std::min(c.ksplit, std::max(1, ktiles / 4)));
+    return c;
+}
+
+template <int BN> int launch_tile(const GemmArgs& g, dim3 grid, cudaStream_t st) {
+    static bool configured[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || !configured[dev]) {
+        HX_TRY(cuda_status(cudaFuncSetAttribute(split_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                Tile<BN>::SMEM_BYTES),
+                           "cudaFuncSetAttribute(split_gemm_kernel)"));
+        if (dev >= 0 && dev < 64) configured[dev] = true;
+    }
+    split_gemm_kernel<BN><<<grid, NUM_THREADS, Tile<BN>::SMEM_BYTES, st>>>(g);
+    return launch_status("split_gemm_kernel");
+}
+
+// partial / counters: workspace for a split-K choice (unused when c.ksplit == 1).
+int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, const TileChoice& c, int grid_z,
+                float* partial, unsigned int* counters, cudaStream_t st) {
     if (A.kpitch != B.kpitch) {
         set_error("internal: split GEMM K mismatch (%d vs %d)", A.kpitch, B.kpitch);
         return HX_ERR_INVALID;
     }
-    HX_TRY(encode_map(&g.tmap_a, A, BM));
-    HX_TRY(encode_map(&g.tmap_b, B, BN));
-    g.ktiles = A.kpitch / BK;
-    const long long m_tiles = a_tile_rows / BM;
-    const int n_tiles = ceil_div(g.N, BN);
-    static bool configured = false;
-    if (!configured) {
-        HX_TRY(cuda_status(cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                SMEM_BYTES),
-                           "cudaFuncSetAttribute(split_gemm_kernel)"));
-        configured = true;
-    }
-    if (m_tiles > 65535 || grid_z > 65535) {
+    const long long m_tiles = A.rows / BM;
+    if (m_tiles > 65535 || grid_z > 65535 || (long long)c.n_tiles * c.ksplit > 2147483647LL) {
         set_error("split GEMM grid too large");
         return HX_ERR_UNSUPPORTED;
     }
-    dim3 grid(n_tiles, (unsigned)m_tiles, grid_z);
-    split_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, st>>>(g);
-    return launch_status("split_gemm_kernel");
+    HX_TRY(encode_map(&g.tmap_a, A, BM));
+    HX_TRY(encode_map(&g.tmap_b, B, c.bn));
+    g.ktiles = A.kpitch / BK;
+    g.ksplit = c.ksplit;
+    g.n_tiles = c.n_tiles;
+    g.partial = partial;
+    g.counters = counters;
+    if (c.ksplit > 1)
+        HX_TRY(cuda_status(cudaMemsetAsync(counters, 0, sizeof(unsigned int) * c.tiles, st), "memset counters"));
+    dim3 grid((unsigned)(c.n_tiles * c.ksplit), (unsigned)m_tiles, grid_z);
+    return c.bn == 64 ? launch_tile<64>(g, grid, st) : launch_tile<128>(g, grid, st);
 }
 
 GemmArgs base_args(int* status) {
@@ -708,30 +947,41 @@ int slice_phase(int rows, int cols, const double* a, const double* b, double sig
     return rc;
 }
 
-// Workspace of one direction: operand slices, the float-float intermediate and the max arrays.
+// Workspace of one direction: operand slices, the float-float intermediate, the max arrays and the split-K
+// partials (shared by the two GEMMs, which run one after the other on the stream).
 struct Ws {
     unsigned int* in_max = nullptr;  // input column maxima (backward only)
     SliceMat s1;                     // sliced input operand of the first GEMM
     FieldIO t;                       // float-float intermediate
     unsigned int* t_max = nullptr;   // its column (forward) or row (backward) maxima
     SliceMat s2;                     // sliced intermediate for the second GEMM
+    TileChoice c1, c2;               // tiles of the two GEMMs
+    float* partial = nullptr;
+    unsigned int* counters = nullptr;
 };
 
 void carve_ws(Carver& c, const SplitMftPlan* p, int direction, int batch, Ws& w) {
     const long long rows = (long long)batch * p->ny;
     const long long nu64 = round_up(p->nu, 64);
+    const long long b_rows = round_up(batch * nu64, 128);
     if (direction == HX_FORWARD) {
         carve_slices(c, w.s1, 2 * round_up(rows, 64), p->nx, rows);
         w.t = carve_ff(c, rows * p->nu);
         w.t_max = (unsigned int*)c.take(sizeof(unsigned int) * batch * nu64);
-        carve_slices(c, w.s2, (long long)batch * nu64, p->ny, (long long)batch * nu64);
+        carve_slices(c, w.s2, b_rows, p->ny, b_rows);
+        w.c1 = choose_tile(w.s1.rows / BM, p->nu, 1, w.s1.kpitch / BK);
+        w.c2 = choose_tile(p->m1f.rows / BM, p->nu, batch, p->m1f.kpitch / BK);
     } else {
         w.in_max = (unsigned int*)c.take(sizeof(unsigned int) * batch * nu64);
-        carve_slices(c, w.s1, (long long)batch * nu64, p->nv, (long long)batch * nu64);
+        carve_slices(c, w.s1, b_rows, p->nv, b_rows);
         w.t = carve_ff(c, rows * p->nu);
         w.t_max = (unsigned int*)c.take(sizeof(unsigned int) * rows);
         carve_slices(c, w.s2, 2 * round_up(rows, 64), p->nu, rows);
+        w.c1 = choose_tile(p->m1b.rows / BM, p->nu, batch, p->m1b.kpitch / BK);
+        w.c2 = choose_tile(w.s2.rows / BM, p->nx, 1, w.s2.kpitch / BK);
     }
+    w.partial = (float*)c.take(sizeof(float) * std::max(w.c1.partial_floats(), w.c2.partial_floats()));
+    w.counters = (unsigned int*)c.take(sizeof(unsigned int) * std::max(w.c1.tiles, w.c2.tiles));
 }
 
 // in/out: c64 or float-float fields.  in_max: optional precomputed maxima of the input in the orientation the
@@ -760,7 +1010,7 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
         g1.colmax = w.t_max;
         g1.colmax_rows_per_field = ny;
         g1.colmax_field_stride = nu64;
-        HX_TRY(launch_gemm(g1, w.s1, p->m2f, w.s1.rows, 1, st));
+        HX_TRY(launch_gemm(g1, w.s1, p->m2f, w.c1, 1, w.partial, w.counters, st));
         // G2: out[b] = alpha M1f . T[b] with the fused epilogue.
         HX_TRY(launch_slice_cols(w.t, ny, nu, batch, (long long)ny * nu, w.t_max, nu64, w.s2, (int)nu64, st));
         GemmArgs g2 = base_args(p->status);
@@ -782,7 +1032,7 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
         g2.rowmax_z = nv;
         g2.colmax = out_colmax;
         g2.colmax_z = nu64;
-        return launch_gemm(g2, p->m1f, w.s2, p->m1f.rows, batch, st);
+        return launch_gemm(g2, p->m1f, w.s2, w.c2, batch, w.partial, w.counters, st);
     }
     const SliceMat& m1 = direction == HX_BACKWARD ? p->m1b : p->m1a;
     const SliceMat& m2 = direction == HX_BACKWARD ? p->m2b : p->m2a;
@@ -807,7 +1057,7 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
     g1.out_z = (long long)ny * nu;
     g1.rowmax = w.t_max;
     g1.rowmax_z = ny;
-    HX_TRY(launch_gemm(g1, m1, w.s1, m1.rows, batch, st));
+    HX_TRY(launch_gemm(g1, m1, w.s1, w.c1, batch, w.partial, w.counters, st));
     // G2: out = alpha T . M2, stacked over the batch, with the fused epilogue.
     HX_TRY(launch_slice_rows(w.t, nu, rows, nu, w.t_max, w.s2, st));
     GemmArgs g2 = base_args(p->status);
@@ -826,7 +1076,7 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
     g2.colmax = out_colmax;
     g2.colmax_rows_per_field = ny;
     g2.colmax_field_stride = round_up(nx, 64);
-    return launch_gemm(g2, w.s2, m2, w.s2.rows, 1, st);
+    return launch_gemm(g2, w.s2, m2, w.c2, 1, w.partial, w.counters, st);
 }
 
 }  // namespace
@@ -843,13 +1093,13 @@ int split_mft_create(int nx, int ny, int nu, int nv, const double* x, const doub
     p->nx = nx; p->ny = ny; p->nu = nu; p->nv = nv;
     const bool own_adj = wx || wy || wu || wv;
     auto layout = [&](Carver& c) {
-        carve_slices(c, p->m2f, round_up(nu, 64), nx, round_up(nu, 64));
+        carve_slices(c, p->m2f, round_up(nu, 128), nx, round_up(nu, 64));
         carve_slices(c, p->m1f, 2 * round_up(nv, 64), ny, nv);
         carve_slices(c, p->m1b, 2 * round_up(ny, 64), nv, ny);
-        carve_slices(c, p->m2b, round_up(nx, 64), nu, round_up(nx, 64));
+        carve_slices(c, p->m2b, round_up(nx, 128), nu, round_up(nx, 64));
         if (own_adj) {
             carve_slices(c, p->m1a, 2 * round_up(ny, 64), nv, ny);
-            carve_slices(c, p->m2a, round_up(nx, 64), nu, round_up(nx, 64));
+            carve_slices(c, p->m2a, round_up(nx, 128), nu, round_up(nx, 64));
         }
         p->status = (int*)c.take(sizeof(int));
     };
@@ -955,7 +1205,7 @@ int split_lyot_execute(const SplitMftPlan* fpm, const SplitMftPlan* img, int bat
                          lp_rowmax, nullptr, inner, st));
     if (lyot_out) {
         const long long n = batch * pupil;
-        field_copy_kernel<<<ceil_div(n, 256), 256, 0, st>>>(lp, output_field(lyot_out, lyot_dtype), n);
+        field_copy_kernel<<<ceil_div(n, 512), 256, 0, st>>>(lp, output_field(lyot_out, lyot_dtype), n);
         HX_TRY(launch_status("field_copy_kernel"));
     }
     if (img) {

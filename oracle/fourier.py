@@ -55,7 +55,10 @@ def mft_adjoint(f, x, y, u, v, w_in):
     """The true adjoint of ``mft_forward``: w_in * M1^H . F . M2^H."""
     m1, m2 = mft_matrices(x, y, u, v)
     f = np.asarray(f).reshape(len(v), len(u))
-    return (w_in * ((m1.conj().T @ f) @ m2.conj().T)).ravel()
+    out = (m1.conj().T @ f) @ m2.conj().T
+    if np.ndim(w_in) == 0:
+        return (w_in * out).ravel()
+    return (np.asarray(w_in).reshape(out.shape) * out).ravel()
 
 
 def mft1d_forward(e, x, u, w_in):

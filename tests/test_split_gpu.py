@@ -112,3 +112,20 @@ def test_split_lyot_dark_hole_512():
     errs = _lyot_ni_errors(512)
     assert errs['split'][0] < 5e-12, errs
     assert errs['split'][0] < errs['fp32'][0] / 20, errs
+
+
+@pytest.mark.parametrize('tile', ['64,1', '128,1', '64,3', '128,4'])
+def test_split_tile_configurations(tile):
+    """Both tile widths, with and without split K, against float64 (the heuristic picks one per GEMM)."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    env = dict(os.environ, HX_SPLIT_TILE=tile)
+    res = subprocess.run([sys.executable, os.path.join(here, 'split_tile_case.py')], env=env,
+                         capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr[-2000:]
+    fields = res.stdout.split()
+    errs = [float(x) for x in fields[:-1]]
+    assert int(fields[-1]) == 0
+    assert len(errs) == 6 and max(errs) < 2e-8, errs
