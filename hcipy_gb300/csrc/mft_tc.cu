@@ -61,7 +61,7 @@ constexpr int A_STAGE_BYTES = NSLICE * A_PLANE_BYTES;
 constexpr int NUM_THREADS = 320;  // TMA warp, MMA warp, 8 epilogue warps
 constexpr uint64_t WAIT_LIMIT = 2000000000ull;  // 2 s per wait
 constexpr int MAX_KPITCH = 4096;                // exact level-0 sums need K' <= 4096
-constexpr int EXTRA_BYTES = 1024 + 1280;        // alignment slack, barriers, flags, per-row tables
+constexpr int EXTRA_BYTES = 1024 + 1664;        // alignment slack, barriers, flags, per-row tables
 
 // Tile of BN output columns: four level accumulators of BN TMEM columns each, so BN = 128 takes all
 // 512 columns of the SM.  Stage count fills the shared memory.
@@ -73,7 +73,7 @@ template <int BN> struct Tile {
     static constexpr int SMEM_BYTES = PIPE_BYTES + EXTRA_BYTES;
     static constexpr int TMEM_COLS = 4 * BN;
     static constexpr int PITCH = BN + 1;  // epilogue staging row pitch in floats (bank spread)
-    static_assert(2 * BM * PITCH * 4 <= PIPE_BYTES, "epilogue staging must fit the pipeline buffers");
+    static_assert((2 * BM + 64) * PITCH * 4 <= PIPE_BYTES, "epilogue staging must fit the pipeline buffers");
     static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
 };
 
@@ -141,32 +141,110 @@ struct FieldIO {
     float* im_lo = nullptr;
 };
 
-__device__ __forceinline__ ff split_double(double x) {
-    const float hi = (float)x;
-    return {hi, (float)(x - (double)hi)};
+// Field formats as compile-time tags of the GEMM epilogue.
+enum : int { FMT_NONE = 0, FMT_C64 = 1, FMT_C128 = 2, FMT_FF = 3 };
+
+// float64 -> float-float with integer operations only (the GB300's float64 pipe is narrow): hi is x truncated
+// to 24 bits, lo the remainder rounded to float (|lo| < ulp(hi)).  Magnitudes below 2^-126 read as zero;
+// infinities and NaNs go to hi.
+__device__ __forceinline__ ff double_to_ff(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7ff);
+    const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+    const int ef = e - 896;  // biased float exponent
+    if (e == 0x7ff) return {__uint_as_float(sign | 0x7f800000u | (mant ? 0x400000u : 0u)), 0.0f};
+    if (ef >= 255) return {__uint_as_float(sign | 0x7f800000u), 0.0f};
+    if (ef <= 0) return {__uint_as_float(sign), 0.0f};
+    const float hi = __uint_as_float(sign | ((unsigned int)ef << 23) | (unsigned int)(mant >> 29));
+    // remainder = rem * 2^(ef - 179) = (rem * 2^-64) * 2^(ef - 115): both powers of two are normal floats, and
+    // the product underflows gradually for the smallest hi.
+    float lo = __uint2float_rn((unsigned int)(mant & 0x1FFFFFFFull)) * 0x1p-64f *
+               __uint_as_float((unsigned int)(ef + 12) << 23);
+    if (sign) lo = -lo;
+    return {hi, lo};
 }
 
-__device__ __forceinline__ cff load_field(const FieldIO& f, long long i) {
-    if (f.re_hi) return {{f.re_hi[i], f.re_lo[i]}, {f.im_hi[i], f.im_lo[i]}};
-    if (f.c128) {
-        const double2 v = f.c128[i];
-        return {split_double(v.x), split_double(v.y)};
+// Exact float -> float64 by bit placement (subnormal floats are normalised).
+__device__ __forceinline__ unsigned long long float_bits_to_double_bits(unsigned int fb) {
+    const unsigned long long sign = (unsigned long long)(fb & 0x80000000u) << 32;
+    const unsigned int e = (fb >> 23) & 0xff;
+    unsigned int m = fb & 0x7fffffu;
+    if (e == 0xff) return sign | 0x7ff0000000000000ull | ((unsigned long long)m << 29);
+    if (e == 0) {
+        if (m == 0) return sign;
+        const int sh = __clz(m) - 8;  // bring the leading one to bit 23
+        m = (m << sh) & 0x7fffffu;
+        return sign | ((unsigned long long)(1 - sh + 896) << 52) | ((unsigned long long)m << 29);
     }
-    const float2 v = f.c64[i];
-    return {{v.x, 0.0f}, {v.y, 0.0f}};
+    return sign | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)m << 29);
 }
 
-__device__ __forceinline__ void store_field(const FieldIO& f, long long i, cff v) {
-    if (f.re_hi) {
+// hi + lo as float64 with integer operations only: lo's significand is added in units of hi's float64 ulp
+// (its bits below that unit are dropped, an error under two ulps of the result).  Needs |lo| < 2^6 ulp_64(hi),
+// which holds for every float-float this library produces (|lo| <= ulp_32(hi)).
+__device__ __forceinline__ double ff_to_double(ff v) {
+    const unsigned int hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
+    const int he = (int)((hb >> 23) & 0xff), le = (int)((lb >> 23) & 0xff);
+    if (he == 0 || he == 0xff || le == 0)
+        return __longlong_as_double(
+            (long long)float_bits_to_double_bits((he == 0 && (hb & 0x7fffffffu) == 0u) ? lb : hb));
+    unsigned long long s = (1ull << 52) | ((unsigned long long)(hb & 0x7fffffu) << 29);
+    const unsigned long long lsig = (1ull << 23) | (lb & 0x7fffffu);
+    const int shift = le - he + 29;
+    const unsigned long long l = shift >= 0 ? lsig << shift : (shift > -40 ? lsig >> -shift : 0ull);
+    s = ((hb ^ lb) >> 31) ? s - l : s + l;
+    int e = he + 896;
+    if (s >= (1ull << 53)) {
+        s >>= 1;
+        ++e;
+    } else if (s < (1ull << 52)) {
+        s <<= 1;
+        --e;
+    }
+    return __longlong_as_double(
+        (long long)(((unsigned long long)(hb & 0x80000000u) << 32) | ((unsigned long long)e << 52) | (s & 0xFFFFFFFFFFFFFull)));
+}
+
+template <int FMT> __device__ __forceinline__ cff load_fmt(const FieldIO& f, long long i) {
+    if constexpr (FMT == FMT_FF) {
+        return {{f.re_hi[i], f.re_lo[i]}, {f.im_hi[i], f.im_lo[i]}};
+    } else if constexpr (FMT == FMT_C128) {
+        const double2 v = f.c128[i];
+        return {double_to_ff(v.x), double_to_ff(v.y)};
+    } else {
+        const float2 v = f.c64[i];
+        return {{v.x, 0.0f}, {v.y, 0.0f}};
+    }
+}
+
+template <int FMT> __device__ __forceinline__ void store_fmt(const FieldIO& f, long long i, cff v) {
+    if constexpr (FMT == FMT_FF) {
         f.re_hi[i] = v.re.hi;
         f.re_lo[i] = v.re.lo;
         f.im_hi[i] = v.im.hi;
         f.im_lo[i] = v.im.lo;
-    } else if (f.c128_out) {
-        f.c128_out[i] = make_double2((double)v.re.hi + (double)v.re.lo, (double)v.im.hi + (double)v.im.lo);
+    } else if constexpr (FMT == FMT_C128) {
+        f.c128_out[i] = make_double2(ff_to_double(v.re), ff_to_double(v.im));
     } else {
         f.c64_out[i] = make_float2(__fadd_rn(v.re.hi, v.re.lo), __fadd_rn(v.im.hi, v.im.lo));
     }
+}
+
+inline int input_fmt(const FieldIO& f) { return f.re_hi ? FMT_FF : f.c128 ? FMT_C128 : f.c64 ? FMT_C64 : FMT_NONE; }
+inline int output_fmt(const FieldIO& f) { return f.re_hi ? FMT_FF : f.c128_out ? FMT_C128 : FMT_C64; }
+
+// Runtime-format forms for the slicing and copy kernels (one format per launch, so the branches are uniform).
+__device__ __forceinline__ cff load_field(const FieldIO& f, long long i) {
+    if (f.re_hi) return load_fmt<FMT_FF>(f, i);
+    if (f.c128) return load_fmt<FMT_C128>(f, i);
+    return load_fmt<FMT_C64>(f, i);
+}
+
+__device__ __forceinline__ void store_field(const FieldIO& f, long long i, cff v) {
+    if (f.re_hi) store_fmt<FMT_FF>(f, i, v);
+    else if (f.c128_out) store_fmt<FMT_C128>(f, i, v);
+    else store_fmt<FMT_C64>(f, i, v);
 }
 
 // ---- the tensor-core GEMM ----------------------------------------------------------------------------
@@ -214,7 +292,8 @@ __device__ __forceinline__ ff combine_levels(float v0, float v1, float v2, float
     return two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(v2 * 0x1p-34f, v3 * 0x1p-45f)));
 }
 
-template <int BN>
+// OUT: format of the result; SRC: format of the Babinet source (FMT_NONE for other epilogues).
+template <int BN, int OUT, int SRC>
 __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid_constant__ GemmArgs g) {
     using T = Tile<BN>;
     constexpr int STAGES = T::STAGES;
@@ -227,10 +306,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(extra + 64);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(extra + 68);
     volatile int* last_flag = reinterpret_cast<volatile int*>(extra + 72);
-    unsigned int* s_rowmax = reinterpret_cast<unsigned int*>(extra + 128);  // per tile row (64)
-    float* s_rscale = reinterpret_cast<float*>(extra + 384);                // row scales
-    int* s_maskrow = reinterpret_cast<int*>(extra + 640);                   // m % rows_per_field
-    int* s_field = reinterpret_cast<int*>(extra + 896);                     // m / colmax_rows_per_field
+    float* s_rscale = reinterpret_cast<float*>(extra + 128);               // per tile row (64): row scale
+    int* s_field = reinterpret_cast<int*>(extra + 384);                    // m / colmax_rows_per_field
+    long long* s_rowoff = reinterpret_cast<long long*>(extra + 640);       // output offset of the row
+    long long* s_maskoff = reinterpret_cast<long long*>(extra + 1152);     // mask offset of the row
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -257,10 +336,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
         const int r = threadIdx.x - 64;
         const int m = m_tile * 64 + r;
         const bool ok = m < g.M;
-        s_rowmax[r] = 0u;
         s_rscale[r] = ok ? g.row_scale[z * g.row_scale_z + m] : 0.0f;
-        s_maskrow[r] = ok ? m % g.rows_per_field : 0;
         s_field[r] = (ok && g.colmax_rows_per_field > 0) ? m / g.colmax_rows_per_field : 0;
+        s_rowoff[r] = z * g.out_z + (long long)m * g.ldo;
+        s_maskoff[r] = ok ? (long long)(m % g.rows_per_field) * g.N : 0;
     }
     if (warp == 1) {
         ptx::tmem_alloc(ptx::smem_addr(tmem_slot), T::TMEM_COLS);
@@ -442,13 +521,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
         }
         ptx::named_barrier(1, EPI);
         const bool run = finish && live && !*abort_flag;
+        // Magnitudes of the tile for the row maxima, after the staging planes.
+        float* s_mag = st_lo + BM * T::PITCH;
         if (run) {
             const cff alpha = {{g.alpha[0], g.alpha[1]}, {g.alpha[2], g.alpha[3]}};
             const bool real_alpha = g.alpha[2] == 0.0f && g.alpha[3] == 0.0f;
             const bool unit_alpha = real_alpha && g.alpha[0] == 1.0f && g.alpha[1] == 0.0f;
-            const bool babinet = g.epi == HX_EPI_BABINET;
-            const float2* mask = (g.epi == HX_EPI_MUL || babinet) ? g.mask : nullptr;
-            const bool want_mag = g.colmax || g.rowmax;
+            const float2* mask = (g.epi == HX_EPI_MUL || g.epi == HX_EPI_BABINET) ? g.mask : nullptr;
             // Each thread keeps one column; a warp covers 32 consecutive columns of one row.
             const int nl = et % BN;
             const int n = n_tile * BN + nl;
@@ -458,6 +537,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
             constexpr int ITER = 64 / RSTEP;
             constexpr int U = 4;                  // rows per batch: loads issued before any store
             const int r0 = et / BN;
+            const int mlim = g.M - m_tile * 64;   // valid rows of this tile
             int cfield = -1;
             float cmax = 0.0f;
 #pragma unroll 1
@@ -467,29 +547,29 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     const int ml = r0 + RSTEP * (i0 + u);
-                    const int m = m_tile * 64 + ml;
-                    const bool ok = nok && m < g.M;
+                    const bool ok = nok && ml < mlim;
                     e[u] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
                     mk[u] = make_float2(1.0f, 0.0f);
-                    if (ok && babinet) e[u] = load_field(g.src, z * g.out_z + (long long)m * g.ldo + n);
-                    if (ok && mask) mk[u] = __ldg(&mask[(long long)s_maskrow[ml] * g.N + n]);
+                    if constexpr (SRC != FMT_NONE) {
+                        if (ok) e[u] = load_fmt<SRC>(g.src, s_rowoff[ml] + n);
+                    }
+                    if (ok && mask) mk[u] = __ldg(&mask[s_maskoff[ml] + n]);
                 }
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     const int ml = r0 + RSTEP * (i0 + u);
-                    const int m = m_tile * 64 + ml;
                     float mag = 0.0f;
-                    if (nok && m < g.M) {
+                    if (nok && ml < mlim) {
                         const float sc = s_rscale[ml] * csc;  // product of powers of two: exact
                         cff v = {ff{st_hi[ml * T::PITCH + nl] * sc, st_lo[ml * T::PITCH + nl] * sc},
                                  ff{st_hi[(64 + ml) * T::PITCH + nl] * sc, st_lo[(64 + ml) * T::PITCH + nl] * sc}};
                         if (!unit_alpha) v = real_alpha ? cff{ff_mul(v.re, alpha.re), ff_mul(v.im, alpha.re)}
                                                         : cff_mul(v, alpha);
-                        if (babinet) v = {ff_add(e[u].re, ff_neg(v.re)), ff_add(e[u].im, ff_neg(v.im))};
+                        if constexpr (SRC != FMT_NONE) v = {ff_add(e[u].re, ff_neg(v.re)), ff_add(e[u].im, ff_neg(v.im))};
                         if (mask) v = mk[u].y == 0.0f ? cff{ff_mulf(v.re, mk[u].x), ff_mulf(v.im, mk[u].x)}
                                                       : cff_mul_c64(v, mk[u]);
-                        store_field(g.out, z * g.out_z + (long long)m * g.ldo + n, v);
-                        if (want_mag) mag = fmaxf(fabsf(v.re.hi), fabsf(v.im.hi));
+                        store_fmt<OUT>(g.out, s_rowoff[ml] + n, v);
+                        mag = fmaxf(fabsf(v.re.hi), fabsf(v.im.hi));
                         if (g.colmax) {
                             const int f = s_field[ml];
                             if (f != cfield) {
@@ -502,21 +582,18 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
                             cmax = fmaxf(cmax, mag);
                         }
                     }
-                    if (g.rowmax) {
-                        float wm = mag;
-#pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
-                        if (lane == 0 && wm > 0.0f) atomicMax(&s_rowmax[ml], __float_as_uint(wm));
-                    }
+                    if (g.rowmax) s_mag[ml * T::PITCH + nl] = mag;
                 }
             }
             if (g.colmax && cfield >= 0 && cmax > 0.0f)
                 atomicMax(&g.colmax[z * g.colmax_z + cfield * g.colmax_field_stride + n], __float_as_uint(cmax));
         }
         ptx::named_barrier(1, EPI);
-        if (run && g.rowmax && et < 64) {
-            const int m = m_tile * 64 + et;
-            if (m < g.M && s_rowmax[et] != 0u) atomicMax(&g.rowmax[z * g.rowmax_z + m], s_rowmax[et]);
+        if (run && g.rowmax && et < 64 && et < g.M - m_tile * 64) {
+            float mx = 0.0f;
+            const int nmax = min(BN, g.N - n_tile * BN);
+            for (int c = 0; c < nmax; ++c) mx = fmaxf(mx, s_mag[et * T::PITCH + c]);
+            if (mx > 0.0f) atomicMax(&g.rowmax[z * g.rowmax_z + m_tile * 64 + et], __float_as_uint(mx));
         }
     }
     ptx::tc_fence_before();
@@ -853,18 +930,37 @@ TileChoice choose_tile(long long m_tiles, int N, int grid_z, int ktiles) {
     return c;
 }
 
-template <int BN> int launch_tile(const GemmArgs& g, dim3 grid, cudaStream_t st) {
+template <int BN, int OUT, int SRC> int launch_tile(const GemmArgs& g, dim3 grid, cudaStream_t st) {
     static bool configured[64];
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64 || !configured[dev]) {
-        HX_TRY(cuda_status(cudaFuncSetAttribute(split_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                Tile<BN>::SMEM_BYTES),
+        HX_TRY(cuda_status(cudaFuncSetAttribute(split_gemm_kernel<BN, OUT, SRC>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, Tile<BN>::SMEM_BYTES),
                            "cudaFuncSetAttribute(split_gemm_kernel)"));
         if (dev >= 0 && dev < 64) configured[dev] = true;
     }
-    split_gemm_kernel<BN><<<grid, NUM_THREADS, Tile<BN>::SMEM_BYTES, st>>>(g);
+    split_gemm_kernel<BN, OUT, SRC><<<grid, NUM_THREADS, Tile<BN>::SMEM_BYTES, st>>>(g);
     return launch_status("split_gemm_kernel");
+}
+
+template <int BN, int OUT> int launch_src(const GemmArgs& g, dim3 grid, int src, cudaStream_t st) {
+    switch (src) {
+        case FMT_NONE: return launch_tile<BN, OUT, FMT_NONE>(g, grid, st);
+        case FMT_C64: return launch_tile<BN, OUT, FMT_C64>(g, grid, st);
+        case FMT_C128: return launch_tile<BN, OUT, FMT_C128>(g, grid, st);
+        default:
+            set_error("internal: unsupported Babinet source format");
+            return HX_ERR_INVALID;
+    }
+}
+
+template <int BN> int launch_out(const GemmArgs& g, dim3 grid, int out, int src, cudaStream_t st) {
+    switch (out) {
+        case FMT_FF: return launch_src<BN, FMT_FF>(g, grid, src, st);
+        case FMT_C128: return launch_src<BN, FMT_C128>(g, grid, src, st);
+        default: return launch_src<BN, FMT_C64>(g, grid, src, st);
+    }
 }
 
 // partial / counters: workspace for a split-K choice (unused when c.ksplit == 1).
@@ -889,7 +985,9 @@ int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, const TileCho
     if (c.ksplit > 1)
         HX_TRY(cuda_status(cudaMemsetAsync(counters, 0, sizeof(unsigned int) * c.tiles, st), "memset counters"));
     dim3 grid((unsigned)(c.n_tiles * c.ksplit), (unsigned)m_tiles, grid_z);
-    return c.bn == 64 ? launch_tile<64>(g, grid, st) : launch_tile<128>(g, grid, st);
+    const int out = output_fmt(g.out);
+    const int src = g.epi == HX_EPI_BABINET ? input_fmt(g.src) : FMT_NONE;
+    return c.bn == 64 ? launch_out<64>(g, grid, out, src, st) : launch_out<128>(g, grid, out, src, st);
 }
 
 GemmArgs base_args(int* status) {
@@ -1200,10 +1298,12 @@ int split_lyot_execute(const SplitMftPlan* fpm, const SplitMftPlan* img, int bat
     // E_f = P(E) (1 - M), kept in float-float with its column maxima.
     HX_TRY(split_mft_run(fpm, HX_FORWARD, batch, fe, nullptr, ef, af_re, af_im, HX_EPI_MUL, one_minus_fpm, none,
                          nullptr, ef_colmax, inner, st));
-    // L = S (E - P^-1(E_f)), in float-float with its row maxima.
-    HX_TRY(split_mft_run(fpm, HX_BACKWARD, batch, ef, ef_colmax, lp, ab_re, ab_im, HX_EPI_BABINET, stop, fe,
-                         lp_rowmax, nullptr, inner, st));
-    if (lyot_out) {
+    // L = S (E - P^-1(E_f)): straight into the caller's Lyot-plane buffer when no image follows, else in
+    // float-float with its row maxima for the image transform.
+    const bool direct = lyot_out && !img;
+    HX_TRY(split_mft_run(fpm, HX_BACKWARD, batch, ef, ef_colmax, direct ? output_field(lyot_out, lyot_dtype) : lp,
+                         ab_re, ab_im, HX_EPI_BABINET, stop, fe, direct ? nullptr : lp_rowmax, nullptr, inner, st));
+    if (lyot_out && !direct) {
         const long long n = batch * pupil;
         field_copy_kernel<<<ceil_div(n, 512), 256, 0, st>>>(lp, output_field(lyot_out, lyot_dtype), n);
         HX_TRY(launch_status("field_copy_kernel"));

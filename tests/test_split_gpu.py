@@ -129,3 +129,23 @@ def test_split_tile_configurations(tile):
     errs = [float(x) for x in fields[:-1]]
     assert int(fields[-1]) == 0
     assert len(errs) == 6 and max(errs) < 2e-8, errs
+
+
+def test_split_complex128_wide_range():
+    """complex128 fields from 1e-20 to 1e20 (the float64 <-> float-float conversions), each against float64."""
+    rng = np.random.default_rng(5)
+    n_in, n_out = 96, 80
+    xg = (np.arange(n_in) - n_in / 2 + 0.5) / n_in
+    ug = (np.arange(n_out) - n_out / 2 + 0.5) * 0.41
+    gi = hg.CartesianGrid(hg.RegularCoords(1.0 / n_in, [n_in, n_in], [xg[0], xg[0]]))
+    go = hg.CartesianGrid(hg.RegularCoords(0.41, [n_out, n_out], [ug[0], ug[0]]))
+    split = hg.MatrixFourierTransform(gi, go, precision='split')
+    scales = np.array([1e-20, 3e-7, 1.0, 7e8, 1e20])
+    base = rng.standard_normal((len(scales), gi.size)) + 1j * rng.standard_normal((len(scales), gi.size))
+    e = base * scales[:, None]
+    out = split.forward(torch.from_numpy(e).cuda()).numpy()
+    assert out.dtype == np.complex128
+    for i in range(len(scales)):
+        ref = ofourier.mft_forward(e[i], xg, xg, ug, ug, gi.weights)
+        assert rel_err(out[i], ref) < 2e-8, (scales[i], rel_err(out[i], ref))
+    assert split._plan(torch.complex64).status() == 0
