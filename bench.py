@@ -41,7 +41,7 @@ def parse_args():
     p.add_argument('--steps', type=int, default=200)
     p.add_argument('--warmup', type=int, default=10)
     p.add_argument('--impl', choices=['ours', 'reference'], default='ours')
-    p.add_argument('--precision', choices=['fp32', 'split'], default='fp32')
+    p.add_argument('--precision', choices=['fp32', 'split'], default='split')
     p.add_argument('--pupil', type=int, default=2048)
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--cpu-seconds', type=float, default=10.0)
@@ -245,6 +245,9 @@ def run_ours(args, rank, world, dist):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    trace_kind = hg._lib.HX_TRACE_SPLIT_GEMM if args.precision == 'split' else hg._lib.HX_TRACE_SIMT_GEMM
+    hg._lib.trace_read(trace_kind, reset=True)
+    hg._lib.trace_enable(True)  # CUDA events around every GEMM launch, on the launching stream
     launches0 = hg.launch_count()
     wall0 = time.perf_counter()
     for i in range(args.steps):
@@ -255,6 +258,8 @@ def run_ours(args, rank, world, dist):
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     launches = hg.launch_count() - launches0
+    hg._lib.trace_enable(False)
+    k_launches, k_ms, k_cmacs = hg._lib.trace_read(trace_kind, reset=True)
     if dist:
         dist.barrier()
     clocks = sampler.stop()
@@ -270,7 +275,7 @@ def run_ours(args, rank, world, dist):
 
     # -- end to end through the public API with host buffers ------------------------------------------
     e_host = torch.from_numpy(w['E'].astype(np.complex64)).pin_memory()
-    img_host = torch.empty(focal.size, dtype=torch.complex64).pin_memory()
+    img_host = torch.empty(focal.size, dtype=img.dtype).pin_memory()  # complex128 for the split form
     e2e_steps = max(10, min(args.steps, 100))
     for _ in range(3):
         img_host.copy_(step(e_host.to(dev, non_blocking=True)), non_blocking=True)
@@ -302,10 +307,13 @@ def run_ours(args, rank, world, dist):
             peaks = json.load(f)
     except (OSError, ValueError):
         pass
-    achieved_tflops = flops / (ms_per_step * 1e-3) / 1e12
+    # achieved = algorithmic FLOP of the GEMM launches (8 per complex MAC, the reference's count) / their
+    # summed CUDA-event durations, recorded live in the timed region on the launching stream.
+    achieved_tflops = 8.0 * k_cmacs / (k_ms * 1e-3) / 1e12 if k_ms > 0 else 0.0
     if args.precision == 'split':
         peak = peaks.get('bf16_tflops', 1900.0)
-        bound, peak_note = 'tensor', 'bf16 dense, %s' % ('of measured' if 'bf16_tflops' in peaks else 'of fallback')
+        bound, peak_note = 'tensor', 'dense fp16/bf16 tensor rate, %s' % (
+            'of measured (burst)' if 'bf16_tflops' in peaks else 'of fallback')
     else:
         props = torch.cuda.get_device_properties(dev)
         max_mhz = (clocks or {}).get('sm_max_mhz') or peaks.get('sm_max_mhz', 2070.0)
@@ -336,7 +344,7 @@ def run_ours(args, rank, world, dist):
     line = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
-        'vs_baseline': None, 'dtype': 'fp32' if args.precision == 'fp32' else 'bf16-split/fp32-acc',
+        'vs_baseline': None, 'dtype': 'fp32' if args.precision == 'fp32' else 'fp16x3-split/fp32-acc',
         'data': 'synthetic (seeded Zernike 2-100 aberrations, 1 nm RMS)',
         'config': {'workload': 'lyot-coronagraph 2048^2 pupil -> 512^2 FPM grid -> 512^2 image (3 MFTs)',
                    'pupil': args.pupil, 'fpm_grid': int(fpm_grid.dims[0]), 'image': int(focal.dims[0]),
@@ -344,11 +352,14 @@ def run_ours(args, rank, world, dist):
                    'l2': 'flushed between steps (256 MiB write outside the per-step events)',
                    'parallelism': 'replicas' if world > 1 else 'single-gpu'},
         'roofline': {'bound': bound, 'achieved': achieved_tflops, 'peak': peak, 'unit': 'TFLOP/s',
-                     'frac': achieved_tflops / peak, 'traffic': traffic, 'kernel': 'cgemm_nn_simt<float>'
-                     if args.precision == 'fp32' else 'split tcgen05 GEMM',
-                     'algorithmic': '%d complex MACs x 8 FLOP per propagation' % cmacs, 'peak_note': peak_note},
+                     'frac': achieved_tflops / peak, 'traffic': traffic,
+                     'kernel': 'cgemm_nn_simt<float>' if args.precision == 'fp32' else 'split_gemm_kernel (tcgen05)',
+                     'launches_per_step': k_launches / args.steps, 'ms_per_launch': k_ms / max(k_launches, 1),
+                     'kernel_share_of_step': k_ms / total_ms if total_ms > 0 else None,
+                     'algorithmic': '%d complex MACs x 8 FLOP per propagation' % cmacs, 'peak_note': peak_note,
+                     'tensor_flop_per_algorithmic_flop': 8 if args.precision == 'split' else None},
         'e2e': {'value': e2e_value, 'unit': UNIT, 'h2d_bytes_per_step': int(e_host.numel() * 8),
-                'd2h_bytes_per_step': int(img_host.numel() * 8)},
+                'd2h_bytes_per_step': int(img_host.numel() * img_host.element_size())},
         'gpu_launches': int(gpu_launches),
         'clocks': clocks,
         'accuracy': {'ni_err_max': ni_max, 'ni_err_mean': ni_mean, 'dark_hole_mean_ni': ni_level,

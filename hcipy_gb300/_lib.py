@@ -30,6 +30,9 @@ HX_PREC_SPLIT = 1
 HX_EPI_NONE = 0
 HX_EPI_MUL = 1
 HX_EPI_BABINET = 2
+HX_TRACE_SPLIT_GEMM = 0
+HX_TRACE_SIMT_GEMM = 1
+HX_TRACE_FFT = 2
 
 c_int = ctypes.c_int
 c_double = ctypes.c_double
@@ -43,6 +46,8 @@ SIGNATURES = {
     'hx_last_error': (ctypes.c_char_p, []),
     'hx_version': (c_int, []),
     'hx_launch_count': (c_ll, []),
+    'hx_trace_enable': (c_int, [c_int]),
+    'hx_trace_read': (c_int, [c_int, P(c_ll), P(c_double), P(c_double), c_int]),
     'hx_mft_plan_create': (c_int, [c_int, c_int, c_int, c_int, P(c_double), P(c_double), P(c_double), P(c_double),
                                    P(c_double), P(c_double), P(c_double), P(c_double), c_int, c_int, c_void_p,
                                    P(c_void_p)]),
@@ -179,3 +184,18 @@ def dtype_code(dt):
 
 def launch_count():
     return int(load().hx_launch_count())
+
+
+def trace_enable(on=True):
+    """Bracket every GEMM and FFT pass the library launches with CUDA events on its stream."""
+    check(lib().hx_trace_enable(1 if on else 0), 'hx_trace_enable')
+
+
+def trace_read(kind, reset=True):
+    """(launches, device milliseconds, algorithmic work) of one kernel family since the last reset."""
+    n = ctypes.c_longlong()
+    ms = ctypes.c_double()
+    work = ctypes.c_double()
+    check(lib().hx_trace_read(kind, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(work), 1 if reset else 0),
+          'hx_trace_read')
+    return int(n.value), float(ms.value), float(work.value)

@@ -111,6 +111,8 @@ int launch_line(const LineArgs<T>& a, int threads, size_t smem, int batch, cudaS
         set_error("FFT batch too large (%d)", batch);
         return HX_ERR_UNSUPPORTED;
     }
+    TraceScope trace(HX_TRACE_FFT,
+                     (double)a.nlines * (a.in_count + a.out_count) * batch * sizeof(typename cplx<T>::type), stream);
     fft_line_kernel<T, SIGN, CONV, MIXED><<<grid, threads, smem, stream>>>(a);
     return launch_status("fft_line_kernel");
 }

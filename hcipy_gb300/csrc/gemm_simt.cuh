@@ -186,6 +186,7 @@ inline int cgemm_nn<float>(int M, int N, int K, float2 alpha, const float2* A, l
         set_error("cgemm: problem too large for one launch (M=%d, batch=%d)", M, batch);
         return HX_ERR_UNSUPPORTED;
     }
+    TraceScope trace(HX_TRACE_SIMT_GEMM, (double)M * N * K * batch, stream);
     cgemm_nn_simt<float, BM, BN, BK, TM, TN><<<grid, 256, 0, stream>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, epi);
     return launch_status("cgemm_nn_simt<float>");
 }
@@ -200,6 +201,7 @@ inline int cgemm_nn<double>(int M, int N, int K, double2 alpha, const double2* A
         set_error("zgemm: problem too large for one launch (M=%d, batch=%d)", M, batch);
         return HX_ERR_UNSUPPORTED;
     }
+    TraceScope trace(HX_TRACE_SIMT_GEMM, (double)M * N * K * batch, stream);
     cgemm_nn_simt<double, BM, BN, BK, TM, TN><<<grid, 256, 0, stream>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, epi);
     return launch_status("cgemm_nn_simt<double>");
 }

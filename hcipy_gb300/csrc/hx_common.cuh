@@ -22,6 +22,22 @@ void count_launch(int n = 1);
 // "launch"), the entry point returns HX_ERR_INJECTED before touching the GPU.
 bool fault_injected(const char* site);
 
+// Kernel timing (hx_trace_enable): a scope records a CUDA event on `stream` when it opens and another when it
+// closes, so a launch issued inside the scope is timed on its own stream.  Free when tracing is off.
+bool trace_on();
+int trace_begin(int kind, double work, cudaStream_t stream);
+void trace_end(int record, cudaStream_t stream);
+struct TraceScope {
+    int record = -1;
+    cudaStream_t stream;
+    TraceScope(int kind, double work, cudaStream_t st) : stream(st) {
+        if (trace_on()) record = trace_begin(kind, work, st);
+    }
+    ~TraceScope() {
+        if (record >= 0) trace_end(record, stream);
+    }
+};
+
 inline int cuda_status(cudaError_t e, const char* what) {
     if (e == cudaSuccess) return HX_OK;
     set_error("%s: %s", what, cudaGetErrorString(e));

@@ -160,6 +160,12 @@ int hx_mft_plan_create(int nx, int ny, int nu, int nv, const double* x, const do
         if ((rc = upload(w_in_y, ny, &dwy, stream))) break;
         if ((rc = upload(w_out_u, nu, &dwu, stream))) break;
         if ((rc = upload(w_out_v, nv, &dwv, stream))) break;
+        if (precision == HX_PREC_SPLIT) {
+            // The split form keeps only its sliced operands.
+            if ((rc = hx::split_mft_create(nx, ny, nu, nv, dx, dy, du, dv, dwx, dwy, dwu, dwv, stream, &p->split)))
+                break;
+            break;
+        }
         if ((rc = gen_matrix(dtype, nv, ny, dv, dy, -1.0, nullptr, dwy, &p->m1f, stream))) break;
         if ((rc = gen_matrix(dtype, nx, nu, dx, du, -1.0, dwx, nullptr, &p->m2f, stream))) break;
         if ((rc = gen_matrix(dtype, ny, nv, dy, dv, +1.0, nullptr, dwv, &p->m1b, stream))) break;
@@ -173,10 +179,6 @@ int hx_mft_plan_create(int nx, int ny, int nu, int nv, const double* x, const do
             p->own_adjoint = true;
             if ((rc = gen_matrix(dtype, ny, nv, dy, dv, +1.0, dwy, nullptr, &p->m1a, stream))) break;
             if ((rc = gen_matrix(dtype, nu, nx, du, dx, +1.0, nullptr, dwx, &p->m2a, stream))) break;
-        }
-        if (precision == HX_PREC_SPLIT) {
-            if ((rc = hx::split_mft_create(nx, ny, nu, nv, dx, dy, du, dv, dwx, dwy, dwu, dwv, stream, &p->split)))
-                break;
         }
     } while (false);
     cleanup();

@@ -180,30 +180,11 @@ __device__ __forceinline__ unsigned long long float_bits_to_double_bits(unsigned
     return sign | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)m << 29);
 }
 
-// hi + lo as float64 with integer operations only: lo's significand is added in units of hi's float64 ulp
-// (its bits below that unit are dropped, an error under two ulps of the result).  Needs |lo| < 2^6 ulp_64(hi),
-// which holds for every float-float this library produces (|lo| <= ulp_32(hi)).
+// hi + lo as float64: each float is placed exactly into float64 bits (integer operations), then one float64
+// addition rounds the sum.
 __device__ __forceinline__ double ff_to_double(ff v) {
-    const unsigned int hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
-    const int he = (int)((hb >> 23) & 0xff), le = (int)((lb >> 23) & 0xff);
-    if (he == 0 || he == 0xff || le == 0)
-        return __longlong_as_double(
-            (long long)float_bits_to_double_bits((he == 0 && (hb & 0x7fffffffu) == 0u) ? lb : hb));
-    unsigned long long s = (1ull << 52) | ((unsigned long long)(hb & 0x7fffffu) << 29);
-    const unsigned long long lsig = (1ull << 23) | (lb & 0x7fffffu);
-    const int shift = le - he + 29;
-    const unsigned long long l = shift >= 0 ? lsig << shift : (shift > -40 ? lsig >> -shift : 0ull);
-    s = ((hb ^ lb) >> 31) ? s - l : s + l;
-    int e = he + 896;
-    if (s >= (1ull << 53)) {
-        s >>= 1;
-        ++e;
-    } else if (s < (1ull << 52)) {
-        s <<= 1;
-        --e;
-    }
-    return __longlong_as_double(
-        (long long)(((unsigned long long)(hb & 0x80000000u) << 32) | ((unsigned long long)e << 52) | (s & 0xFFFFFFFFFFFFFull)));
+    return __dadd_rn(__longlong_as_double((long long)float_bits_to_double_bits(__float_as_uint(v.hi))),
+                     __longlong_as_double((long long)float_bits_to_double_bits(__float_as_uint(v.lo))));
 }
 
 template <int FMT> __device__ __forceinline__ cff load_fmt(const FieldIO& f, long long i) {
@@ -526,6 +507,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
         if (run) {
             const cff alpha = {{g.alpha[0], g.alpha[1]}, {g.alpha[2], g.alpha[3]}};
             const bool real_alpha = g.alpha[2] == 0.0f && g.alpha[3] == 0.0f;
+            const bool imag_alpha = g.alpha[0] == 0.0f && g.alpha[1] == 0.0f;  // e.g. Fraunhofer's 1/(i f lambda)
             const bool unit_alpha = real_alpha && g.alpha[0] == 1.0f && g.alpha[1] == 0.0f;
             const float2* mask = (g.epi == HX_EPI_MUL || g.epi == HX_EPI_BABINET) ? g.mask : nullptr;
             // Each thread keeps one column; a warp covers 32 consecutive columns of one row.
@@ -563,8 +545,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
                         const float sc = s_rscale[ml] * csc;  // product of powers of two: exact
                         cff v = {ff{st_hi[ml * T::PITCH + nl] * sc, st_lo[ml * T::PITCH + nl] * sc},
                                  ff{st_hi[(64 + ml) * T::PITCH + nl] * sc, st_lo[(64 + ml) * T::PITCH + nl] * sc}};
-                        if (!unit_alpha) v = real_alpha ? cff{ff_mul(v.re, alpha.re), ff_mul(v.im, alpha.re)}
-                                                        : cff_mul(v, alpha);
+                        if (!unit_alpha)
+                            v = real_alpha   ? cff{ff_mul(v.re, alpha.re), ff_mul(v.im, alpha.re)}
+                                : imag_alpha ? cff{ff_neg(ff_mul(v.im, alpha.im)), ff_mul(v.re, alpha.im)}
+                                             : cff_mul(v, alpha);
                         if constexpr (SRC != FMT_NONE) v = {ff_add(e[u].re, ff_neg(v.re)), ff_add(e[u].im, ff_neg(v.im))};
                         if (mask) v = mk[u].y == 0.0f ? cff{ff_mulf(v.re, mk[u].x), ff_mulf(v.im, mk[u].x)}
                                                       : cff_mul_c64(v, mk[u]);
@@ -906,9 +890,10 @@ struct TileChoice {
     size_t partial_floats() const { return ksplit > 1 ? (size_t)tiles * ksplit * 2 * bn * BM : 0; }
 };
 
-// BN = 128 halves the A traffic per product against BN = 64; a GEMM with fewer output tiles than SMs splits
-// K so that the grid fills the GPU, keeping at least four K-steps per CTA.  HX_SPLIT_TILE="bn[,ksplit]"
-// overrides the choice (tuning).
+// BN = 128 halves the A traffic per product against BN = 64 and is taken when its tiles fill at least 3/4 of
+// the SMs.  Smaller GEMMs take BN = 64 and split K so that the grid fills the GPU (at least four K-steps per
+// CTA): more CTAs share the epilogue and the last CTA of a tile reads fewer partial bytes.
+// HX_SPLIT_TILE="bn[,ksplit]" overrides the choice (tuning).
 TileChoice choose_tile(long long m_tiles, int N, int grid_z, int ktiles) {
     static int forced_bn = 0, forced_split = 0;
     static std::once_flag once;
@@ -920,10 +905,11 @@ TileChoice choose_tile(long long m_tiles, int N, int grid_z, int ktiles) {
         if (n == 2 && ks >= 1) forced_split = ks;
     });
     TileChoice c;
-    c.bn = forced_bn ? forced_bn : (N <= 64 ? 64 : 128);
+    const int sms = sm_count();
+    const long long tiles128 = m_tiles * (long long)ceil_div(N, 128) * grid_z;
+    c.bn = forced_bn ? forced_bn : (N > 64 && 4 * tiles128 >= 3LL * sms ? 128 : 64);
     c.n_tiles = (int)ceil_div(N, c.bn);
     c.tiles = m_tiles * c.n_tiles * grid_z;
-    const int sms = sm_count();
     if (forced_split) c.ksplit = forced_split;
     else if (c.tiles < sms) c.ksplit = (int)(sms / c.tiles);
     c.ksplit = std::max(1, std::min(c.ksplit, std::max(1, ktiles / 4)));
@@ -965,7 +951,7 @@ template <int BN> int launch_out(const GemmArgs& g, dim3 grid, int out, int src,
 
 // partial / counters: workspace for a split-K choice (unused when c.ksplit == 1).
 int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, const TileChoice& c, int grid_z,
-                float* partial, unsigned int* counters, cudaStream_t st) {
+                float* partial, unsigned int* counters, double cmacs, cudaStream_t st) {
     if (A.kpitch != B.kpitch) {
         set_error("internal: split GEMM K mismatch (%d vs %d)", A.kpitch, B.kpitch);
         return HX_ERR_INVALID;
@@ -987,6 +973,7 @@ int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, const TileCho
     dim3 grid((unsigned)(c.n_tiles * c.ksplit), (unsigned)m_tiles, grid_z);
     const int out = output_fmt(g.out);
     const int src = g.epi == HX_EPI_BABINET ? input_fmt(g.src) : FMT_NONE;
+    TraceScope trace(HX_TRACE_SPLIT_GEMM, cmacs, st);
     return c.bn == 64 ? launch_out<64>(g, grid, out, src, st) : launch_out<128>(g, grid, out, src, st);
 }
 
@@ -1108,7 +1095,7 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
         g1.colmax = w.t_max;
         g1.colmax_rows_per_field = ny;
         g1.colmax_field_stride = nu64;
-        HX_TRY(launch_gemm(g1, w.s1, p->m2f, w.c1, 1, w.partial, w.counters, st));
+        HX_TRY(launch_gemm(g1, w.s1, p->m2f, w.c1, 1, w.partial, w.counters, (double)rows * nu * nx, st));
         // G2: out[b] = alpha M1f . T[b] with the fused epilogue.
         HX_TRY(launch_slice_cols(w.t, ny, nu, batch, (long long)ny * nu, w.t_max, nu64, w.s2, (int)nu64, st));
         GemmArgs g2 = base_args(p->status);
@@ -1130,7 +1117,7 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
         g2.rowmax_z = nv;
         g2.colmax = out_colmax;
         g2.colmax_z = nu64;
-        return launch_gemm(g2, p->m1f, w.s2, w.c2, batch, w.partial, w.counters, st);
+        return launch_gemm(g2, p->m1f, w.s2, w.c2, batch, w.partial, w.counters, (double)nv * nu * ny * batch, st);
     }
     const SliceMat& m1 = direction == HX_BACKWARD ? p->m1b : p->m1a;
     const SliceMat& m2 = direction == HX_BACKWARD ? p->m2b : p->m2a;
@@ -1155,7 +1142,7 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
     g1.out_z = (long long)ny * nu;
     g1.rowmax = w.t_max;
     g1.rowmax_z = ny;
-    HX_TRY(launch_gemm(g1, m1, w.s1, w.c1, batch, w.partial, w.counters, st));
+    HX_TRY(launch_gemm(g1, m1, w.s1, w.c1, batch, w.partial, w.counters, (double)ny * nu * nv * batch, st));
     // G2: out = alpha T . M2, stacked over the batch, with the fused epilogue.
     HX_TRY(launch_slice_rows(w.t, nu, rows, nu, w.t_max, w.s2, st));
     GemmArgs g2 = base_args(p->status);
@@ -1174,7 +1161,7 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
     g2.colmax = out_colmax;
     g2.colmax_rows_per_field = ny;
     g2.colmax_field_stride = round_up(nx, 64);
-    return launch_gemm(g2, w.s2, m2, w.c2, 1, w.partial, w.counters, st);
+    return launch_gemm(g2, w.s2, m2, w.c2, 1, w.partial, w.counters, (double)rows * nx * nu, st);
 }
 
 }  // namespace

@@ -63,6 +63,17 @@ HX_API int hx_version(void);
 /* Number of kernels this library has launched in this process. */
 HX_API long long hx_launch_count(void);
 
+/* Kernel timing (no counterpart in the reference, which has no device kernels).  While enabled, every GEMM
+ * and FFT pass the library launches is bracketed by a CUDA event pair recorded on the launching stream and
+ * tagged with its algorithmic work (complex multiply-adds for a GEMM, bytes moved for an FFT pass).
+ * hx_trace_read waits for the recorded events of one kernel family and returns launches, summed device time
+ * and summed work since the last reset. */
+#define HX_TRACE_SPLIT_GEMM 0 /* split-operand tcgen05 GEMM of the MFT */
+#define HX_TRACE_SIMT_GEMM 1  /* CUDA-core complex GEMM of the MFT (FP32 or FP64) */
+#define HX_TRACE_FFT 2        /* line-FFT passes (FFT, filter, chirp-Z) */
+HX_API int hx_trace_enable(int on);
+HX_API int hx_trace_read(int kind, long long* launches, double* total_ms, double* total_work, int reset);
+
 /* ------------------------------------------------------------------------
  * Matrix Fourier transform.
  * Replaces MatrixFourierTransform (hcipy/fourier/matrix_fourier_transform.py:42-224):
