@@ -13,6 +13,10 @@ from .optics import (Wavefront, OpticalElement, AgnosticOpticalElement, Apodizer
 from .propagation import FraunhoferPropagator, AngularSpectrumPropagator
 from .fft import FastFourierTransform, ChirpZTransform, ZoomFastFourierTransform, FourierFilter
 from .coronagraphy import LyotCoronagraph
+from .deformable_mirror import (ModeBasis, DeformableMirror, make_actuator_positions,
+                                make_gaussian_influence_functions, find_illuminated_actuators)
+from .atmosphere import (AtmosphericLayer, InfiniteAtmosphericLayer, MultiLayerAtmosphere,
+                         Cn_squared_from_fried_parameter, fried_parameter_from_Cn_squared, subpixel_shift)
 from ._lib import HXError, launch_count
 
 __all__ = [
@@ -24,4 +28,7 @@ __all__ = [
     'make_agnostic_forward', 'make_agnostic_backward',
     'FraunhoferPropagator', 'AngularSpectrumPropagator', 'LyotCoronagraph', 'HXError', 'launch_count',
     'FastFourierTransform', 'ChirpZTransform', 'ZoomFastFourierTransform', 'FourierFilter',
+    'ModeBasis', 'DeformableMirror', 'make_actuator_positions', 'make_gaussian_influence_functions',
+    'find_illuminated_actuators', 'AtmosphericLayer', 'InfiniteAtmosphericLayer', 'MultiLayerAtmosphere',
+    'Cn_squared_from_fried_parameter', 'fried_parameter_from_Cn_squared', 'subpixel_shift',
 ]

@@ -22,6 +22,8 @@ HX_ERR_INJECTED = -6
 
 HX_C64 = 0
 HX_C128 = 1
+HX_F32 = 2
+HX_F64 = 3
 HX_FORWARD = 0
 HX_BACKWARD = 1
 HX_ADJOINT = 2
@@ -47,6 +49,17 @@ SIGNATURES = {
     'hx_version': (c_int, []),
     'hx_launch_count': (c_ll, []),
     'hx_trace_enable': (c_int, [c_int]),
+    'hx_influence_apply': (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p,
+                                   c_void_p]),
+    'hx_influence_apply_transpose': (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p,
+                                             c_void_p, c_void_p]),
+    'hx_phase_apply': (c_int, [c_ll, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_double, c_void_p, c_void_p]),
+    'hx_phase_apply_grad': (c_int, [c_ll, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_double, c_void_p,
+                                    c_void_p, c_void_p, c_void_p]),
+    'hx_atmosphere_extrude': (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p,
+                                      c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
+    'hx_atmosphere_shift': (c_int, [c_void_p, c_int, c_int, c_int, c_int, P(c_double), P(c_double), c_void_p, c_int,
+                                    c_void_p]),
     'hx_trace_read': (c_int, [c_int, P(c_ll), P(c_double), P(c_double), c_int]),
     'hx_mft_plan_create': (c_int, [c_int, c_int, c_int, c_int, P(c_double), P(c_double), P(c_double), P(c_double),
                                    P(c_double), P(c_double), P(c_double), P(c_double), c_int, c_int, c_void_p,
@@ -179,6 +192,10 @@ def dtype_code(dt):
         return HX_C64
     if dt == torch.complex128:
         return HX_C128
+    if dt == torch.float32:
+        return HX_F32
+    if dt == torch.float64:
+        return HX_F64
     raise ValueError('unsupported dtype %s' % dt)
 
 

@@ -1,0 +1,442 @@
+"""Atmospheric layers (hcipy/atmosphere) with the per-frame work on the device.
+
+``InfiniteAtmosphericLayer`` follows hcipy/atmosphere/infinite_atmospheric_layer.py: the same stencils
+(including the random far pixel of each column, drawn from the layer's generator first, :111-140), the same
+von Karman covariances and autoregressive matrices A = C_xz C_zz^-1 and B from the SVD of C_xx - A C_zx
+(:142-202), and the same extrusion and time stepping (:216-364).  Plan-time work (covariances, Cholesky,
+SVD) runs on the host in float64 as in the reference; every frame runs on the GPU:
+
+* the screen is a ring buffer, so an extrusion moves an offset and writes one row or column
+  (``hx_atmosphere_extrude``: A . stencil + B . noise) instead of copying the screen;
+* the extrusion noise is drawn on the host from the layer's numpy Generator with the reference's call,
+  ``rng.normal(0, sqrt(Cn^2), size=B.shape[1])``, one draw per step in the reference's order, so a layer seeded
+  like the reference's extrudes the same rows;
+* the quintic sub-pixel shift (hcipy/_math/subpixel_shift.py) reads the ring and writes the shifted screen
+  (``hx_atmosphere_shift``);
+* ``forward``/``backward`` multiply by exp(+-i screen / lambda) in one kernel (``hx_phase_apply``).
+
+The initial screen is this package's own: a von Karman FFT screen of twice the extent, cropped (the reference
+draws it with its multi-scale spectral-noise generator, hcipy/util/spectral_noise.py:203-320, so a seeded layer
+here starts from a different but statistically equivalent screen).  ``initial_screen`` sets it explicitly.
+"""
+import copy
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from .field import Field, as_tensor
+from .kernels import apply_phase
+from .optics import OpticalElement, Wavefront
+
+
+# ---- turbulence statistics (hcipy/atmosphere/atmospheric_model.py:321-420) -------------------------------
+
+def Cn_squared_from_fried_parameter(r0, wavelength=500e-9):  # noqa: N802
+    k = 2 * np.pi / wavelength
+    return r0**(-5. / 3) / (0.423 * k**2)
+
+
+def fried_parameter_from_Cn_squared(Cn_squared, wavelength=500e-9):  # noqa: N802
+    k = 2 * np.pi / wavelength
+    return (0.423 * Cn_squared * k**2)**(-3. / 5)
+
+
+def von_karman_covariance(r, r0, L0):  # noqa: N803
+    """Phase covariance of von Karman turbulence at separations r (atmospheric_model.py:321-346)."""
+    from scipy.special import gamma, kv
+    r = np.asarray(r, np.float64) + 1e-10
+    a = (L0 / r0)**(5 / 3)
+    b = gamma(11 / 6) / (2**(5 / 6) * np.pi**(8 / 3))
+    c = (24 / 5 * gamma(6 / 5))**(5 / 6)
+    d = (2 * np.pi * r / L0)**(5 / 6)
+    e = kv(5 / 6, 2 * np.pi * r / L0)
+    return a * b * c * d * e
+
+
+def quintic_weights(shift):
+    """7-tap quintic B-spline weights of a shift in [-0.5, 0.5] pixels (subpixel_shift.py:7-35)."""
+    f = abs(shift)
+    b = np.empty(6)
+    for i, offset in enumerate((2.0 + f, 1.0 + f, f, 1.0 - f, 2.0 - f, 3.0 - f)):
+        acc, x = 0.0, offset + 3.0
+        for c in (1.0, -6.0, 15.0, -20.0, 15.0, -6.0, 1.0):
+            if x > 0.0:
+                acc += c * x**5
+            x -= 1.0
+        b[i] = acc / 120.0
+    if shift >= 0:
+        return np.array([0.0, b[0], b[1], b[2], b[3], b[4], b[5]])
+    return np.array([b[5], b[4], b[3], b[2], b[1], b[0], 0.0])
+
+
+def von_karman_screen(nx, ny, delta, Cn_squared, L0, rng, pad=2):  # noqa: N803
+    """An FFT phase screen (radians at wavelength 1 m) of pad times the extent, cropped to ny x nx."""
+    n = pad * max(nx, ny)
+    d = float(np.max(delta))
+    k = 2 * np.pi * np.fft.fftfreq(n, d)
+    kx, ky = np.meshgrid(k, k)
+    k0 = 2 * np.pi / L0 if np.isfinite(L0) else 0.0
+    r0 = fried_parameter_from_Cn_squared(Cn_squared, 1.0)
+    # 0.023 r0^-5/3 f^-11/3 per (cycle/m)^2, written for angular frequency k = 2 pi f
+    psd = 0.023 * (2 * np.pi)**(5 / 3) * r0**(-5 / 3) * (kx**2 + ky**2 + k0**2)**(-11 / 6)
+    psd[0, 0] = 0.0
+    dk = 2 * np.pi / (n * d)
+    c = np.sqrt(psd) * dk * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    screen = np.real(np.fft.ifft2(c)) * n * n
+    return screen[:ny, :nx].copy()
+
+
+def make_stencils(nx, ny, stencil_length, rng):
+    """Flat indices of the bottom and left stencils: the first ``stencil_length`` rows (columns) plus one pixel
+    per column (row) at a geometric distance, drawn from ``rng`` in the reference's order
+    (infinite_atmospheric_layer.py:111-140)."""
+    st = np.zeros((ny, nx), bool)
+    st[:stencil_length, :] = True
+    for i, n in enumerate(rng.geometric(0.5, nx)):
+        st[(n + stencil_length - 1) % ny, i] = True
+    bottom = np.where(st.ravel())[0]
+    st = np.zeros((ny, nx), bool)
+    st[:, :stencil_length] = True
+    for i, n in enumerate(rng.geometric(0.5, ny)):
+        st[i, (n + stencil_length - 1) % nx] = True
+    left = np.where(st.ravel())[0]
+    return bottom, left
+
+
+def ar_matrices(grid, stencil_idx, where, L0):  # noqa: N803
+    """Autoregressive matrices of one extrusion direction for unit Cn^2 (infinite_atmospheric_layer.py:142-202):
+    the von Karman covariance of stencil and new slice, A = C_xz C_zz^-1 (Cholesky), B = U sqrt(S) from the SVD
+    of C_xx - A C_zx."""
+    from scipy import linalg
+    xs, ys = (np.asarray(c, np.float64) for c in grid.separated_coords)
+    d = np.asarray(grid.delta, np.float64)
+    xx, yy = np.meshgrid(xs, ys)
+    px, py = xx.ravel(), yy.ravel()
+    if where == 'bottom':
+        new_x, new_y = xs, np.full(xs.size, ys[0] - d[1])
+    else:
+        new_x, new_y = np.full(ys.size, xs[0] - d[0]), ys
+    x = np.concatenate((px[stencil_idx], new_x))
+    y = np.concatenate((py[stencil_idx], new_y))
+    sep = np.hypot(x[None, :] - x[:, None], y[None, :] - y[:, None])
+    cov = von_karman_covariance(sep, fried_parameter_from_Cn_squared(1, 1), L0)
+    n = stencil_idx.size
+    cov_zz, cov_xz, cov_zx, cov_xx = cov[:n, :n], cov[n:, :n], cov[:n, n:], cov[n:, n:]
+    cf = linalg.cho_factor(cov_zz)
+    a = cov_xz.dot(linalg.cho_solve(cf, np.eye(n)))
+    u, sv, _ = np.linalg.svd(cov_xx - a.dot(cov_zx))
+    b = u * np.sqrt(sv[:new_x.size])
+    return a, b
+
+
+def subpixel_shift(img, row_shift, col_shift):
+    """Shift an image (ny, nx) by fractions of a pixel with the quintic B-spline (subpixel_shift.py:306-343)."""
+    if not (-0.5 <= row_shift <= 0.5) or not (-0.5 <= col_shift <= 0.5):
+        raise ValueError('row_shift and col_shift must be in [-0.5, 0.5]')
+    t = as_tensor(img).contiguous()
+    if t.dtype not in (torch.float32, torch.float64):
+        t = t.to(torch.float64)
+    ny, nx = t.shape[-2:]
+    out = torch.empty_like(t)
+    tr = np.ascontiguousarray(quintic_weights(col_shift))
+    tc = np.ascontiguousarray(quintic_weights(row_shift))
+    P = _lib.ctypes.POINTER(_lib.ctypes.c_double)
+    rc = _lib.lib().hx_atmosphere_shift(_lib.dptr(t), int(ny), int(nx), 0, 0, tr.ctypes.data_as(P),
+                                        tc.ctypes.data_as(P), _lib.dptr(out), _lib.dtype_code(t.dtype),
+                                        _lib.stream_handle())
+    _lib.check(rc, 'hx_atmosphere_shift')
+    return out
+
+
+# ---- layers ---------------------------------------------------------------------------------------------
+
+class AtmosphericLayer(OpticalElement):
+    """Base of the atmospheric layers (atmospheric_model.py:10-151): E exp(+-i phase_for(lambda))."""
+
+    def __init__(self, input_grid, Cn_squared, L0=np.inf, velocity=0, height=0):  # noqa: N803
+        self.input_grid = input_grid
+        self._Cn_squared = Cn_squared
+        self._L0 = L0
+        self.velocity = velocity
+        self.height = height
+        self._t = 0
+
+    @property
+    def t(self):
+        return self._t
+
+    @t.setter
+    def t(self, t):
+        self.evolve_until(t)
+
+    @property
+    def velocity(self):
+        return self._velocity
+
+    @velocity.setter
+    def velocity(self, velocity):
+        self._velocity = np.array([velocity, 0.0]) if np.isscalar(velocity) else np.array(velocity, np.float64)
+
+    @property
+    def outer_scale(self):
+        return self._L0
+
+    @outer_scale.setter
+    def outer_scale(self, L0):  # noqa: N803
+        self._L0 = L0
+
+    @property
+    def L0(self):  # noqa: N802
+        return self.outer_scale
+
+    @L0.setter
+    def L0(self, L0):  # noqa: N802, N803
+        self.outer_scale = L0
+
+    @property
+    def output_grid(self):
+        return self.input_grid
+
+    def _screen_tensor(self):
+        raise NotImplementedError()
+
+    def phase_for(self, wavelength):
+        return Field(self._screen_tensor() / wavelength, self.input_grid)
+
+    def _apply(self, wf, sign):
+        e = as_tensor(wf.electric_field)
+        s = self._screen_tensor()
+        if torch.is_grad_enabled() and e.requires_grad:
+            from .autograd import phase_apply
+            out = phase_apply(e, s, sign / wf.wavelength)
+        else:
+            out = apply_phase(e, s, sign / wf.wavelength)
+        return Wavefront(Field(out, wf.electric_field.grid), wf.wavelength)
+
+    def forward(self, wf):
+        return self._apply(wf, 1.0)
+
+    def backward(self, wf):
+        return self._apply(wf, -1.0)
+
+
+_WHERE = {'bottom': 0, 'top': 1, 'left': 2, 'right': 3}
+
+
+class InfiniteAtmosphericLayer(AtmosphericLayer):
+    """An infinitely extendable layer (Assemat et al. 2006), infinite_atmospheric_layer.py:14-390.
+
+    Extra arguments: ``dtype`` of the device screen and AR matrices (float64 as the reference, or float32 to
+    halve the bytes of every extrusion), ``initial_screen`` (ny x nx, radians at 1 m) instead of the generated
+    one.
+    """
+
+    def __init__(self, input_grid, Cn_squared, L0=np.inf, velocity=0, height=0, stencil_length=2,  # noqa: N803
+                 use_interpolation=True, seed=None, dtype=torch.float64, initial_screen=None):
+        self._initialized = False
+        AtmosphericLayer.__init__(self, input_grid, Cn_squared, L0, velocity, height)
+        if not getattr(input_grid, 'is_regular', False):
+            raise ValueError('Input grid must be regularly spaced')
+        if input_grid.ndim != 2:
+            raise ValueError('Input grid must be two-dimensional.')
+        self.stencil_length = stencil_length
+        self.use_interpolation = use_interpolation
+        self.dtype = dtype
+        self.rng = np.random.default_rng(seed)
+        self._initial_screen = None if initial_screen is None else np.asarray(initial_screen, np.float64)
+        self.nx, self.ny = (int(d) for d in input_grid.dims)
+        self._delta = np.asarray(input_grid.delta, np.float64)
+        self._make_stencils()
+        self._make_ab_matrices()
+        self._original_rng = self.rng
+        self.reset()
+        self._initialized = True
+
+    # -- plan-time matrices (host, float64) --------------------------------------------------------------
+    def _make_stencils(self):
+        self.stencil_bottom_idx, self.stencil_left_idx = make_stencils(self.nx, self.ny, self.stencil_length, self.rng)
+        self.stencil_bottom = np.zeros(self.nx * self.ny, bool)
+        self.stencil_bottom[self.stencil_bottom_idx] = True
+        self.stencil_left = np.zeros(self.nx * self.ny, bool)
+        self.stencil_left[self.stencil_left_idx] = True
+
+    def _make_ab_matrices(self):
+        g = self.input_grid
+        self.A_vertical, self.B_vertical = ar_matrices(g, self.stencil_bottom_idx, 'bottom', self._L0)
+        self.A_horizontal, self.B_horizontal = ar_matrices(g, self.stencil_left_idx, 'left', self._L0)
+        self._upload_matrices()
+
+    def _upload_matrices(self):
+        dev, dt = torch.device('cuda'), self.dtype
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device=dev, dtype=dt)  # noqa: E731
+        self._dev = {
+            'A_v': t(self.A_vertical), 'B_v': t(self.B_vertical),
+            'A_h': t(self.A_horizontal), 'B_h': t(self.B_horizontal),
+            'idx_v': torch.from_numpy(self.stencil_bottom_idx.astype(np.int64)).to(dev),
+            'idx_h': torch.from_numpy(self.stencil_left_idx.astype(np.int64)).to(dev),
+        }
+        self._work = torch.empty(max(self.stencil_bottom_idx.size, self.stencil_left_idx.size), dtype=dt, device=dev)
+
+    # -- state ---------------------------------------------------------------------------------------------
+    def reset(self, make_independent_realization=False):
+        """infinite_atmospheric_layer.py:276-303."""
+        if make_independent_realization:
+            self._original_rng = copy.deepcopy(self.rng)
+        else:
+            self.rng = copy.deepcopy(self._original_rng)
+        if self._initial_screen is not None:
+            screen = self._initial_screen.reshape(self.ny, self.nx)
+        else:
+            screen = von_karman_screen(self.nx, self.ny, self._delta, self._Cn_squared, self._L0, self.rng)
+        self._ring = torch.from_numpy(np.ascontiguousarray(screen)).to(device='cuda', dtype=self.dtype)
+        self._row0 = 0
+        self._col0 = 0
+        self._shifted = self._ring.clone()
+        self.center = np.zeros(2)
+        self._t = 0
+
+    @property
+    def Cn_squared(self):  # noqa: N802
+        return self._Cn_squared
+
+    @Cn_squared.setter
+    def Cn_squared(self, Cn_squared):  # noqa: N802, N803
+        self._Cn_squared = Cn_squared
+
+    @property
+    def outer_scale(self):
+        return self._L0
+
+    @outer_scale.setter
+    def outer_scale(self, L0):  # noqa: N803
+        self._L0 = L0
+        if self._initialized:
+            self._make_ab_matrices()
+
+    # -- time stepping -------------------------------------------------------------------------------------
+    def _extrude(self, where, noise):
+        w = _WHERE[where]
+        d = self._dev
+        vertical = w <= 1
+        A, B, idx = (d['A_v'], d['B_v'], d['idx_v']) if vertical else (d['A_h'], d['B_h'], d['idx_h'])
+        rc = _lib.lib().hx_atmosphere_extrude(_lib.dptr(self._ring), self.ny, self.nx, self._row0, self._col0, w,
+                                              _lib.dptr(idx), int(idx.numel()), _lib.dptr(A), _lib.dptr(B),
+                                              int(B.shape[1]), _lib.dptr(noise), _lib.dtype_code(self.dtype),
+                                              _lib.dptr(self._work), _lib.stream_handle())
+        _lib.check(rc, 'hx_atmosphere_extrude')
+        if w == 0:
+            self._row0 = (self._row0 - 1) % self.ny
+        elif w == 1:
+            self._row0 = (self._row0 + 1) % self.ny
+        elif w == 2:
+            self._col0 = (self._col0 - 1) % self.nx
+        else:
+            self._col0 = (self._col0 + 1) % self.nx
+
+    def evolve_until(self, t):
+        """infinite_atmospheric_layer.py:305-364."""
+        if t is None:
+            self.reset()
+            return
+        if t < self._t:
+            raise ValueError('Backwards temporal evolution is not allowed.')
+        delta = self._delta
+        old_center = np.round(self.center / delta).astype('int')
+        self.center = self.center + self.velocity * (t - self._t)
+        new_center = np.round(self.center / delta).astype('int')
+        self._t = t
+        steps = new_center - old_center
+        sub = self.center - new_center * delta
+        plan = (['left' if steps[0] < 0 else 'right'] * abs(int(steps[0])) +
+                ['bottom' if steps[1] < 0 else 'top'] * abs(int(steps[1])))
+        if plan:
+            std = math.sqrt(self._Cn_squared)
+            draws = [self.rng.normal(0, std, size=(self.B_vertical if _WHERE[w] <= 1 else self.B_horizontal).shape[1])
+                     for w in plan]
+            width = max(x.size for x in draws)
+            host = np.zeros((len(plan), width))
+            for i, x in enumerate(draws):
+                host[i, :x.size] = x
+            noise = torch.from_numpy(host).to(device='cuda', dtype=self.dtype)
+            for i, w in enumerate(plan):
+                self._extrude(w, noise[i])
+        if self.use_interpolation:
+            shift = sub / delta  # [x_px, y_px]
+            taps_row = quintic_weights(shift[0])  # along x
+            taps_col = quintic_weights(shift[1])  # along y
+        else:
+            taps_row = taps_col = np.array([0, 0, 0, 1.0, 0, 0, 0])
+        self._shift(taps_row, taps_col)
+
+    def _shift(self, taps_row, taps_col):
+        tr = np.ascontiguousarray(taps_row, np.float64)
+        tc = np.ascontiguousarray(taps_col, np.float64)
+        P = _lib.ctypes.POINTER(_lib.ctypes.c_double)
+        rc = _lib.lib().hx_atmosphere_shift(_lib.dptr(self._ring), self.ny, self.nx, self._row0, self._col0,
+                                            tr.ctypes.data_as(P), tc.ctypes.data_as(P), _lib.dptr(self._shifted),
+                                            _lib.dtype_code(self.dtype), _lib.stream_handle())
+        _lib.check(rc, 'hx_atmosphere_shift')
+
+    # -- screens -------------------------------------------------------------------------------------------
+    @property
+    def achromatic_screen(self):
+        """The unshifted screen (logical order), radians at a wavelength of 1 m."""
+        taps = np.array([0, 0, 0, 1.0, 0, 0, 0])
+        out = torch.empty_like(self._shifted)
+        P = _lib.ctypes.POINTER(_lib.ctypes.c_double)
+        rc = _lib.lib().hx_atmosphere_shift(_lib.dptr(self._ring), self.ny, self.nx, self._row0, self._col0,
+                                            taps.ctypes.data_as(P), taps.ctypes.data_as(P), _lib.dptr(out),
+                                            _lib.dtype_code(self.dtype), _lib.stream_handle())
+        _lib.check(rc, 'hx_atmosphere_shift')
+        return Field(out.reshape(-1), self.input_grid)
+
+    def _screen_tensor(self):
+        return self._shifted.reshape(-1)
+
+
+class MultiLayerAtmosphere(OpticalElement):
+    """Layers applied in order without inter-layer propagation (atmospheric_model.py:153-310 with
+    scintillation=False)."""
+
+    def __init__(self, layers, scintillation=False):
+        if scintillation:
+            raise NotImplementedError('scintillation needs Fresnel propagation between the layers')
+        self.layers = list(layers)
+        self._t = 0
+
+    def evolve_until(self, t):
+        for layer in self.layers:
+            layer.evolve_until(t)
+        self._t = t
+
+    def reset(self, make_independent_realization=False):
+        for layer in self.layers:
+            layer.reset(make_independent_realization)
+        self._t = 0
+
+    @property
+    def t(self):
+        return self._t
+
+    @t.setter
+    def t(self, t):
+        self.evolve_until(t)
+
+    def phase_for(self, wavelength):
+        total = None
+        for layer in self.layers:
+            p = layer.phase_for(wavelength).data
+            total = p if total is None else total + p
+        return Field(total, self.layers[0].input_grid)
+
+    def forward(self, wavefront):
+        for layer in self.layers:
+            wavefront = layer.forward(wavefront)
+        return wavefront
+
+    def backward(self, wavefront):
+        for layer in reversed(self.layers):
+            wavefront = layer.backward(wavefront)
+        return wavefront

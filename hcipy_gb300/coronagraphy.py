@@ -67,9 +67,19 @@ class LyotCoronagraph(OpticalElement):
         inst = self.prop.get_instance_data(wavefront.grid, None, wavefront.wavelength)
         if not self._can_fuse(inst):
             return self._forward_unfused(wavefront)
-        ft = inst.fourier_transform
         e = wavefront.electric_field
-        t = as_tensor(e).contiguous()
+        t = as_tensor(e)
+        if torch.is_grad_enabled() and t.requires_grad:
+            from .autograd import LyotFunction
+            out = LyotFunction.apply(t, self, inst)
+        else:
+            out = self._lyot_tensor(t, inst)
+        return Wavefront(Field(out, e.grid), wavefront.wavelength)
+
+    def _lyot_tensor(self, t, inst):
+        """The fused chain on a tensor of pupil fields (..., n): one library call."""
+        ft = inst.fourier_transform
+        t = t.detach().contiguous()
         split = ft.precision == 'split'
         one_minus, stop = self._fused_masks(t.dtype)
         a_fwd = complex(ft._w_in_scalar) * inst.norm_factor
@@ -87,7 +97,7 @@ class LyotCoronagraph(OpticalElement):
                                  _lib.dptr(out), _lib.dtype_code(out.dtype), None, _lib.HX_C64,
                                  _lib.dptr(ws), nbytes, _lib.stream_handle())
         _lib.check(rc, 'hx_lyot_execute')
-        return Wavefront(Field(out, e.grid), wavefront.wavelength)
+        return out
 
     def _forward_unfused(self, wavefront):
         wf_foc = self.prop.forward(wavefront)

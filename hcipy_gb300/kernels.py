@@ -1,0 +1,104 @@
+"""Element-wise and sparse device operations behind the optical elements (phase screens, influence functions).
+
+Every function launches a kernel of ``lib/libhcipy_gb300.so``; there is no CPU path.
+"""
+import numpy as np
+import torch
+
+from . import _lib
+
+_REAL = {torch.complex64: torch.float32, torch.complex128: torch.float64}
+
+
+def _batched(t, n):
+    """(batch, n) contiguous view of a tensor whose last axis has n elements."""
+    t = t.contiguous()
+    if t.shape[-1] != n:
+        raise ValueError('expected a last axis of %d elements, got %s' % (n, tuple(t.shape)))
+    return t.reshape(-1, n)
+
+
+def apply_phase(e, s, scale):
+    """e * exp(i * scale * s) with broadcasting of a leading batch (e or s may hold one field).
+
+    e: complex tensor (..., n); s: real tensor (..., n).  The result has the broader of the two batch shapes and
+    e's dtype; s is cast to the matching real type.
+    """
+    n = e.shape[-1]
+    rdt = _REAL[e.dtype]
+    s = s.to(device=e.device, dtype=rdt)
+    shape_e, shape_s = tuple(e.shape[:-1]), tuple(s.shape[:-1])
+    be = int(np.prod(shape_e)) if shape_e else 1
+    bs = int(np.prod(shape_s)) if shape_s else 1
+    batch = max(be, bs)
+    out_shape = (shape_e if be >= bs else shape_s) + (n,)
+    e2, s2 = _batched(e, n), _batched(s, n)
+    out = torch.empty(out_shape, dtype=e.dtype, device=e.device)
+    rc = _lib.lib().hx_phase_apply(n, batch, be, bs, _lib.dptr(e2), _lib.dtype_code(e.dtype), _lib.dptr(s2),
+                                   float(scale), _lib.dptr(out), _lib.stream_handle())
+    _lib.check(rc, 'hx_phase_apply')
+    return out
+
+
+def apply_phase_grad(e, s, scale, g_out, need_e=True, need_s=True):
+    """Gradients of ``apply_phase`` for real s: (g_e, g_s), each reduced to its input's batch shape."""
+    n = e.shape[-1]
+    rdt = _REAL[e.dtype]
+    s = s.to(device=e.device, dtype=rdt)
+    shape_e, shape_s = tuple(e.shape[:-1]), tuple(s.shape[:-1])
+    be = int(np.prod(shape_e)) if shape_e else 1
+    bs = int(np.prod(shape_s)) if shape_s else 1
+    batch = max(be, bs)
+    e2, s2 = _batched(e, n), _batched(s, n)
+    g2 = _batched(g_out.to(e.dtype), n)
+    g_e = torch.empty(shape_e + (n,), dtype=e.dtype, device=e.device) if need_e else None
+    g_s = torch.empty(shape_s + (n,), dtype=rdt, device=e.device) if need_s else None
+    rc = _lib.lib().hx_phase_apply_grad(n, batch, be, bs, _lib.dptr(e2), _lib.dtype_code(e.dtype), _lib.dptr(s2),
+                                        float(scale), _lib.dptr(g2), None if g_s is None else _lib.dptr(g_s),
+                                        None if g_e is None else _lib.dptr(g_e), _lib.stream_handle())
+    _lib.check(rc, 'hx_phase_apply_grad')
+    return g_e, g_s
+
+
+class SparseBasis(object):
+    """A sparse (npix x nact) influence-function matrix on the device, in CSR (pixels) and CSC (actuators) form."""
+
+    def __init__(self, csr, device, dtype):
+        import scipy.sparse
+        csr = scipy.sparse.csr_matrix(csr)
+        csr.sort_indices()
+        csc = csr.tocsc()
+        csc.sort_indices()
+        self.shape = csr.shape
+        self.dtype = dtype
+        self.row_ptr = torch.from_numpy(csr.indptr.astype(np.int32)).to(device)
+        self.col_idx = torch.from_numpy(csr.indices.astype(np.int32)).to(device)
+        self.vals = torch.from_numpy(csr.data).to(device=device, dtype=dtype)
+        self.col_ptr = torch.from_numpy(csc.indptr.astype(np.int32)).to(device)
+        self.row_idx = torch.from_numpy(csc.indices.astype(np.int32)).to(device)
+        self.vals_csc = torch.from_numpy(csc.data).to(device=device, dtype=dtype)
+
+    def apply(self, coeffs):
+        """surface[v, p] = sum_a M[p, a] coeffs[v, a] for coeffs of shape (..., nact)."""
+        npix, nact = self.shape
+        lead = tuple(coeffs.shape[:-1])
+        c = _batched(coeffs.to(device=self.vals.device, dtype=self.dtype), nact)
+        out = torch.empty(lead + (npix,), dtype=self.dtype, device=self.vals.device)
+        rc = _lib.lib().hx_influence_apply(npix, nact, _lib.dptr(self.row_ptr), _lib.dptr(self.col_idx),
+                                           _lib.dptr(self.vals), _lib.dtype_code(self.dtype), c.shape[0],
+                                           _lib.dptr(c), _lib.dptr(out), _lib.stream_handle())
+        _lib.check(rc, 'hx_influence_apply')
+        return out
+
+    def apply_transpose(self, g):
+        """g_coeffs[v, a] = sum_p M[p, a] g[v, p] for g of shape (..., npix)."""
+        npix, nact = self.shape
+        lead = tuple(g.shape[:-1])
+        g2 = _batched(g.to(device=self.vals.device, dtype=self.dtype), npix)
+        out = torch.empty(lead + (nact,), dtype=self.dtype, device=self.vals.device)
+        rc = _lib.lib().hx_influence_apply_transpose(npix, nact, _lib.dptr(self.col_ptr), _lib.dptr(self.row_idx),
+                                                     _lib.dptr(self.vals_csc), _lib.dtype_code(self.dtype),
+                                                     g2.shape[0], _lib.dptr(g2), _lib.dptr(out),
+                                                     _lib.stream_handle())
+        _lib.check(rc, 'hx_influence_apply_transpose')
+        return out

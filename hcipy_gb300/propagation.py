@@ -1,10 +1,17 @@
 """Propagators (hcipy/propagation) on the device."""
 import numpy as np
+import torch
 
 from . import _lib
 from .field import Field
 from .fourier import make_fourier_transform, MatrixFourierTransform
 from .optics import AgnosticOpticalElement, Wavefront, make_agnostic_forward, make_agnostic_backward
+
+
+def _differentiable(field):
+    """True when autograd records operations on this field's tensor."""
+    t = field.data if isinstance(field, Field) else field
+    return torch.is_grad_enabled() and isinstance(t, torch.Tensor) and t.requires_grad
 
 
 class FraunhoferPropagator(AgnosticOpticalElement):
@@ -52,9 +59,16 @@ class FraunhoferPropagator(AgnosticOpticalElement):
         ft = instance_data.fourier_transform
         e = wavefront.electric_field
         if isinstance(ft, MatrixFourierTransform):
-            res = ft._run(e, ft.input_grid, ft.output_grid, _lib.HX_FORWARD,
-                          complex(ft._w_in_scalar) * instance_data.norm_factor)
+            alpha = complex(ft._w_in_scalar) * instance_data.norm_factor
+            if _differentiable(e):
+                from .autograd import mft_apply
+                return Wavefront(Field(mft_apply(ft, e.data, _lib.HX_FORWARD, alpha), instance_data.output_grid),
+                                 wavefront.wavelength)
+            res = ft._run(e, ft.input_grid, ft.output_grid, _lib.HX_FORWARD, alpha)
         else:
+            if _differentiable(e):
+                raise NotImplementedError('gradients through an FFT-based Fraunhofer propagator are not implemented; '
+                                          'use grids that make the planner choose the matrix Fourier transform')
             res = ft.forward(e) * instance_data.norm_factor
         return Wavefront(Field(res.data, instance_data.output_grid), wavefront.wavelength)
 
@@ -65,8 +79,14 @@ class FraunhoferPropagator(AgnosticOpticalElement):
         e = wavefront.electric_field
         if isinstance(ft, MatrixFourierTransform):
             alpha = complex(ft._w_out_scalar / (2 * np.pi)**ft.ndim) / instance_data.norm_factor
+            if _differentiable(e):
+                from .autograd import mft_apply
+                return Wavefront(Field(mft_apply(ft, e.data, _lib.HX_BACKWARD, alpha), instance_data.input_grid),
+                                 wavefront.wavelength)
             res = ft._run(e, ft.output_grid, ft.input_grid, _lib.HX_BACKWARD, alpha)
         else:
+            if _differentiable(e):
+                raise NotImplementedError('gradients through an FFT-based Fraunhofer propagator are not implemented')
             res = ft.backward(e) / instance_data.norm_factor
         return Wavefront(Field(res.data, instance_data.input_grid), wavefront.wavelength)
 

@@ -85,3 +85,32 @@ def dark_hole_mask(focal, r_in=3.0, r_out=15.0):
     x, y = focal.points_list()
     r = np.hypot(x, y)
     return (r >= r_in) & (r <= r_out)
+
+
+def dm_gradient_workload(pupil_n=512, n_act=34, crosstalk=0.15, nvec=64, act_rms=1e-3, seed=4, fpm_q=8,
+                         fpm_num_airy=32, occulter_radius=4.0, stop_diameter=0.9, final_q=4, final_num_airy=32,
+                         roi=(3.0, 12.0)):
+    """The adjoint-gradient workload: a Gaussian-influence DM ahead of the Lyot coronagraph.
+
+    Defaults: 512^2 circular pupil, 34 x 34 actuators at pitch D/34 (crosstalk 0.15), the actuators with at
+    least 10% of their power inside the pupil, nvec = 64 command vectors of N(0, act_rms) (meters at
+    lambda0 = 1 m units, i.e. 1e-3 lambda0), FPM radius 4 lambda/D on a q=8, num_airy=32 grid (512^2), Lyot
+    stop 0.9 D, final grid q=4, num_airy=32 (256^2); the loss is the intensity summed over the half annulus
+    3-12 lambda/D with x > 0.
+    """
+    from .deformable_mirror import make_gaussian_influence_functions, find_illuminated_actuators
+    pupil = make_pupil_grid(pupil_n, 1)
+    aperture = circular_aperture(pupil, 1.0)
+    inf = make_gaussian_influence_functions(pupil, n_act, 1.0 / n_act, crosstalk=crosstalk)
+    inf = find_illuminated_actuators(inf, aperture, 0.1)
+    rng = np.random.default_rng(seed)
+    actuators = rng.standard_normal((nvec, inf.num_modes)) * act_rms
+    fpm_grid = make_focal_grid(fpm_q, fpm_num_airy)
+    fpm = 1 - circular_aperture(fpm_grid, 2 * occulter_radius)
+    stop = circular_aperture(pupil, stop_diameter)
+    focal = make_focal_grid(final_q, final_num_airy)
+    x, y = focal.points_list()
+    r = np.hypot(x, y)
+    roi_mask = (r >= roi[0]) & (r <= roi[1]) & (x > 0)
+    return dict(pupil=pupil, aperture=aperture, influence=inf, actuators=actuators, fpm_grid=fpm_grid, fpm=fpm,
+                stop=stop, focal=focal, roi=roi_mask)

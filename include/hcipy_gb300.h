@@ -46,6 +46,8 @@ extern "C" {
 /* Element types. */
 #define HX_C64 0
 #define HX_C128 1
+#define HX_F32 2 /* real arrays: DM surfaces, influence functions, phase screens */
+#define HX_F64 3
 
 /* Directions of a Fourier operator. */
 #define HX_FORWARD 0  /* FourierTransform.forward */
@@ -255,6 +257,53 @@ HX_API int hx_asp_transfer_function(int nx, int ny, double zero_x, double zero_y
 HX_API int hx_asp_impulse_response(int nx, int ny, double zero_x, double zero_y, double delta_x, double delta_y,
                             double wavenumber, double distance, int oversampling, int dtype, void* out,
                             void* stream);
+
+/* ------------------------------------------------------------------------
+ * Deformable mirror.
+ * Surface of nvec command vectors at once: surface[v, p] = sum_a Phi[p, a] actuators[v, a]
+ * (DeformableMirror.surface / ModeBasis.linear_combination, hcipy/optics/deformable_mirror.py:251-262,
+ * hcipy/mode_basis/mode_basis.py:239-258).  Phi (npix x nact) is CSR over pupil pixels; vals, actuators
+ * and surface are HX_F32 or HX_F64 device arrays, row-major (vector-major).
+ * ------------------------------------------------------------------------ */
+HX_API int hx_influence_apply(int npix, int nact, const int* row_ptr, const int* col_idx, const void* vals,
+                              int dtype, int nvec, const void* actuators, void* surface, void* stream);
+/* The transpose, g_actuators[v, a] = sum_p Phi[p, a] g_surface[v, p], from the CSC form of Phi
+ * (col_ptr[nact + 1], row_idx[nnz]): the gradient of a loss with respect to the actuators.  No counterpart
+ * in the reference, which has no gradients. */
+HX_API int hx_influence_apply_transpose(int npix, int nact, const int* col_ptr, const int* row_idx,
+                                        const void* vals, int dtype, int nvec, const void* g_surface,
+                                        void* g_actuators, void* stream);
+
+/* Phase screen: out[b, p] = e[b % batch_e, p] exp(i scale s[b % batch_s, p]) for b < batch (batch_e and
+ * batch_s are 1 or batch).  e/out are HX_C64 or HX_C128 (dtype), s the matching real type.  Replaces the
+ * exponentials of DeformableMirror.forward/backward (scale = +-2k, hcipy/optics/deformable_mirror.py:200-238)
+ * and AtmosphericLayer.forward/backward (scale = +-1/lambda, hcipy/atmosphere/atmospheric_model.py:143-151). */
+HX_API int hx_phase_apply(long long n, int batch, int batch_e, int batch_s, const void* e, int dtype,
+                          const void* s, double scale, void* out, void* stream);
+/* Its gradient for real s (no counterpart in the reference): g_s = scale Im(conj(out) g_out) (summed over
+ * the batch when batch_s == 1), g_e = g_out exp(-i scale s) (summed when batch_e == 1).  Either output may be
+ * NULL. */
+HX_API int hx_phase_apply_grad(long long n, int batch, int batch_e, int batch_s, const void* e, int dtype,
+                               const void* s, double scale, const void* g_out, void* g_s, void* g_e, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Infinite atmospheric layer (hcipy/atmosphere/infinite_atmospheric_layer.py:216-364).
+ * The ny x nx achromatic screen is a ring buffer: logical pixel (i, j) is stored at
+ * ((i + row0) % ny, (j + col0) % nx).  One extrusion (InfiniteAtmosphericLayer._extrude, :216-259):
+ * where = 0 bottom, 1 top, 2 left, 3 right; stencil_idx (device, nst int64 in [0, ny*nx)) indexes the
+ * logical flat screen (flipped for top/right as in the reference); A (nslice x nst), B (nslice x nb) and
+ * noise (nb) are HX_F32 or HX_F64 device arrays; work holds nst values.  The caller passes the offsets
+ * before the step and then moves them: bottom row0 -= 1, top row0 += 1, left col0 -= 1, right col0 += 1
+ * (mod ny / nx).
+ * ------------------------------------------------------------------------ */
+HX_API int hx_atmosphere_extrude(void* ring, int ny, int nx, int row0, int col0, int where,
+                                 const long long* stencil_idx, int nst, const void* A, const void* B, int nb,
+                                 const void* noise, int dtype, void* work, void* stream);
+/* Sub-pixel shift of the logical screen into out (ny x nx): the separable 7-tap filter taps_row along x
+ * then taps_col along y, clamp to edge (quintic weights of subpixel_shift, hcipy/_math/subpixel_shift.py:7-343;
+ * taps are host arrays of 7 float64). */
+HX_API int hx_atmosphere_shift(const void* ring, int ny, int nx, int row0, int col0, const double* taps_row,
+                               const double* taps_col, void* out, int dtype, void* stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,108 @@
+"""Infinite atmospheric layer and sub-pixel shift on the GPU against the reference's replayed values.
+
+The golden case is the reference's own layer (24^2 grid, seed 5, L0 = 25 m, wind along x) evolved over three
+time steps; the layer here starts from the reference's initial screen, uses the reference's A and B matrices
+(B comes from an SVD whose singular vectors differ between LAPACK builds at ~1e-9; the host-side matrices are
+pinned separately on the CPU) and is fed the reference's noise rows, so every extruded column and every
+sub-pixel-shifted screen must agree.
+Tolerances: float64 screens 1e-12 relative (the same products summed in another order); float32 1e-5.
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import load_golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+hg = pytest.importorskip('hcipy_gb300')
+
+
+def _grid(rec, prefix):
+    return hg.CartesianGrid(hg.RegularCoords(rec[prefix + '_delta'], rec[prefix + '_dims'], rec[prefix + '_zero']))
+
+
+def _use_reference_matrices(layer, g):
+    layer.A_vertical, layer.B_vertical = g['A_vertical'], g['B_vertical']
+    layer.A_horizontal, layer.B_horizontal = g['A_horizontal'], g['B_horizontal']
+    layer._upload_matrices()
+
+
+class _Replay(object):
+    """Stands in for the layer's generator: returns the recorded extrusion noise rows in order."""
+
+    def __init__(self, rows):
+        self.rows = list(rows)
+
+    def normal(self, loc, scale, size):
+        return self.rows.pop(0)
+
+
+def test_subpixel_shift_matches_reference():
+    g = load_golden('subpixel')
+    for i in range(4):
+        out = hg.subpixel_shift(torch.from_numpy(g['img']), float(g['dy_%d' % i]), float(g['dx_%d' % i]))
+        assert rel_err(out.cpu().numpy(), g['out_%d' % i]) < 1e-13
+    with pytest.raises(ValueError):
+        hg.subpixel_shift(torch.from_numpy(g['img']), 0.6, 0.0)
+
+
+@pytest.mark.parametrize('dtype,tol', [(torch.float64, 1e-12), (torch.float32, 1e-5)])
+def test_infinite_layer_replays_reference(dtype, tol):
+    g = load_golden('atmosphere')
+    grid = _grid(g, 'pupil')
+    layer = hg.InfiniteAtmosphericLayer(grid, float(g['cn2']), L0=25, velocity=tuple(g['velocity']),
+                                        use_interpolation=True, seed=5, dtype=dtype, initial_screen=g['screen0'])
+    assert np.array_equal(layer.stencil_bottom_idx, g['stencil_bottom_idx'])
+    _use_reference_matrices(layer, g)
+    rows = [r for i in range(3) for r in g['noise_%d' % i]]
+    layer.rng = _Replay(rows)
+    t = 0.0
+    for i in range(3):
+        t += float(g['dt_%d' % i])
+        layer.t = t
+        assert rel_err(layer.achromatic_screen.numpy(), g['screen_%d' % i]) < tol, i
+        assert rel_err(layer.phase_for(1.0).numpy(), g['shifted_%d' % i]) < tol, i
+    assert not layer.rng.rows
+
+
+def test_layer_extrudes_all_four_directions_like_the_oracle():
+    """Bottom/top/left/right extrusions through the ring buffer against the oracle's array copies."""
+    from oracle import atmosphere as oatm
+    g = load_golden('atmosphere')
+    grid = _grid(g, 'pupil')
+    nx, ny = (int(d) for d in g['pupil_dims'])
+    layer = hg.InfiniteAtmosphericLayer(grid, float(g['cn2']), L0=25, seed=5, initial_screen=g['screen0'])
+    _use_reference_matrices(layer, g)
+    rng = np.random.default_rng(9)
+    screen = g['screen0'].copy()
+    for where in ['right', 'top', 'left', 'bottom', 'top', 'right', 'right', 'bottom']:
+        vertical = where in ('top', 'bottom')
+        a = g['A_vertical'] if vertical else g['A_horizontal']
+        b = g['B_vertical'] if vertical else g['B_horizontal']
+        idx = g['stencil_bottom_idx'] if vertical else g['stencil_left_idx']
+        noise = rng.standard_normal(b.shape[1])
+        screen = oatm.extrude(screen, (ny, nx), where, a, b, idx, noise)
+        layer._extrude(where, torch.from_numpy(noise).cuda())
+        assert rel_err(layer.achromatic_screen.numpy(), screen) < 1e-12, where
+
+
+def test_layer_forward_backward_and_multilayer():
+    g = load_golden('atmosphere')
+    grid = _grid(g, 'pupil')
+    l1 = hg.InfiniteAtmosphericLayer(grid, float(g['cn2']), L0=25, velocity=3.0, seed=5, initial_screen=g['screen0'])
+    l2 = hg.InfiniteAtmosphericLayer(grid, float(g['cn2']) * 2, L0=25, velocity=(0.0, -2.0), seed=6)
+    atm = hg.MultiLayerAtmosphere([l1, l2])
+    atm.evolve_until(0.05)
+    wl = 0.7
+    rng = np.random.default_rng(0)
+    e = rng.standard_normal(grid.size) + 1j * rng.standard_normal(grid.size)
+    wf = hg.Wavefront(hg.Field(e, grid), wl)
+    phase = l1.phase_for(wl).numpy() + l2.phase_for(wl).numpy()
+    assert rel_err(atm.phase_for(wl).numpy(), phase) < 1e-13
+    out = atm.forward(wf).electric_field.numpy()
+    assert rel_err(out, e * np.exp(1j * phase)) < 1e-12
+    back = atm.backward(atm.forward(wf)).electric_field.numpy()
+    assert rel_err(back, e) < 1e-12
+    with pytest.raises(ValueError):
+        l1.evolve_until(0.01)

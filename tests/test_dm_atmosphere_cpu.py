@@ -1,0 +1,90 @@
+"""Host-side plan data of the deformable mirror and the atmospheric layer against the reference's own values.
+
+These run without a GPU: the influence functions, the extrusion stencils and the autoregressive matrices are
+built on the host (as the reference builds them), so they are compared with the golden vectors directly.
+Tolerances: the same float64 operations in the same order as the reference, so 1e-12 relative (observed 0).
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_err
+
+pytest.importorskip('scipy')
+
+
+def _grid(rec, prefix):
+    from hcipy_gb300.field import CartesianGrid, RegularCoords
+    return CartesianGrid(RegularCoords(rec[prefix + '_delta'], rec[prefix + '_dims'], rec[prefix + '_zero']))
+
+
+def test_gaussian_influence_functions_match_reference():
+    from hcipy_gb300 import deformable_mirror as dmm
+    g = load_golden('dm')
+    inf = dmm.make_gaussian_influence_functions(_grid(g, 'pupil'), 8, 1 / 8, crosstalk=0.15)
+    m = inf.transformation_matrix.toarray()
+    assert m.shape == g['influence'].shape
+    assert np.count_nonzero(m) == np.count_nonzero(g['influence'])
+    assert rel_err(m, g['influence']) < 1e-12
+    assert rel_err(m @ g['actuators'], g['surface']) < 1e-12
+
+
+def test_find_illuminated_actuators():
+    from hcipy_gb300 import deformable_mirror as dmm
+    g = load_golden('dm')
+    grid = _grid(g, 'pupil')
+    inf = dmm.make_gaussian_influence_functions(grid, 8, 1 / 8, crosstalk=0.15)
+    aperture = np.abs(g['E']) > 0
+    sel = dmm.find_illuminated_actuators(inf, aperture, 0.1)
+    m = g['influence']
+    keep = (np.abs(m[aperture])**2).sum(0) >= 0.1 * (np.abs(m)**2).sum(0)
+    assert sel.num_modes == keep.sum()
+    assert rel_err(sel.transformation_matrix.toarray(), m[:, keep]) < 1e-12
+
+
+def test_actuator_positions_bmc_convention():
+    from hcipy_gb300.deformable_mirror import make_actuator_positions
+    x, y = make_actuator_positions(4, 0.25)
+    assert np.allclose(np.unique(x), [-0.375, -0.125, 0.125, 0.375])
+    assert np.allclose(np.unique(y), [-0.375, -0.125, 0.125, 0.375])
+
+
+def test_atmosphere_stencils_and_matrices_match_reference():
+    from hcipy_gb300 import atmosphere as at
+    g = load_golden('atmosphere')
+    grid = _grid(g, 'pupil')
+    nx, ny = (int(d) for d in g['pupil_dims'])
+    bottom, left = at.make_stencils(nx, ny, 2, np.random.default_rng(5))
+    assert np.array_equal(bottom, g['stencil_bottom_idx'])
+    assert np.array_equal(left, g['stencil_left_idx'])
+    av, bv = at.ar_matrices(grid, bottom, 'bottom', 25)
+    ah, bh = at.ar_matrices(grid, left, 'left', 25)
+    assert rel_err(av, g['A_vertical']) < 1e-12
+    assert rel_err(ah, g['A_horizontal']) < 1e-12
+    # B is defined up to the signs of the singular vectors: compare B B^T, and B itself (same LAPACK here).
+    assert rel_err(bv @ bv.T, g['B_vertical'] @ g['B_vertical'].T) < 1e-12
+    assert rel_err(bh @ bh.T, g['B_horizontal'] @ g['B_horizontal'].T) < 1e-12
+
+
+def test_quintic_weights_match_reference():
+    from hcipy_gb300.atmosphere import quintic_weights
+    g = load_golden('subpixel')
+    for i in range(4):
+        assert rel_err(quintic_weights(float(g['dy_%d' % i])), g['wy_%d' % i]) < 1e-14
+        assert rel_err(quintic_weights(float(g['dx_%d' % i])), g['wx_%d' % i]) < 1e-14
+
+
+def test_von_karman_screen_statistics():
+    """The package's initial screen follows the von Karman structure function 2 (C(0) - C(r)) within the
+    sampling error and the power lost above the grid's Nyquist frequency (10-15% at 4-8 pixels)."""
+    from hcipy_gb300 import atmosphere as at
+    rng = np.random.default_rng(0)
+    n, d, l0 = 128, 8.0 / 128, 25.0
+    cn2 = at.Cn_squared_from_fried_parameter(0.5, 500e-9)
+    r0 = at.fried_parameter_from_Cn_squared(cn2, 1.0)
+    for lag in (4, 8):
+        sf = []
+        for _ in range(6):
+            s = at.von_karman_screen(n, n, np.array([d, d]), cn2, l0, rng, pad=4)
+            sf.append(np.mean((s[:, lag:] - s[:, :-lag])**2))
+        theory = 2 * (at.von_karman_covariance(0.0, r0, l0) - at.von_karman_covariance(lag * d, r0, l0))
+        assert 0.75 < np.mean(sf) / theory < 1.1, (lag, np.mean(sf) / theory)
