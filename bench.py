@@ -45,6 +45,7 @@ def parse_args():
     p.add_argument('--pupil', type=int, default=2048)
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--cpu-seconds', type=float, default=10.0)
+    p.add_argument('--grad-steps', type=int, default=20, help='timed DM-gradient steps (0: skip that leg)')
     return p.parse_args()
 
 
@@ -211,6 +212,80 @@ def dark_hole_error(img, ref_img, focal, aperture_peak):
     return float(d.max()), float(d.mean()), float(ni_ref[mask].mean())
 
 
+def run_grad(args, dev):
+    """Adjoint gradient steps: 64 DM command vectors -> Lyot coronagraph -> image intensity over a half annulus;
+    one step = loss + gradient in all actuators through the device adjoints.  Returns the JSON object."""
+    import torch
+    import hcipy_gb300 as hg
+    from hcipy_gb300 import workloads
+    from oracle import optics
+    w = workloads.dm_gradient_workload()
+    pupil, fpm_grid, focal = w['pupil'], w['fpm_grid'], w['focal']
+    lyot = hg.LyotCoronagraph(pupil, hg.Field(w['fpm'], fpm_grid), hg.Field(w['stop'], pupil),
+                              precision=args.precision)
+    prop = hg.FraunhoferPropagator(pupil, focal, precision=args.precision)
+    dm = hg.DeformableMirror(w['influence'])
+    e0 = torch.from_numpy(w['aperture'].astype(np.complex64)).to(dev)
+    roi = torch.from_numpy(w['roi'].astype(np.float32)).to(dev)
+    a0 = torch.from_numpy(w['actuators'].astype(np.float32)).to(dev)
+
+    def step():
+        a = a0.clone().requires_grad_(True)
+        dm.actuators = a
+        e = dm.forward(hg.Wavefront(hg.Field(e0, pupil), 1.0))
+        img = prop.forward(lyot.forward(e)).electric_field.data
+        loss = ((img.real**2 + img.imag**2) * roi).sum()
+        loss.backward()
+        return loss, a.grad
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = hg.launch_count()
+    t0.record(stream)
+    for _ in range(args.grad_steps):
+        loss, grad = step()
+    t1.record(stream)
+    t1.synchronize()
+    ms = t0.elapsed_time(t1) / args.grad_steps
+    launches = (hg.launch_count() - launches0) / args.grad_steps
+
+    # accuracy: the float64 oracle gradient of the first command vectors
+    from oracle.grids import RegularGrid
+    og = lambda g: RegularGrid(g.delta, g.dims, g.zero)  # noqa: E731
+    chain = optics.LyotChain(og(pupil), og(fpm_grid), og(focal), w['fpm'], w['stop'])
+    m = w['influence'].transformation_matrix
+    nv = 2
+    g_dev = grad[:nv].double().cpu().numpy()
+    errs = []
+    for v in range(nv):
+        _, g_ref = optics.dm_lyot_loss_grad(chain, m, w['aperture'], w['actuators'][v], w['roi'])
+        errs.append(float(np.linalg.norm(g_dev[v] - g_ref) / np.linalg.norm(g_ref)))
+    # CPU baseline: the same adjoint gradient with the oracle (complex64 numpy/OpenBLAS), per command vector
+    chain64 = optics.LyotChain(og(pupil), og(fpm_grid), og(focal), w['fpm'], w['stop'], dtype=np.complex64)
+    n, t_start = 0, time.perf_counter()
+    while n < 1 or time.perf_counter() - t_start < args.cpu_seconds / 2:
+        optics.dm_lyot_loss_grad(chain64, m, w['aperture'], w['actuators'][n % len(w['actuators'])], w['roi'])
+        n += 1
+    cpu_dt = time.perf_counter() - t_start
+    nvec = w['actuators'].shape[0]
+    return {
+        'metric': 'adjoint grad steps/s', 'value': 1000.0 / ms, 'unit': 'grad steps/s', 'ms_per_step': ms,
+        'steps': args.grad_steps, 'gpu_launches_per_step': launches,
+        'config': {'workload': 'DM (34x34 Gaussian, %d illuminated actuators) -> Lyot coronagraph -> image '
+                               'intensity over 3-12 lambda/D, x > 0; loss + gradient' % w['influence'].num_modes,
+                   'pupil': int(pupil.dims[0]), 'fpm_grid': int(fpm_grid.dims[0]), 'image': int(focal.dims[0]),
+                   'command_vectors': nvec, 'precision': args.precision,
+                   'l2': 'not flushed; a step moves >1 GB (64 fields of 512^2, complex128 intermediates)'},
+        'accuracy': {'grad_rel_l2_err_max': max(errs), 'vectors_checked': nv, 'against': 'float64 oracle adjoint'},
+        'cpu_baseline': {'value': n / cpu_dt / nvec, 'unit': 'grad steps/s', 'cores': host_cores(), 'kind': 'port',
+                         'sample': '%d command vectors in %.1f s (oracle adjoint gradient, complex64 numpy/OpenBLAS; '
+                                   'the reference has no gradient)' % (n, cpu_dt)},
+    }
+
+
 def run_ours(args, rank, world, dist):
     import torch
     import hcipy_gb300 as hg
@@ -368,6 +443,8 @@ def run_ours(args, rank, world, dist):
     }
     if cpu is not None:
         line['cpu_baseline'] = cpu
+    if args.grad_steps > 0:
+        line['grad_steps'] = run_grad(args, dev)
     print(json.dumps(line), flush=True)
 
 

@@ -103,3 +103,34 @@ class LyotChain(object):
 
     def __call__(self, e):
         return self.image(self.lyot(e))
+
+    def image_adjoint(self, g):
+        """Conjugate transpose of ``image``: conj(a_img) F1^H g F2^H."""
+        g = np.asarray(g, self.dtype).reshape(self.focal_shape)
+        return (np.conj(self.a_img) * (self.f1.conj().T @ (g @ self.f2.conj().T))).ravel()
+
+    def lyot_adjoint(self, g):
+        """Conjugate transpose of ``lyot``: u - conj(a_fwd) M1^H [(1 - M) conj(a_bwd) M1 u M2] M2^H, u = S g."""
+        u = np.asarray(g, self.dtype).reshape(self.shape_in) * self.stop
+        v = (self.m1 @ (u @ self.m2)) * np.conj(self.a_bwd)
+        v *= self.one_minus_fpm
+        w = ((self.m1h @ v) @ self.m2h) * np.conj(self.a_fwd)
+        return (u - w).ravel()
+
+
+def dm_lyot_loss_grad(chain, influence, aperture, actuators, roi, wavelength=1.0):
+    """Loss sum_roi |image|^2 of one command vector through DM -> Lyot -> image, and its gradient in the
+    actuators by the adjoint chain (torch's convention: dL/d(conj z) times 2 for complex intermediates).
+
+    influence: (npix x nact) scipy sparse or dense matrix; the DM reflects E exp(2ik S)
+    (hcipy/optics/deformable_mirror.py:200-217).
+    """
+    k = 2 * np.pi / wavelength
+    s = influence @ np.asarray(actuators, np.float64)
+    e = np.asarray(aperture) * np.exp(2j * k * s)
+    img = chain(e)
+    roi = np.asarray(roi, np.float64)
+    loss = float(np.sum(roi * np.abs(img)**2))
+    g_e = chain.lyot_adjoint(chain.image_adjoint(2 * roi * img))
+    g_s = 2 * k * np.imag(np.conj(e) * g_e)
+    return loss, influence.T @ g_s

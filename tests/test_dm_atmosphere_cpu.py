@@ -88,3 +88,35 @@ def test_von_karman_screen_statistics():
             sf.append(np.mean((s[:, lag:] - s[:, :-lag])**2))
         theory = 2 * (at.von_karman_covariance(0.0, r0, l0) - at.von_karman_covariance(lag * d, r0, l0))
         assert 0.75 < np.mean(sf) / theory < 1.1, (lag, np.mean(sf) / theory)
+
+
+def test_oracle_lyot_adjoint_and_gradient():
+    """The oracle's adjoint chain (the checker of the device gradients): dot-product identity and central
+    differences of its loss."""
+    import hcipy_gb300 as hg
+    from hcipy_gb300 import workloads
+    from hcipy_gb300.deformable_mirror import make_gaussian_influence_functions
+    from oracle import optics as oo
+    from oracle.grids import RegularGrid
+    og = lambda g: RegularGrid(g.delta, g.dims, g.zero)  # noqa: E731
+    pupil, fpm_grid, focal = hg.make_pupil_grid(48, 1), hg.make_focal_grid(3.7, 6), hg.make_focal_grid(3.3, 8)
+    fpm = 1 - workloads.circular_aperture(fpm_grid, 5.0)
+    ch = oo.LyotChain(og(pupil), og(fpm_grid), og(focal), fpm, workloads.circular_aperture(pupil, 0.9))
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(pupil.size) + 1j * rng.standard_normal(pupil.size)
+    w = rng.standard_normal(focal.size) + 1j * rng.standard_normal(focal.size)
+    lhs, rhs = np.vdot(w, ch(x)), np.vdot(ch.lyot_adjoint(ch.image_adjoint(w)), x)
+    assert abs(lhs - rhs) < 1e-13 * np.linalg.norm(w) * np.linalg.norm(ch(x))
+    inf = make_gaussian_influence_functions(pupil, 6, 1 / 6).transformation_matrix
+    ap = workloads.circular_aperture(pupil, 1.0)
+    fx, fy = focal.points_list()
+    roi = (np.hypot(fx, fy) >= 2) & (np.hypot(fx, fy) <= 6) & (fx > 0)
+    a = rng.standard_normal(inf.shape[1]) * 2e-3
+    _, g = oo.dm_lyot_loss_grad(ch, inf, ap, a, roi)
+    h = 1e-6
+    for i in (3, 7, 20):
+        ap_, am_ = a.copy(), a.copy()
+        ap_[i] += h
+        am_[i] -= h
+        fd = (oo.dm_lyot_loss_grad(ch, inf, ap, ap_, roi)[0] - oo.dm_lyot_loss_grad(ch, inf, ap, am_, roi)[0]) / (2 * h)
+        assert abs(fd - g[i]) < 1e-7 * np.abs(g).max()
