@@ -94,7 +94,7 @@ int launch_shape(int M, const std::vector<int>& radices, int nlines, int batch, 
     a.radix_code = 0;
     for (size_t i = 0; i < radices.size(); ++i) a.radix_code |= (unsigned long long)radices[i] << (4 * i);
     *threads = thr;
-    *smem = (size_t)lpc * a.pitch * sizeof(typename cplx<T>::type);
+    *smem = (size_t)smem_elems(lpc * a.pitch) * sizeof(typename cplx<T>::type);
     return HX_OK;
 }
 

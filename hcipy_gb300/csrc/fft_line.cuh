@@ -245,6 +245,11 @@ struct Ppt<double, MIXED> { static constexpr int value = MIXED ? 4 : 8; };
 
 constexpr int kFftThreads = 512;
 
+// Shared-memory index with one pad element per 32: breaks the power-of-two strides of the early Stockham stages
+// (16-way bank conflicts at radix 8) down to 2-way.
+__device__ __forceinline__ int sidx(int x) { return x + (x >> 5); }
+__host__ __device__ constexpr int smem_elems(int n) { return n + (n >> 5) + 1; }
+
 // One Stockham stage of radix R over all lines in shared memory.
 template <typename T, int R, int SIGN, bool MIXED>
 __device__ __forceinline__ void fft_stage(typename cplx<T>::type* buf, int M, int pitch, int lines, int Ns,
@@ -254,6 +259,9 @@ __device__ __forceinline__ void fft_stage(typename cplx<T>::type* buf, int M, in
     const int nb = M / R;
     const int total = lines * nb;
     const int stride = M / (Ns * R);
+    // Power-of-two kernels index with shifts and masks (runtime integer division costs ~20 instructions).
+    const int lg_nb = MIXED ? 0 : __ffs(nb) - 1;
+    const int lg_ns = MIXED ? 0 : __ffs(Ns) - 1;
     Cx v[BPT][R];
     int dst[BPT];
 #pragma unroll
@@ -261,12 +269,21 @@ __device__ __forceinline__ void fft_stage(typename cplx<T>::type* buf, int M, in
         const int b = threadIdx.x + i * blockDim.x;
         dst[i] = -1;
         if (b < total) {
-            const int line = b / nb;
-            const int j = b - line * nb;
+            int line, j, k, jd;
+            if (MIXED) {
+                line = b / nb;
+                j = b - line * nb;
+                k = j % Ns;
+                jd = j / Ns;
+            } else {
+                line = b >> lg_nb;
+                j = b & (nb - 1);
+                k = j & (Ns - 1);
+                jd = j >> lg_ns;
+            }
             const int base = line * pitch;
-            const int k = j % Ns;
 #pragma unroll
-            for (int r = 0; r < R; ++r) v[i][r] = buf[base + j + r * nb];
+            for (int r = 0; r < R; ++r) v[i][r] = buf[sidx(base + j + r * nb)];
 #pragma unroll
             for (int r = 1; r < R; ++r) {
                 Cx w = tw[r * k * stride];
@@ -274,7 +291,7 @@ __device__ __forceinline__ void fft_stage(typename cplx<T>::type* buf, int M, in
                 v[i][r] = c_mul(v[i][r], w);
             }
             Dft<T, R, SIGN>::run(v[i]);
-            dst[i] = base + (j / Ns) * Ns * R + k;
+            dst[i] = base + jd * Ns * R + k;
         }
     }
     __syncthreads();
@@ -282,7 +299,7 @@ __device__ __forceinline__ void fft_stage(typename cplx<T>::type* buf, int M, in
     for (int i = 0; i < BPT; ++i) {
         if (dst[i] >= 0) {
 #pragma unroll
-            for (int r = 0; r < R; ++r) buf[dst[i] + r * Ns] = v[i][r];
+            for (int r = 0; r < R; ++r) buf[sidx(dst[i] + r * Ns)] = v[i][r];
         }
     }
     __syncthreads();
@@ -308,6 +325,22 @@ __device__ __forceinline__ void fft_smem(typename cplx<T>::type* buf, const Line
     }
 }
 
+// (line, output index) of the i-th stored element: lines fastest when lines are adjacent in memory.
+__device__ __forceinline__ void store_coords(int i, int lines, bool line_fast, int count, int& ll, int& kk) {
+    if (line_fast) {
+        if (lines == 1) { ll = 0; kk = i; }
+        else if (lines == 2) { ll = i & 1; kk = i >> 1; }
+        else { ll = i % lines; kk = i / lines; }
+    } else if ((count & (count - 1)) == 0) {
+        const int lg = __ffs(count) - 1;
+        ll = i >> lg;
+        kk = i & (count - 1);
+    } else {
+        ll = i / count;
+        kk = i - ll * count;
+    }
+}
+
 // grid: x = line blocks, y = batch.  SIGN = -1 forward, +1 inverse (of the main FFT).
 template <typename T, int SIGN, bool CONV, bool MIXED>
 __global__ void __launch_bounds__(kFftThreads) fft_line_kernel(const __grid_constant__ LineArgs<T> a) {
@@ -323,26 +356,55 @@ __global__ void __launch_bounds__(kFftThreads) fft_line_kernel(const __grid_cons
     const Cx zero = make_c<T>(T(0), T(0));
 
     // ---- load ----
+    // U elements per thread per round (8 in float, 4 in double to stay within 128 registers): their global loads
+    // are all issued before any shared store, so a thread keeps U requests in flight instead of one.
+    constexpr int U = sizeof(T) == 4 ? 8 : 4;
     const int nload = lines * a.M;
     const bool line_fast = (a.in_es != 1);
-    for (int i = threadIdx.x; i < nload; i += blockDim.x) {
-        int ll, j;
-        if (line_fast) { ll = i % lines; j = i / lines; }
-        else { ll = i / a.M; j = i - ll * a.M; }
-        Cx val = zero;
-        if (j < a.n_log) {
-            int pa = j + a.load_add;
-            pa %= a.n_log;
-            if (pa < 0) pa += a.n_log;
-            const int p = pa - a.in_offset;
-            if (p >= 0 && p < a.in_count) {
-                const long long l = l0 + ll;
-                val = in[l * a.in_ls + (long long)p * a.in_es];
-                if (a.pre) val = c_mul(val, a.pre[l * a.pre_ls + p]);
-                if (a.chirp_in) val = c_mul(val, a.chirp_in[j]);
+    const bool pow2_m = (a.M & (a.M - 1)) == 0;
+    const int lg_m = __ffs(a.M) - 1;
+    // Index shifts reduced once, so each element needs one conditional subtraction instead of a modulo.
+    const int ladd = ((a.load_add % a.n_log) + a.n_log) % a.n_log;
+    const int soff = ((a.out_offset + a.store_add) % a.out_mod + a.out_mod) % a.out_mod;
+    for (int i0 = threadIdx.x; i0 < nload; i0 += U * blockDim.x) {
+        Cx val[U];
+        int dst[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = i0 + u * blockDim.x;
+            val[u] = zero;
+            dst[u] = -1;
+            if (i < nload) {
+                int ll, j;
+                if (line_fast) {
+                    if (lines == 1) { ll = 0; j = i; }
+                    else if (lines == 2) { ll = i & 1; j = i >> 1; }
+                    else { ll = i % lines; j = i / lines; }
+                } else if (pow2_m) {
+                    ll = i >> lg_m;
+                    j = i & (a.M - 1);
+                } else {
+                    ll = i / a.M;
+                    j = i - ll * a.M;
+                }
+                dst[u] = ll * a.pitch + j;
+                if (j < a.n_log) {
+                    int pa = j + ladd;
+                    if (pa >= a.n_log) pa -= a.n_log;
+                    const int p = pa - a.in_offset;
+                    if (p >= 0 && p < a.in_count) {
+                        const long long l = l0 + ll;
+                        Cx v = in[l * a.in_ls + (long long)p * a.in_es];
+                        if (a.pre) v = c_mul(v, a.pre[l * a.pre_ls + p]);
+                        if (a.chirp_in) v = c_mul(v, a.chirp_in[j]);
+                        val[u] = v;
+                    }
+                }
             }
         }
-        buf[ll * a.pitch + j] = val;
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (dst[u] >= 0) buf[sidx(dst[u])] = val[u];
     }
     __syncthreads();
 
@@ -355,7 +417,8 @@ __global__ void __launch_bounds__(kFftThreads) fft_line_kernel(const __grid_cons
             const int k = i - ll * a.M;
             Cx m = a.mid[(long long)(l0 + ll) * a.mid_ls + (long long)k * a.mid_es];
             if (a.mid_conj) m.y = -m.y;
-            buf[ll * a.pitch + k] = c_mul(buf[ll * a.pitch + k], m);
+            const int q = sidx(ll * a.pitch + k);
+            buf[q] = c_mul(buf[q], m);
         }
         __syncthreads();
         fft_smem<T, -SIGN, MIXED>(buf, a, lines);
@@ -364,17 +427,31 @@ __global__ void __launch_bounds__(kFftThreads) fft_line_kernel(const __grid_cons
     // ---- store ----
     const int nstore = lines * a.out_count;
     const bool line_fast_out = (a.out_es != 1);
-    for (int i = threadIdx.x; i < nstore; i += blockDim.x) {
-        int ll, kk;
-        if (line_fast_out) { ll = i % lines; kk = i / lines; }
-        else { ll = i / a.out_count; kk = i - ll * a.out_count; }
-        int src = (a.out_offset + kk + a.store_add) % a.out_mod;
-        if (src < 0) src += a.out_mod;
-        Cx val = c_mul(buf[ll * a.pitch + src], a.scale);
-        if (a.chirp_out) val = c_mul(val, a.chirp_out[src]);
-        const long long l = l0 + ll;
-        if (a.post) val = c_mul(val, a.post[l * a.post_ls + (long long)kk * a.post_es]);
-        out[l * a.out_ls + (long long)kk * a.out_es] = val;
+    for (int i0 = threadIdx.x; i0 < nstore; i0 += U * blockDim.x) {
+        Cx post[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = i0 + u * blockDim.x;
+            post[u] = make_c<T>(T(1), T(0));
+            if (a.post && i < nstore) {
+                int ll, kk;
+                store_coords(i, lines, line_fast_out, a.out_count, ll, kk);
+                post[u] = a.post[(long long)(l0 + ll) * a.post_ls + (long long)kk * a.post_es];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = i0 + u * blockDim.x;
+            if (i >= nstore) continue;
+            int ll, kk;
+            store_coords(i, lines, line_fast_out, a.out_count, ll, kk);
+            int src = soff + kk;
+            if (src >= a.out_mod) src -= a.out_mod;
+            Cx val = c_mul(buf[sidx(ll * a.pitch + src)], a.scale);
+            if (a.chirp_out) val = c_mul(val, a.chirp_out[src]);
+            if (a.post) val = c_mul(val, post[u]);
+            out[(long long)(l0 + ll) * a.out_ls + (long long)kk * a.out_es] = val;
+        }
     }
 }
 
