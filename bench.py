@@ -46,6 +46,7 @@ def parse_args():
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--cpu-seconds', type=float, default=10.0)
     p.add_argument('--grad-steps', type=int, default=20, help='timed DM-gradient steps (0: skip that leg)')
+    p.add_argument('--no-atmosphere', action='store_true', help='skip the atmospheric-layer leg')
     return p.parse_args()
 
 
@@ -238,6 +239,7 @@ def run_grad(args, dev):
         loss.backward()
         return loss, a.grad
 
+    hg.autotune(True)
     for _ in range(3):
         step()
     torch.cuda.synchronize()
@@ -286,6 +288,71 @@ def run_grad(args, dev):
     }
 
 
+def run_atmosphere(args, dev, peaks):
+    """Infinite atmospheric layer at the broadband workload's size: 1024^2 screen over 8 m, float32 device
+    matrices, wind 25 m/s, 1 ms frames (3.2 pixel steps per frame).  Times one extrusion (the A . stencil +
+    B . noise update) and one quintic shift with CUDA events; the extrusion streams A and B from HBM."""
+    import torch
+    import hcipy_gb300 as hg
+    from hcipy_gb300 import _lib
+    pupil = hg.make_pupil_grid(1024, 8.0)
+    t0 = time.perf_counter()
+    layer = hg.InfiniteAtmosphericLayer(pupil, hg.Cn_squared_from_fried_parameter(0.1, 500e-9), L0=25,
+                                        velocity=25.0, seed=5, dtype=torch.float32)
+    init_s = time.perf_counter() - t0
+    noise = torch.randn(64, layer.B_horizontal.shape[1], device=dev)
+    for i in range(4):
+        layer._extrude('right', noise[i])
+    taps = np.array([0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0])
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = 60
+    e0.record()
+    for i in range(n):
+        layer._extrude('right', noise[i % 64])
+    e1.record()
+    e1.synchronize()
+    ext_us = e0.elapsed_time(e1) / n * 1e3
+    e0.record()
+    for i in range(n):
+        layer._shift(taps, taps)
+    e1.record()
+    e1.synchronize()
+    shift_us = e0.elapsed_time(e1) / n * 1e3
+    ab_bytes = 4 * (layer.A_horizontal.size + layer.B_horizontal.size)
+    hbm = peaks.get('hbm_gbs', 6800.0)
+    frames = 20
+    t_frame0 = torch.cuda.Event(enable_timing=True)
+    t_frame1 = torch.cuda.Event(enable_timing=True)
+    t_frame0.record()
+    for f in range(frames):
+        layer.evolve_until((f + 1) * 1e-3)
+    t_frame1.record()
+    t_frame1.synchronize()
+    from oracle import atmosphere as oatm
+    screen = layer.achromatic_screen.data.double().cpu().numpy()
+    rng = np.random.default_rng(0)
+    cpu_n, c0 = 0, time.perf_counter()
+    while cpu_n < 3 or time.perf_counter() - c0 < 2.0:
+        screen = oatm.extrude(screen, (1024, 1024), 'right', layer.A_horizontal, layer.B_horizontal,
+                              layer.stencil_left_idx, rng.standard_normal(layer.B_horizontal.shape[1]))
+        cpu_n += 1
+    cpu_ms = (time.perf_counter() - c0) / cpu_n * 1e3
+    return {
+        'layer': '1024^2 over 8 m, L0 25 m, v 25 m/s, float32 screen and A/B; init %.1f s on the host' % init_s,
+        'extrusion_us': ext_us, 'extrusion_GBps': ab_bytes / (ext_us * 1e-6) / 1e9,
+        'extrusion_frac_of_hbm': ab_bytes / (ext_us * 1e-6) / 1e9 / hbm,
+        'extrusion_bytes': int(ab_bytes), 'shift_us': shift_us,
+        'shift_GBps': 2 * 4 * pupil.size / (shift_us * 1e-6) / 1e9,
+        'frame_ms': t_frame0.elapsed_time(t_frame1) / frames,
+        'frame': 'evolve_until for a 1 ms step: 3-4 extrusions (noise drawn on the host) and one shift',
+        'cpu_baseline_ms_per_extrusion': cpu_ms,
+        'cpu_baseline': 'oracle extrusion (the reference algorithm: float64 GEMV + screen copy in numpy), %d steps '
+                        'on the host' % cpu_n,
+        'peak_note': 'hbm_gbs of measured' if 'hbm_gbs' in peaks else 'fallback',
+    }
+
+
 def run_ours(args, rank, world, dist):
     import torch
     import hcipy_gb300 as hg
@@ -307,6 +374,7 @@ def run_ours(args, rank, world, dist):
         return prop.forward(lyot.forward(wf)).electric_field.data
 
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    hg.autotune(True)  # the warm-up measures the tile candidates of each GEMM shape once
     for _ in range(max(args.warmup, 3)):
         img = step(e_dev)
     torch.cuda.synchronize()
@@ -424,6 +492,7 @@ def run_ours(args, rank, world, dist):
         'config': {'workload': 'lyot-coronagraph 2048^2 pupil -> 512^2 FPM grid -> 512^2 image (3 MFTs)',
                    'pupil': args.pupil, 'fpm_grid': int(fpm_grid.dims[0]), 'image': int(focal.dims[0]),
                    'batch': 1, 'precision': args.precision, 'field_dtype': 'complex64',
+                   'tiles': 'autotuned during the warm-up (hx_autotune)',
                    'l2': 'flushed between steps (256 MiB write outside the per-step events)',
                    'parallelism': 'replicas' if world > 1 else 'single-gpu'},
         'roofline': {'bound': bound, 'achieved': achieved_tflops, 'peak': peak, 'unit': 'TFLOP/s',
@@ -445,6 +514,8 @@ def run_ours(args, rank, world, dist):
         line['cpu_baseline'] = cpu
     if args.grad_steps > 0:
         line['grad_steps'] = run_grad(args, dev)
+    if not args.no_atmosphere:
+        line['atmosphere'] = run_atmosphere(args, dev, peaks)
     print(json.dumps(line), flush=True)
 
 

@@ -17,7 +17,8 @@ from .deformable_mirror import (ModeBasis, DeformableMirror, make_actuator_posit
                                 make_gaussian_influence_functions, find_illuminated_actuators)
 from .atmosphere import (AtmosphericLayer, InfiniteAtmosphericLayer, MultiLayerAtmosphere,
                          Cn_squared_from_fried_parameter, fried_parameter_from_Cn_squared, subpixel_shift)
-from ._lib import HXError, launch_count
+from .broadband import BroadbandImager, diffraction_scaled_focal_grids
+from ._lib import HXError, launch_count, autotune
 
 __all__ = [
     'Field', 'CartesianGrid', 'RegularCoords', 'SeparatedCoords', 'UnstructuredCoords', 'make_uniform_grid',
@@ -31,4 +32,5 @@ __all__ = [
     'ModeBasis', 'DeformableMirror', 'make_actuator_positions', 'make_gaussian_influence_functions',
     'find_illuminated_actuators', 'AtmosphericLayer', 'InfiniteAtmosphericLayer', 'MultiLayerAtmosphere',
     'Cn_squared_from_fried_parameter', 'fried_parameter_from_Cn_squared', 'subpixel_shift',
+    'BroadbandImager', 'diffraction_scaled_focal_grids', 'autotune',
 ]

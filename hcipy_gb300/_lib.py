@@ -49,6 +49,9 @@ SIGNATURES = {
     'hx_version': (c_int, []),
     'hx_launch_count': (c_ll, []),
     'hx_trace_enable': (c_int, [c_int]),
+    'hx_autotune': (c_int, [c_int]),
+    'hx_autotune_entries': (c_int, []),
+    'hx_autotune_clear': (c_int, []),
     'hx_influence_apply': (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p,
                                    c_void_p]),
     'hx_influence_apply_transpose': (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p,
@@ -201,6 +204,15 @@ def dtype_code(dt):
 
 def launch_count():
     return int(load().hx_launch_count())
+
+
+def autotune(on=True):
+    """Measure the split-GEMM tile candidates of each new GEMM shape once and keep the fastest."""
+    check(lib().hx_autotune(1 if on else 0), 'hx_autotune')
+
+
+def autotune_entries():
+    return int(lib().hx_autotune_entries())
 
 
 def trace_enable(on=True):

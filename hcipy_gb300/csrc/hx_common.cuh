@@ -30,8 +30,8 @@ void trace_end(int record, cudaStream_t stream);
 struct TraceScope {
     int record = -1;
     cudaStream_t stream;
-    TraceScope(int kind, double work, cudaStream_t st) : stream(st) {
-        if (trace_on()) record = trace_begin(kind, work, st);
+    TraceScope(int kind, double work, cudaStream_t st, bool enabled = true) : stream(st) {
+        if (enabled && trace_on()) record = trace_begin(kind, work, st);
     }
     ~TraceScope() {
         if (record >= 0) trace_end(record, stream);

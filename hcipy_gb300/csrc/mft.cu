@@ -317,4 +317,16 @@ int hx_mft_plan_destroy(hx_mft_plan* p) {
     return HX_OK;
 }
 
+int hx_autotune(int on) {
+    hx::split_autotune(on);
+    return HX_OK;
+}
+
+int hx_autotune_entries(void) { return hx::split_autotune_entries(); }
+
+int hx_autotune_clear(void) {
+    hx::split_autotune_clear();
+    return HX_OK;
+}
+
 }  // extern "C"

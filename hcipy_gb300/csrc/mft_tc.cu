@@ -48,7 +48,11 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <atomic>
+#include <map>
 #include <mutex>
+#include <tuple>
+#include <vector>
 
 namespace hx {
 namespace {
@@ -890,31 +894,74 @@ struct TileChoice {
     size_t partial_floats() const { return ksplit > 1 ? (size_t)tiles * ksplit * 2 * bn * BM : 0; }
 };
 
-// BN = 128 halves the A traffic per product against BN = 64 and is taken when its tiles fill at least 3/4 of
-// the SMs.  Smaller GEMMs take BN = 64 and split K so that the grid fills the GPU (at least four K-steps per
-// CTA): more CTAs share the epilogue and the last CTA of a tile reads fewer partial bytes.
-// HX_SPLIT_TILE="bn[,ksplit]" overrides the choice (tuning).
-TileChoice choose_tile(long long m_tiles, int N, int grid_z, int ktiles) {
+void forced_tiles(int* bn, int* ks) {
     static int forced_bn = 0, forced_split = 0;
     static std::once_flag once;
     std::call_once(once, [] {
         const char* e = getenv("HX_SPLIT_TILE");
-        int bn = 0, ks = 0;
-        const int n = e ? sscanf(e, "%d,%d", &bn, &ks) : 0;
-        if (n >= 1 && (bn == 64 || bn == 128)) forced_bn = bn;
-        if (n == 2 && ks >= 1) forced_split = ks;
+        int b = 0, k = 0;
+        const int n = e ? sscanf(e, "%d,%d", &b, &k) : 0;
+        if (n >= 1 && (b == 64 || b == 128)) forced_bn = b;
+        if (n == 2 && k >= 1) forced_split = k;
     });
+    *bn = forced_bn;
+    *ks = forced_split;
+}
+
+TileChoice make_choice(long long m_tiles, int N, int grid_z, int ktiles, int bn, int ksplit) {
     TileChoice c;
-    const int sms = sm_count();
-    const long long tiles128 = m_tiles * (long long)ceil_div(N, 128) * grid_z;
-    c.bn = forced_bn ? forced_bn : (N > 64 && 4 * tiles128 >= 3LL * sms ? 128 : 64);
-    c.n_tiles = (int)ceil_div(N, c.bn);
+    c.bn = bn;
+    c.n_tiles = (int)ceil_div(N, bn);
     c.tiles = m_tiles * c.n_tiles * grid_z;
-    if (forced_split) c.ksplit = forced_split;
-    else if (c.tiles < sms) c.ksplit = (int)(sms / c.tiles);
-    c.ksplit = std::max(1, std::min(c.ksplit, std::max(1, ktiles / 4)));
+    c.ksplit = std::max(1, std::min(ksplit, std::max(1, ktiles / 4)));
     return c;
 }
+
+// K split that fills the GPU with a given tile count.
+int fill_split(long long tiles, int sms) { return tiles < sms ? (int)(sms / tiles) : 1; }
+
+// Candidate tiles of one GEMM: BN 128 and 64, each unsplit and split to fill the GPU.
+std::vector<TileChoice> tile_candidates(long long m_tiles, int N, int grid_z, int ktiles) {
+    std::vector<TileChoice> v;
+    const int sms = sm_count();
+    for (int bn : {128, 64}) {
+        if (bn == 128 && N <= 64) continue;
+        const TileChoice c1 = make_choice(m_tiles, N, grid_z, ktiles, bn, 1);
+        v.push_back(c1);
+        const TileChoice c2 = make_choice(m_tiles, N, grid_z, ktiles, bn, fill_split(c1.tiles, sms));
+        if (c2.ksplit > 1) v.push_back(c2);
+    }
+    return v;
+}
+
+// BN = 128 halves the A traffic per product against BN = 64 and is taken when its tiles fill at least 3/4 of
+// the SMs.  Smaller GEMMs take BN = 64 and split K so that the grid fills the GPU (at least four K-steps per
+// CTA): more CTAs share the epilogue and the last CTA of a tile reads fewer partial bytes.
+// HX_SPLIT_TILE="bn[,ksplit]" overrides the choice (tuning); with the autotuner on, a measured choice for the
+// same GEMM shape takes precedence (see launch_gemm).
+TileChoice choose_tile(long long m_tiles, int N, int grid_z, int ktiles) {
+    int fbn, fks;
+    forced_tiles(&fbn, &fks);
+    const int sms = sm_count();
+    const long long tiles128 = m_tiles * (long long)ceil_div(N, 128) * grid_z;
+    const int bn = fbn ? fbn : (N > 64 && 4 * tiles128 >= 3LL * sms ? 128 : 64);
+    const long long tiles = m_tiles * (long long)ceil_div(N, bn) * grid_z;
+    return make_choice(m_tiles, N, grid_z, ktiles, bn, fks ? fks : fill_split(tiles, sms));
+}
+
+// ---- autotuner: the fastest candidate per GEMM shape, measured once on the caller's stream -------------
+
+struct GemmShape {
+    long long m_tiles;
+    int N, grid_z, ktiles, sms, dev;
+    bool operator<(const GemmShape& o) const {
+        return std::tie(m_tiles, N, grid_z, ktiles, sms, dev) < std::tie(o.m_tiles, o.N, o.grid_z, o.ktiles, o.sms, o.dev);
+    }
+};
+
+std::atomic<int> g_autotune{0};
+std::mutex g_tune_mu;
+std::map<GemmShape, TileChoice> g_tuned;
 
 template <int BN, int OUT, int SRC> int launch_tile(const GemmArgs& g, dim3 grid, cudaStream_t st) {
     static bool configured[64];
@@ -949,13 +996,9 @@ template <int BN> int launch_out(const GemmArgs& g, dim3 grid, int out, int src,
     }
 }
 
-// partial / counters: workspace for a split-K choice (unused when c.ksplit == 1).
-int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, const TileChoice& c, int grid_z,
-                float* partial, unsigned int* counters, double cmacs, cudaStream_t st) {
-    if (A.kpitch != B.kpitch) {
-        set_error("internal: split GEMM K mismatch (%d vs %d)", A.kpitch, B.kpitch);
-        return HX_ERR_INVALID;
-    }
+// One launch with a given tile choice.  partial / counters: split-K workspace (unused when c.ksplit == 1).
+int launch_choice(GemmArgs& g, const SliceMat& A, const SliceMat& B, const TileChoice& c, int grid_z,
+                  float* partial, unsigned int* counters, double cmacs, bool traced, cudaStream_t st) {
     const long long m_tiles = A.rows / BM;
     if (m_tiles > 65535 || grid_z > 65535 || (long long)c.n_tiles * c.ksplit > 2147483647LL) {
         set_error("split GEMM grid too large");
@@ -973,8 +1016,72 @@ int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, const TileCho
     dim3 grid((unsigned)(c.n_tiles * c.ksplit), (unsigned)m_tiles, grid_z);
     const int out = output_fmt(g.out);
     const int src = g.epi == HX_EPI_BABINET ? input_fmt(g.src) : FMT_NONE;
-    TraceScope trace(HX_TRACE_SPLIT_GEMM, cmacs, st);
+    TraceScope trace(HX_TRACE_SPLIT_GEMM, cmacs, st, traced);
     return c.bn == 64 ? launch_out<64>(g, grid, out, src, st) : launch_out<128>(g, grid, out, src, st);
+}
+
+// Times every candidate (one warm-up launch, then one timed launch each) with CUDA events on the stream and
+// keeps the fastest.  The launches write the same result each time (the epilogue maxima are idempotent).
+int tune(GemmArgs& g, const SliceMat& A, const SliceMat& B, const GemmShape& key, int grid_z, float* partial,
+         unsigned int* counters, cudaStream_t st, TileChoice* best) {
+    const std::vector<TileChoice> cands = tile_candidates(key.m_tiles, key.N, key.grid_z, key.ktiles);
+    cudaEvent_t e0, e1;
+    HX_TRY(cuda_status(cudaEventCreate(&e0), "autotune event"));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        set_error("autotune event");
+        return HX_ERR_CUDA;
+    }
+    float best_ms = 1e30f;
+    int rc = HX_OK;
+    for (const TileChoice& c : cands) {
+        if ((rc = launch_choice(g, A, B, c, grid_z, partial, counters, 0.0, false, st)) != HX_OK) break;
+        cudaEventRecord(e0, st);
+        if ((rc = launch_choice(g, A, B, c, grid_z, partial, counters, 0.0, false, st)) != HX_OK) break;
+        cudaEventRecord(e1, st);
+        if ((rc = cuda_status(cudaEventSynchronize(e1), "autotune sync")) != HX_OK) break;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_ms) {
+            best_ms = ms;
+            *best = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != HX_OK) return rc;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tuned[key] = *best;
+    return HX_OK;
+}
+
+// partial / counters are sized for every candidate (carve_ws), so the autotuner may pick any of them.
+int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, TileChoice c, int grid_z, float* partial,
+                unsigned int* counters, double cmacs, cudaStream_t st) {
+    if (A.kpitch != B.kpitch) {
+        set_error("internal: split GEMM K mismatch (%d vs %d)", A.kpitch, B.kpitch);
+        return HX_ERR_INVALID;
+    }
+    int fbn, fks;
+    forced_tiles(&fbn, &fks);
+    if (g_autotune.load(std::memory_order_relaxed) && !fbn && !fks) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        const GemmShape key{A.rows / BM, g.N, grid_z, A.kpitch / BK, sm_count(), dev};
+        bool found = false;
+        {
+            std::lock_guard<std::mutex> lock(g_tune_mu);
+            auto it = g_tuned.find(key);
+            if (it != g_tuned.end()) {
+                c = it->second;
+                found = true;
+            }
+        }
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(st, &cap);
+        if (!found && cap == cudaStreamCaptureStatusNone) HX_TRY(tune(g, A, B, key, grid_z, partial, counters, st, &c));
+    }
+    return launch_choice(g, A, B, c, grid_z, partial, counters, cmacs, true, st);
 }
 
 GemmArgs base_args(int* status) {
@@ -1046,6 +1153,8 @@ struct Ws {
 };
 
 void carve_ws(Carver& c, const SplitMftPlan* p, int direction, int batch, Ws& w) {
+    long long g1_rows, g2_rows;
+    int g1_n, g1_z, g1_kt, g2_n, g2_z, g2_kt;
     const long long rows = (long long)batch * p->ny;
     const long long nu64 = round_up(p->nu, 64);
     const long long b_rows = round_up(batch * nu64, 128);
@@ -1054,19 +1163,34 @@ void carve_ws(Carver& c, const SplitMftPlan* p, int direction, int batch, Ws& w)
         w.t = carve_ff(c, rows * p->nu);
         w.t_max = (unsigned int*)c.take(sizeof(unsigned int) * batch * nu64);
         carve_slices(c, w.s2, b_rows, p->ny, b_rows);
-        w.c1 = choose_tile(w.s1.rows / BM, p->nu, 1, w.s1.kpitch / BK);
-        w.c2 = choose_tile(p->m1f.rows / BM, p->nu, batch, p->m1f.kpitch / BK);
+        g1_rows = w.s1.rows, g1_n = p->nu, g1_z = 1, g1_kt = w.s1.kpitch / BK;
+        g2_rows = p->m1f.rows, g2_n = p->nu, g2_z = batch, g2_kt = p->m1f.kpitch / BK;
     } else {
         w.in_max = (unsigned int*)c.take(sizeof(unsigned int) * batch * nu64);
         carve_slices(c, w.s1, b_rows, p->nv, b_rows);
         w.t = carve_ff(c, rows * p->nu);
         w.t_max = (unsigned int*)c.take(sizeof(unsigned int) * rows);
         carve_slices(c, w.s2, 2 * round_up(rows, 64), p->nu, rows);
-        w.c1 = choose_tile(p->m1b.rows / BM, p->nu, batch, p->m1b.kpitch / BK);
-        w.c2 = choose_tile(w.s2.rows / BM, p->nx, 1, w.s2.kpitch / BK);
+        g1_rows = p->m1b.rows, g1_n = p->nu, g1_z = batch, g1_kt = p->m1b.kpitch / BK;
+        g2_rows = w.s2.rows, g2_n = p->nx, g2_z = 1, g2_kt = w.s2.kpitch / BK;
     }
-    w.partial = (float*)c.take(sizeof(float) * std::max(w.c1.partial_floats(), w.c2.partial_floats()));
-    w.counters = (unsigned int*)c.take(sizeof(unsigned int) * std::max(w.c1.tiles, w.c2.tiles));
+    w.c1 = choose_tile(g1_rows / BM, g1_n, g1_z, g1_kt);
+    w.c2 = choose_tile(g2_rows / BM, g2_n, g2_z, g2_kt);
+    // split-K workspace for every candidate tile of both GEMMs, so the layout does not depend on the choice
+    size_t part = 0;
+    long long tiles = 0;
+    for (const TileChoice* t : {&w.c1, &w.c2}) {
+        const long long m_tiles = t == &w.c1 ? g1_rows / BM : g2_rows / BM;
+        for (const TileChoice& cand : tile_candidates(m_tiles, t == &w.c1 ? g1_n : g2_n, t == &w.c1 ? g1_z : g2_z,
+                                                      t == &w.c1 ? g1_kt : g2_kt)) {
+            part = std::max(part, cand.partial_floats());
+            tiles = std::max(tiles, cand.tiles);
+        }
+        part = std::max(part, t->partial_floats());
+        tiles = std::max(tiles, t->tiles);
+    }
+    w.partial = (float*)c.take(sizeof(float) * part);
+    w.counters = (unsigned int*)c.take(sizeof(unsigned int) * tiles);
 }
 
 // in/out: c64 or float-float fields.  in_max: optional precomputed maxima of the input in the orientation the
@@ -1309,6 +1433,18 @@ int split_mft_status(const SplitMftPlan* p, int reset) {
     if (reset && h != 0) cudaMemset(p->status, 0, sizeof(int));
     if (h != 0) set_error("a bounded wait in the split tensor-core GEMM gave up");
     return h;
+}
+
+void split_autotune(int on) { g_autotune.store(on ? 1 : 0, std::memory_order_relaxed); }
+
+int split_autotune_entries() {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    return (int)g_tuned.size();
+}
+
+void split_autotune_clear() {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tuned.clear();
 }
 
 void split_mft_destroy(SplitMftPlan* p) {

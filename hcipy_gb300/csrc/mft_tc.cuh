@@ -27,5 +27,9 @@ int split_lyot_execute(const SplitMftPlan* fpm, const SplitMftPlan* img, int bat
 // Status word of the bounded device waits (HX_OK or HX_ERR_TIMEOUT); synchronizes with the device.
 int split_mft_status(const SplitMftPlan* p, int reset);
 void split_mft_destroy(SplitMftPlan* p);
+// Autotuner of the split GEMM tiles (process-wide): on/off, number of measured shapes, forget them.
+void split_autotune(int on);
+int split_autotune_entries();
+void split_autotune_clear();
 
 }  // namespace hx

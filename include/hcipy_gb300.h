@@ -164,6 +164,15 @@ HX_API int hx_lyot_execute(const hx_mft_plan* fpm_plan, const hx_mft_plan* img_p
  * returned without writing).  Synchronizes with the device; reset != 0 clears it. */
 HX_API int hx_mft_plan_status(const hx_mft_plan* plan, int reset);
 
+/* Tile autotuner of the split tensor-core GEMMs (process-wide; no counterpart in the reference).  When on,
+ * the first execution of each GEMM shape times every candidate tile (64 or 128 output columns, with and
+ * without a split of K) with CUDA events on the caller's stream, synchronizes, and keeps the fastest for
+ * later executions of that shape; executions inside CUDA-graph capture use the kept or default tiles and
+ * never measure.  Workspace sizes do not depend on it. */
+HX_API int hx_autotune(int on);
+HX_API int hx_autotune_entries(void);
+HX_API int hx_autotune_clear(void);
+
 /* No counterpart in the reference.  The same transform as hx_mft_execute for
  * callers that cannot allocate device memory while they run (a real-time loop
  * that must not stall on an allocator, a host framework or plugin ABI that hands

@@ -106,3 +106,23 @@ def test_layer_forward_backward_and_multilayer():
     assert rel_err(back, e) < 1e-12
     with pytest.raises(ValueError):
         l1.evolve_until(0.01)
+
+
+def test_layer_full_size_extrusion_matches_oracle():
+    """A 1024^2 layer (the broadband workload's size): four extrusions in float64 against the oracle's array
+    copies with the layer's own matrices and noise."""
+    from oracle import atmosphere as oatm
+    pupil = hg.make_pupil_grid(1024, 8.0)
+    layer = hg.InfiniteAtmosphericLayer(pupil, hg.Cn_squared_from_fried_parameter(0.1, 500e-9), L0=25,
+                                        velocity=25.0, seed=5)
+    screen = layer.achromatic_screen.numpy()
+    rng = np.random.default_rng(3)
+    for where in ('right', 'right', 'top', 'left'):
+        vertical = where in ('top', 'bottom')
+        a = layer.A_vertical if vertical else layer.A_horizontal
+        b = layer.B_vertical if vertical else layer.B_horizontal
+        idx = layer.stencil_bottom_idx if vertical else layer.stencil_left_idx
+        noise = rng.standard_normal(b.shape[1]) * np.sqrt(layer.Cn_squared)
+        screen = oatm.extrude(screen, (1024, 1024), where, a, b, idx, noise)
+        layer._extrude(where, torch.from_numpy(noise).cuda())
+    assert rel_err(layer.achromatic_screen.numpy(), screen) < 1e-12

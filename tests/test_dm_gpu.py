@@ -205,3 +205,42 @@ def _loss_plain(setup, dm, a, aperture, roi, wl):
     e = dm.forward(hg.Wavefront(hg.Field(torch.from_numpy(aperture).cuda(), pupil), wl))
     img = prop.forward(lyot.forward(e)).electric_field.data
     return ((img.real**2 + img.imag**2) * roi).sum().item()
+
+
+@pytest.mark.parametrize('precision', ['fp32', 'split'])
+def test_gradient_matches_oracle_poke_jacobian(precision):
+    """The device adjoint gradient against a Jacobian built by poking actuators in the float64 oracle chain
+    (central differences of the reference algorithm's loss, one actuator at a time): within 1e-6 relative."""
+    pupil, fpm_grid, focal, fpm, stop, lyot, prop = _lyot_setup(n=48, precision=precision)
+    inf = hg.make_gaussian_influence_functions(pupil, 6, 1 / 6, crosstalk=0.15)
+    m = inf.transformation_matrix.toarray()
+    from hcipy_gb300 import workloads
+    aperture = workloads.circular_aperture(pupil, 1.0).astype(np.complex128)
+    roi = _roi(focal, 2.0, 8.0)
+    rng = np.random.default_rng(8)
+    a0 = rng.standard_normal(inf.num_modes) * 2e-3
+    dm = hg.DeformableMirror(inf, dtype=torch.float64)
+    a = torch.from_numpy(a0).cuda().requires_grad_(True)
+    dm.actuators = a
+    e = dm.forward(hg.Wavefront(hg.Field(torch.from_numpy(aperture).cuda(), pupil), 1.0))
+    img = prop.forward(lyot.forward(e)).electric_field.data
+    loss = ((img.real**2 + img.imag**2) * torch.from_numpy(roi.astype(np.float64)).cuda()).sum()
+    loss.backward()
+    grad = a.grad.cpu().numpy()
+
+    chain = ooptics.LyotChain(RegularGrid(pupil.delta, pupil.dims, pupil.zero),
+                              RegularGrid(fpm_grid.delta, fpm_grid.dims, fpm_grid.zero),
+                              RegularGrid(focal.delta, focal.dims, focal.zero), fpm, stop)
+
+    def oracle_loss(act):
+        img = chain(aperture * np.exp(2j * 2 * np.pi * (m @ act)))
+        return np.sum(np.abs(img)**2 * roi)
+
+    h = 1e-7
+    jac = np.empty(inf.num_modes)
+    for i in range(inf.num_modes):
+        ap, am = a0.copy(), a0.copy()
+        ap[i] += h
+        am[i] -= h
+        jac[i] = (oracle_loss(ap) - oracle_loss(am)) / (2 * h)
+    assert np.linalg.norm(grad - jac) < 1e-6 * np.linalg.norm(jac), np.linalg.norm(grad - jac) / np.linalg.norm(jac)
