@@ -305,20 +305,24 @@ def run_atmosphere(args, dev, peaks):
         layer._extrude('right', noise[i])
     taps = np.array([0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0])
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # kernel times: CUDA events around each launch on its stream (the Python calls between launches are not
+    # counted, so a launch-bound loop does not hide the kernel's own time)
     n = 60
-    e0.record()
+    _lib.trace_read(_lib.HX_TRACE_ATMOSPHERE, reset=True)
+    _lib.trace_enable(True)
     for i in range(n):
         layer._extrude('right', noise[i % 64])
-    e1.record()
-    e1.synchronize()
-    ext_us = e0.elapsed_time(e1) / n * 1e3
-    e0.record()
+    torch.cuda.synchronize()
+    _lib.trace_enable(False)
+    k, ms, _ = _lib.trace_read(_lib.HX_TRACE_ATMOSPHERE, reset=True)
+    ext_us = ms / max(k, 1) * 1e3
+    _lib.trace_enable(True)
     for i in range(n):
         layer._shift(taps, taps)
-    e1.record()
-    e1.synchronize()
-    shift_us = e0.elapsed_time(e1) / n * 1e3
+    torch.cuda.synchronize()
+    _lib.trace_enable(False)
+    k, ms, _ = _lib.trace_read(_lib.HX_TRACE_ATMOSPHERE, reset=True)
+    shift_us = ms / max(k, 1) * 1e3
     ab_bytes = 4 * (layer.A_horizontal.size + layer.B_horizontal.size)
     hbm = peaks.get('hbm_gbs', 6800.0)
     frames = 20
@@ -345,7 +349,9 @@ def run_atmosphere(args, dev, peaks):
         'extrusion_bytes': int(ab_bytes), 'shift_us': shift_us,
         'shift_GBps': 2 * 4 * pupil.size / (shift_us * 1e-6) / 1e9,
         'frame_ms': t_frame0.elapsed_time(t_frame1) / frames,
-        'frame': 'evolve_until for a 1 ms step: 3-4 extrusions (noise drawn on the host) and one shift',
+        'frame': 'evolve_until for a 1 ms step: 3-4 extrusions (noise drawn on the host) and one shift, wall '
+                 'time on the GPU including the host calls between launches',
+        'kernel_timing': 'CUDA events around each extrusion / shift launch (hx_trace_enable)',
         'cpu_baseline_ms_per_extrusion': cpu_ms,
         'cpu_baseline': 'oracle extrusion (the reference algorithm: float64 GEMV + screen copy in numpy), %d steps '
                         'on the host' % cpu_n,
@@ -512,6 +518,8 @@ def run_ours(args, rank, world, dist):
     }
     if cpu is not None:
         line['cpu_baseline'] = cpu
+    line['config']['autotuned_tiles'] = [
+        {'shape': list(shape), 'best': list(c[0]), 'candidates': len(c)} for shape, c in hg._lib.autotune_table()]
     if args.grad_steps > 0:
         line['grad_steps'] = run_grad(args, dev)
     if not args.no_atmosphere:

@@ -35,6 +35,8 @@ HX_EPI_BABINET = 2
 HX_TRACE_SPLIT_GEMM = 0
 HX_TRACE_SIMT_GEMM = 1
 HX_TRACE_FFT = 2
+HX_TRACE_ATMOSPHERE = 3
+HX_TRACE_DM = 4
 
 c_int = ctypes.c_int
 c_double = ctypes.c_double
@@ -51,6 +53,7 @@ SIGNATURES = {
     'hx_trace_enable': (c_int, [c_int]),
     'hx_autotune': (c_int, [c_int]),
     'hx_autotune_entries': (c_int, []),
+    'hx_autotune_entry': (c_int, [c_int, P(c_ll), P(c_int), P(c_int), P(c_int), P(ctypes.c_float)]),
     'hx_autotune_clear': (c_int, []),
     'hx_influence_apply': (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p,
                                    c_void_p]),
@@ -213,6 +216,20 @@ def autotune(on=True):
 
 def autotune_entries():
     return int(lib().hx_autotune_entries())
+
+
+def autotune_table():
+    """[(shape (row tiles, columns, z, K steps), [(bn, ksplit, ms), ...] best first)] of the autotuner."""
+    out = []
+    for i in range(autotune_entries()):
+        shape = (ctypes.c_longlong * 4)()
+        n = ctypes.c_int()
+        bn, ks = (ctypes.c_int * 8)(), (ctypes.c_int * 8)()
+        ms = (ctypes.c_float * 8)()
+        check(lib().hx_autotune_entry(i, shape, ctypes.byref(n), bn, ks, ms), 'hx_autotune_entry')
+        cands = sorted([(bn[k], ks[k], round(float(ms[k]), 4)) for k in range(n.value)], key=lambda c: c[2])
+        out.append((tuple(shape), cands))
+    return out
 
 
 def trace_enable(on=True):

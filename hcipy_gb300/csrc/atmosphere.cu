@@ -29,27 +29,57 @@ __global__ void gather_stencil_kernel(const T* ring, int ny, int nx, int row0, i
     if (k < nst) stencil[k] = ring[ring_index(stencil_idx[k], ny, nx, row0, col0, flip)];
 }
 
-// new_slice[r] = sum_k A[r, k] stencil[k] + sum_k B[r, k] noise[k], one warp per r, written into the ring slot
-// that the shift frees.  where: 0 bottom, 1 top, 2 left, 3 right; row0/col0 are the offsets before the step.
+// new_slice[r] = sum_k A[r, k] stencil[k] + sum_k B[r, k] noise[k], written into the ring slot that the shift
+// frees.  where: 0 bottom, 1 top, 2 left, 3 right; row0/col0 are the offsets before the step.  A CTA of 256
+// threads computes 2 rows with 4 warps per row, each warp a quarter of the stencil and of the noise, with
+// 16-byte loads when the rows allow them: A and B stream from HBM once per step, so the kernel is sized for
+// many requests in flight (512 CTAs for a 1024-pixel slice) and starts loading at once (no staging).
+constexpr int EXT_ROWS = 2;      // rows per CTA
+constexpr int EXT_WARPS_ROW = 4; // warps per row
+
+template <typename T>
+__device__ __forceinline__ T dot_part(const T* __restrict__ w, const T* __restrict__ x, int n, int part, int lane) {
+    // Elements [part * n / 4, (part + 1) * n / 4) of w . x, lanes strided; x (the stencil or the noise, a few
+    // KB shared by every CTA) is read through L1/L2 like w.
+    const int k0 = (int)((long long)n * part / EXT_WARPS_ROW);
+    const int k1 = (int)((long long)n * (part + 1) / EXT_WARPS_ROW);
+    T acc = T(0);
+    if (sizeof(T) == 4 && ((k0 & 3) == 0) && ((reinterpret_cast<size_t>(w + k0) & 15) == 0) &&
+        ((reinterpret_cast<size_t>(x + k0) & 15) == 0)) {
+        const int n4 = (k1 - k0) >> 2;
+        const float4* w4 = reinterpret_cast<const float4*>(w + k0);
+        const float4* x4 = reinterpret_cast<const float4*>(x + k0);
+#pragma unroll 4
+        for (int q = lane; q < n4; q += 32) {
+            const float4 a = __ldg(&w4[q]);
+            const float4 b = __ldg(&x4[q]);
+            acc += (T)(a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w);
+        }
+        for (int k = k0 + 4 * n4 + lane; k < k1; k += 32) acc += w[k] * x[k];
+    } else {
+#pragma unroll 4
+        for (int k = k0 + lane; k < k1; k += 32) acc += __ldg(&w[k]) * __ldg(&x[k]);
+    }
+    return acc;
+}
+
 template <typename T>
 __global__ void extrude_kernel(T* ring, int ny, int nx, int row0, int col0, int where, const T* stencil, int nst,
                                const T* A, const T* B, int nb, const T* noise, int nslice) {
-    extern __shared__ unsigned char smem_raw[];
-    T* st = reinterpret_cast<T*>(smem_raw);  // nst stencil values, then nb noise values
-    T* nz = st + nst;
-    for (int k = threadIdx.x; k < nst; k += blockDim.x) st[k] = stencil[k];
-    for (int k = threadIdx.x; k < nb; k += blockDim.x) nz[k] = noise[k];
-    __syncthreads();
+    __shared__ T part_sum[EXT_ROWS][EXT_WARPS_ROW];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int r = blockIdx.x * (blockDim.x >> 5) + warp;
-    if (r >= nslice) return;
+    const int rl = warp / EXT_WARPS_ROW, part = warp % EXT_WARPS_ROW;
+    const int r = blockIdx.x * EXT_ROWS + rl;
     T acc = T(0);
-    const T* a = A + (long long)r * nst;
-    for (int k = lane; k < nst; k += 32) acc += a[k] * st[k];
-    const T* b = B + (long long)r * nb;
-    for (int k = lane; k < nb; k += 32) acc += b[k] * nz[k];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane != 0) return;
+    if (r < nslice) {
+        acc = dot_part(A + (long long)r * nst, stencil, nst, part, lane) +
+              dot_part(B + (long long)r * nb, noise, nb, part, lane);
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    }
+    if (lane == 0) part_sum[rl][part] = acc;
+    __syncthreads();
+    if (part != 0 || lane != 0 || r >= nslice) return;
+    acc = part_sum[rl][0] + part_sum[rl][1] + part_sum[rl][2] + part_sum[rl][3];
     // Destination in logical coordinates after the shift: bottom -> row 0, top -> row ny-1 reversed,
     // left -> column 0, right -> column nx-1 reversed.
     int i, j;
@@ -80,7 +110,12 @@ template <typename T>
 __global__ void ring_shift_kernel(const T* ring, int ny, int nx, int row0, int col0, Taps taps, T* out) {
     __shared__ T in[TIN][TIN + 1];
     __shared__ T mid[TIN][TS + 1];
+    __shared__ T wr[7], wc[7];  // taps in the working type, converted once
     const int x0 = blockIdx.x * TS, y0 = blockIdx.y * TS;
+    if (threadIdx.y == 0 && threadIdx.x < 7) {
+        wr[threadIdx.x] = (T)taps.row[threadIdx.x];
+        wc[threadIdx.x] = (T)taps.col[threadIdx.x];
+    }
     for (int t = threadIdx.y * blockDim.x + threadIdx.x; t < TIN * TIN; t += blockDim.x * blockDim.y) {
         const int ly = t / TIN, lx = t % TIN;
         const int gy = min(max(y0 + ly - HALO, 0), ny - 1);
@@ -93,7 +128,7 @@ __global__ void ring_shift_kernel(const T* ring, int ny, int nx, int row0, int c
         const int ly = t / TS, x = t % TS;
         T s = T(0);
 #pragma unroll
-        for (int k = 0; k < 7; ++k) s += in[ly][x + k] * (T)taps.row[k];
+        for (int k = 0; k < 7; ++k) s += in[ly][x + k] * wr[k];
         mid[ly][x] = s;
     }
     __syncthreads();
@@ -102,7 +137,7 @@ __global__ void ring_shift_kernel(const T* ring, int ny, int nx, int row0, int c
         if (y0 + y >= ny || x0 + x >= nx) continue;
         T s = T(0);
 #pragma unroll
-        for (int k = 0; k < 7; ++k) s += mid[y + k][x] * (T)taps.col[k];
+        for (int k = 0; k < 7; ++k) s += mid[y + k][x] * wc[k];
         out[(long long)(y0 + y) * nx + x0 + x] = s;
     }
 }
@@ -120,22 +155,17 @@ int hx_atmosphere_extrude(void* ring, int ny, int nx, int row0, int col0, int wh
     HX_CHECK_ARG(row0 >= 0 && row0 < ny && col0 >= 0 && col0 < nx, "hx_atmosphere_extrude: ring offsets out of range");
     HX_CHECK_ARG(dtype == HX_F32 || dtype == HX_F64, "hx_atmosphere_extrude: dtype must be HX_F32 or HX_F64");
     const int nslice = (where <= 1) ? nx : ny;
-    const size_t esz = dtype == HX_F32 ? 4 : 8;
-    const size_t smem = esz * ((size_t)nst + nb);
-    HX_CHECK_ARG(smem <= 200 * 1024, "hx_atmosphere_extrude: stencil of %d plus %d noise values exceeds shared memory",
-                 nst, nb);
     if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
     cudaStream_t st = (cudaStream_t)stream;
     const bool flip = where == 1 || where == 3;
-    const int threads = 256, rows_per_cta = threads / 32;
-    dim3 grid(hx::ceil_div(nslice, rows_per_cta));
+    const int threads = 32 * EXT_ROWS * EXT_WARPS_ROW;
+    dim3 grid(hx::ceil_div(nslice, EXT_ROWS));
     if (dtype == HX_F32) {
         gather_stencil_kernel<float><<<hx::ceil_div(nst, 256), 256, 0, st>>>((const float*)ring, ny, nx, row0, col0,
                                                                              flip, stencil_idx, nst, (float*)work);
         HX_TRY(hx::launch_status("gather_stencil_kernel"));
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(extrude_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        extrude_kernel<float><<<grid, threads, smem, st>>>((float*)ring, ny, nx, row0, col0, where,
+        hx::TraceScope trace(HX_TRACE_ATMOSPHERE, 4.0 * ((double)nslice * (nst + nb) + nst + nb), st);
+        extrude_kernel<float><<<grid, threads, 0, st>>>((float*)ring, ny, nx, row0, col0, where,
                                                           (const float*)work, nst, (const float*)A, (const float*)B,
                                                           nb, (const float*)noise, nslice);
     } else {
@@ -143,9 +173,8 @@ int hx_atmosphere_extrude(void* ring, int ny, int nx, int row0, int col0, int wh
                                                                               col0, flip, stencil_idx, nst,
                                                                               (double*)work);
         HX_TRY(hx::launch_status("gather_stencil_kernel"));
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(extrude_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        extrude_kernel<double><<<grid, threads, smem, st>>>((double*)ring, ny, nx, row0, col0, where,
+        hx::TraceScope trace(HX_TRACE_ATMOSPHERE, 8.0 * ((double)nslice * (nst + nb) + nst + nb), st);
+        extrude_kernel<double><<<grid, threads, 0, st>>>((double*)ring, ny, nx, row0, col0, where,
                                                            (const double*)work, nst, (const double*)A,
                                                            (const double*)B, nb, (const double*)noise, nslice);
     }
@@ -167,6 +196,7 @@ int hx_atmosphere_shift(const void* ring, int ny, int nx, int row0, int col0, co
     dim3 grid(hx::ceil_div(nx, TS), hx::ceil_div(ny, TS));
     dim3 block(32, 8);
     cudaStream_t st = (cudaStream_t)stream;
+    hx::TraceScope trace(HX_TRACE_ATMOSPHERE, 2.0 * (dtype == HX_F32 ? 4 : 8) * (double)nx * ny, st);
     if (dtype == HX_F32)
         ring_shift_kernel<float><<<grid, block, 0, st>>>((const float*)ring, ny, nx, row0, col0, t, (float*)out);
     else

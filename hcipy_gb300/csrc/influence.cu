@@ -141,6 +141,8 @@ int hx_influence_apply(int npix, int nact, const int* row_ptr, const int* col_id
     if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
     dim3 grid(hx::ceil_div(npix, 256), hx::ceil_div(nvec, VC));
     cudaStream_t st = (cudaStream_t)stream;
+    const double esz = dtype == HX_F32 ? 4.0 : 8.0;
+    hx::TraceScope trace(HX_TRACE_DM, esz * ((double)nvec * (npix + nact)) + 4.0 * (npix + 1), st);
     if (dtype == HX_F32)
         influence_apply_kernel<float><<<grid, 256, 0, st>>>(npix, nact, row_ptr, col_idx, (const float*)vals, nvec,
                                                             (const float*)actuators, (float*)surface);
@@ -159,6 +161,8 @@ int hx_influence_apply_transpose(int npix, int nact, const int* col_ptr, const i
     if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
     dim3 grid(nact, hx::ceil_div(nvec, VC));
     cudaStream_t st = (cudaStream_t)stream;
+    const double esz = dtype == HX_F32 ? 4.0 : 8.0;
+    hx::TraceScope trace(HX_TRACE_DM, esz * ((double)nvec * (npix + nact)) + 4.0 * (nact + 1), st);
     if (dtype == HX_F32)
         influence_transpose_kernel<float><<<grid, 256, 0, st>>>(npix, nact, col_ptr, row_idx, (const float*)vals,
                                                                 nvec, (const float*)g_surface, (float*)g_actuators);
@@ -180,6 +184,8 @@ int hx_phase_apply(long long n, int batch, int batch_e, int batch_s, const void*
     if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
     dim3 grid(hx::ceil_div(n, 256), batch);
     cudaStream_t st = (cudaStream_t)stream;
+    const double csz = dtype == HX_C64 ? 8.0 : 16.0;
+    hx::TraceScope trace(HX_TRACE_DM, (double)n * (csz * (batch_e + batch) + csz / 2 * batch_s), st);
     if (dtype == HX_C64)
         phase_apply_kernel<float><<<grid, 256, 0, st>>>(n, batch, batch_e, batch_s, (const float2*)e, (const float*)s,
                                                         (float)scale, (float2*)out);

@@ -324,6 +324,13 @@ int hx_autotune(int on) {
 
 int hx_autotune_entries(void) { return hx::split_autotune_entries(); }
 
+int hx_autotune_entry(int i, long long* shape, int* n, int* bn, int* ksplit, float* ms) {
+    HX_CHECK_ARG(shape && n && bn && ksplit && ms, "hx_autotune_entry: NULL pointer");
+    const int rc = hx::split_autotune_entry(i, shape, n, bn, ksplit, ms);
+    if (rc != HX_OK) hx::set_error("hx_autotune_entry: no entry %d", i);
+    return rc;
+}
+
 int hx_autotune_clear(void) {
     hx::split_autotune_clear();
     return HX_OK;

@@ -70,12 +70,13 @@ constexpr int EXTRA_BYTES = 1024 + 1664;        // alignment slack, barriers, fl
 // Tile of BN output columns: four level accumulators of BN TMEM columns each, so BN = 128 takes all
 // 512 columns of the SM.  Stage count fills the shared memory.
 template <int BN> struct Tile {
+    static_assert(BN % 16 == 0 && 4 * BN <= 512, "four level accumulators of BN columns must fit TMEM");
     static constexpr int B_PLANE_BYTES = BN * BK * 2;
     static constexpr int STAGE_BYTES = A_STAGE_BYTES + NSLICE * B_PLANE_BYTES;
     static constexpr int STAGES = BN == 64 ? 3 : 2;
     static constexpr int PIPE_BYTES = STAGES * STAGE_BYTES;
     static constexpr int SMEM_BYTES = PIPE_BYTES + EXTRA_BYTES;
-    static constexpr int TMEM_COLS = 4 * BN;
+    static constexpr int TMEM_COLS = 4 * BN <= 256 ? 256 : 512;  // allocation: a power of two >= 4 BN
     static constexpr int PITCH = BN + 1;  // epilogue staging row pitch in floats (bank spread)
     static_assert((2 * BM + 64) * PITCH * 4 <= PIPE_BYTES, "epilogue staging must fit the pipeline buffers");
     static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
@@ -522,12 +523,16 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
             constexpr int RSTEP = EPI / BN;       // rows per iteration
             constexpr int ITER = 64 / RSTEP;
             constexpr int U = 4;                  // rows per batch: loads issued before any store
+            static_assert(64 % (RSTEP * U) == 0, "rows of a tile per batch");
+            // With BN not dividing the epilogue threads (BN = 112) the last EPI - RSTEP * BN threads have no
+            // column; they skip the loop so that no row beyond the tile's 64 is touched.
+            const bool has_col = et < RSTEP * BN;
             const int r0 = et / BN;
             const int mlim = g.M - m_tile * 64;   // valid rows of this tile
             int cfield = -1;
             float cmax = 0.0f;
 #pragma unroll 1
-            for (int i0 = 0; i0 < ITER; i0 += U) {
+            for (int i0 = 0; i0 < (has_col ? ITER : 0); i0 += U) {
                 cff e[U];
                 float2 mk[U];
 #pragma unroll
@@ -901,7 +906,7 @@ void forced_tiles(int* bn, int* ks) {
         const char* e = getenv("HX_SPLIT_TILE");
         int b = 0, k = 0;
         const int n = e ? sscanf(e, "%d,%d", &b, &k) : 0;
-        if (n >= 1 && (b == 64 || b == 128)) forced_bn = b;
+        if (n >= 1 && (b == 64 || b == 112 || b == 128)) forced_bn = b;
         if (n == 2 && k >= 1) forced_split = k;
     });
     *bn = forced_bn;
@@ -924,8 +929,8 @@ int fill_split(long long tiles, int sms) { return tiles < sms ? (int)(sms / tile
 std::vector<TileChoice> tile_candidates(long long m_tiles, int N, int grid_z, int ktiles) {
     std::vector<TileChoice> v;
     const int sms = sm_count();
-    for (int bn : {128, 64}) {
-        if (bn == 128 && N <= 64) continue;
+    for (int bn : {128, 112, 64}) {
+        if (bn > 64 && N <= 64) continue;
         const TileChoice c1 = make_choice(m_tiles, N, grid_z, ktiles, bn, 1);
         v.push_back(c1);
         const TileChoice c2 = make_choice(m_tiles, N, grid_z, ktiles, bn, fill_split(c1.tiles, sms));
@@ -959,9 +964,16 @@ struct GemmShape {
     }
 };
 
+struct TunedEntry {
+    TileChoice best;
+    int n = 0;                 // candidates measured
+    int bn[8], ksplit[8];
+    float ms[8];               // best of two timed launches each
+};
+
 std::atomic<int> g_autotune{0};
 std::mutex g_tune_mu;
-std::map<GemmShape, TileChoice> g_tuned;
+std::map<GemmShape, TunedEntry> g_tuned;
 
 template <int BN, int OUT, int SRC> int launch_tile(const GemmArgs& g, dim3 grid, cudaStream_t st) {
     static bool configured[64];
@@ -1017,41 +1029,56 @@ int launch_choice(GemmArgs& g, const SliceMat& A, const SliceMat& B, const TileC
     const int out = output_fmt(g.out);
     const int src = g.epi == HX_EPI_BABINET ? input_fmt(g.src) : FMT_NONE;
     TraceScope trace(HX_TRACE_SPLIT_GEMM, cmacs, st, traced);
-    return c.bn == 64 ? launch_out<64>(g, grid, out, src, st) : launch_out<128>(g, grid, out, src, st);
+    if (c.bn == 64) return launch_out<64>(g, grid, out, src, st);
+    if (c.bn == 112) return launch_out<112>(g, grid, out, src, st);
+    return launch_out<128>(g, grid, out, src, st);
 }
 
-// Times every candidate (one warm-up launch, then one timed launch each) with CUDA events on the stream and
-// keeps the fastest.  The launches write the same result each time (the epilogue maxima are idempotent).
+// Times every candidate (one warm-up launch, then the best of two timed launches) with CUDA events on the
+// stream and keeps the fastest.  The launches write the same result each time (the epilogue maxima are
+// idempotent).
 int tune(GemmArgs& g, const SliceMat& A, const SliceMat& B, const GemmShape& key, int grid_z, float* partial,
          unsigned int* counters, cudaStream_t st, TileChoice* best) {
     const std::vector<TileChoice> cands = tile_candidates(key.m_tiles, key.N, key.grid_z, key.ktiles);
-    cudaEvent_t e0, e1;
-    HX_TRY(cuda_status(cudaEventCreate(&e0), "autotune event"));
-    if (cudaEventCreate(&e1) != cudaSuccess) {
-        cudaEventDestroy(e0);
-        set_error("autotune event");
-        return HX_ERR_CUDA;
+    cudaEvent_t ev[3];
+    for (int i = 0; i < 3; ++i) {
+        if (cudaEventCreate(&ev[i]) != cudaSuccess) {
+            for (int j = 0; j < i; ++j) cudaEventDestroy(ev[j]);
+            set_error("autotune: cudaEventCreate failed");
+            return HX_ERR_CUDA;
+        }
     }
+    TunedEntry entry;
     float best_ms = 1e30f;
     int rc = HX_OK;
     for (const TileChoice& c : cands) {
         if ((rc = launch_choice(g, A, B, c, grid_z, partial, counters, 0.0, false, st)) != HX_OK) break;
-        cudaEventRecord(e0, st);
+        cudaEventRecord(ev[0], st);
         if ((rc = launch_choice(g, A, B, c, grid_z, partial, counters, 0.0, false, st)) != HX_OK) break;
-        cudaEventRecord(e1, st);
-        if ((rc = cuda_status(cudaEventSynchronize(e1), "autotune sync")) != HX_OK) break;
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventRecord(ev[1], st);
+        if ((rc = launch_choice(g, A, B, c, grid_z, partial, counters, 0.0, false, st)) != HX_OK) break;
+        cudaEventRecord(ev[2], st);
+        if ((rc = cuda_status(cudaEventSynchronize(ev[2]), "autotune sync")) != HX_OK) break;
+        float t1 = 0.0f, t2 = 0.0f;
+        cudaEventElapsedTime(&t1, ev[0], ev[1]);
+        cudaEventElapsedTime(&t2, ev[1], ev[2]);
+        const float ms = std::min(t1, t2);
+        if (entry.n < 8) {
+            entry.bn[entry.n] = c.bn;
+            entry.ksplit[entry.n] = c.ksplit;
+            entry.ms[entry.n] = ms;
+            ++entry.n;
+        }
         if (ms < best_ms) {
             best_ms = ms;
             *best = c;
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    for (int i = 0; i < 3; ++i) cudaEventDestroy(ev[i]);
     if (rc != HX_OK) return rc;
+    entry.best = *best;
     std::lock_guard<std::mutex> lock(g_tune_mu);
-    g_tuned[key] = *best;
+    g_tuned[key] = entry;
     return HX_OK;
 }
 
@@ -1073,7 +1100,7 @@ int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, TileChoice c,
             std::lock_guard<std::mutex> lock(g_tune_mu);
             auto it = g_tuned.find(key);
             if (it != g_tuned.end()) {
-                c = it->second;
+                c = it->second.best;
                 found = true;
             }
         }
@@ -1440,6 +1467,24 @@ void split_autotune(int on) { g_autotune.store(on ? 1 : 0, std::memory_order_rel
 int split_autotune_entries() {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     return (int)g_tuned.size();
+}
+
+int split_autotune_entry(int i, long long* shape, int* n, int* bn, int* ksplit, float* ms) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    if (i < 0 || i >= (int)g_tuned.size()) return HX_ERR_INVALID;
+    auto it = g_tuned.begin();
+    std::advance(it, i);
+    shape[0] = it->first.m_tiles;
+    shape[1] = it->first.N;
+    shape[2] = it->first.grid_z;
+    shape[3] = it->first.ktiles;
+    *n = it->second.n;
+    for (int k = 0; k < it->second.n; ++k) {
+        bn[k] = it->second.bn[k];
+        ksplit[k] = it->second.ksplit[k];
+        ms[k] = it->second.ms[k];
+    }
+    return HX_OK;
 }
 
 void split_autotune_clear() {

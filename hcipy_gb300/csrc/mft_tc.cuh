@@ -30,6 +30,8 @@ void split_mft_destroy(SplitMftPlan* p);
 // Autotuner of the split GEMM tiles (process-wide): on/off, number of measured shapes, forget them.
 void split_autotune(int on);
 int split_autotune_entries();
+// Entry i: shape {m_tiles, N, grid_z, ktiles}, n candidates with their tile width, K split and time (<= 8).
+int split_autotune_entry(int i, long long* shape, int* n, int* bn, int* ksplit, float* ms);
 void split_autotune_clear();
 
 }  // namespace hx

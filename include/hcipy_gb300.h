@@ -73,6 +73,8 @@ HX_API long long hx_launch_count(void);
 #define HX_TRACE_SPLIT_GEMM 0 /* split-operand tcgen05 GEMM of the MFT */
 #define HX_TRACE_SIMT_GEMM 1  /* CUDA-core complex GEMM of the MFT (FP32 or FP64) */
 #define HX_TRACE_FFT 2        /* line-FFT passes (FFT, filter, chirp-Z) */
+#define HX_TRACE_ATMOSPHERE 3 /* screen extrusion and sub-pixel shift (work = bytes) */
+#define HX_TRACE_DM 4         /* influence-function products and phase screens (work = bytes) */
 HX_API int hx_trace_enable(int on);
 HX_API int hx_trace_read(int kind, long long* launches, double* total_ms, double* total_work, int reset);
 
@@ -171,6 +173,9 @@ HX_API int hx_mft_plan_status(const hx_mft_plan* plan, int reset);
  * never measure.  Workspace sizes do not depend on it. */
 HX_API int hx_autotune(int on);
 HX_API int hx_autotune_entries(void);
+/* Entry i of the autotuner's table: shape[4] = {A row tiles, output columns, grid z, K steps}, and for each of the
+ * n (<= 8) candidates its tile width, K split and measured milliseconds (arrays of 8). */
+HX_API int hx_autotune_entry(int i, long long* shape, int* n, int* bn, int* ksplit, float* ms);
 HX_API int hx_autotune_clear(void);
 
 /* No counterpart in the reference.  The same transform as hx_mft_execute for

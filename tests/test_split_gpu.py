@@ -114,7 +114,7 @@ def test_split_lyot_dark_hole_512():
     assert errs['split'][0] < errs['fp32'][0] / 20, errs
 
 
-@pytest.mark.parametrize('tile', ['64,1', '128,1', '64,3', '128,4'])
+@pytest.mark.parametrize('tile', ['64,1', '128,1', '64,3', '128,4', '112,1', '112,2'])
 def test_split_tile_configurations(tile):
     """Both tile widths, with and without split K, against float64 (the heuristic picks one per GEMM)."""
     import os
