@@ -120,7 +120,10 @@ __global__ void ring_shift_kernel(const T* ring, int ny, int nx, int row0, int c
         const int ly = t / TIN, lx = t % TIN;
         const int gy = min(max(y0 + ly - HALO, 0), ny - 1);
         const int gx = min(max(x0 + lx - HALO, 0), nx - 1);
-        in[ly][lx] = ring[(long long)((gy + row0) % ny) * nx + (gx + col0) % nx];
+        int py = gy + row0, px = gx + col0;  // offsets are in [0, n): one subtraction wraps them
+        if (py >= ny) py -= ny;
+        if (px >= nx) px -= nx;
+        in[ly][lx] = ring[(long long)py * nx + px];
     }
     __syncthreads();
     // rows: mid[ly][x] = sum_k in[ly][x + k] * row[k]
