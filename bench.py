@@ -359,6 +359,16 @@ def run_atmosphere(args, dev, peaks):
     }
 
 
+def max_over_ranks(value, dist, device):
+    """The largest value over all ranks (a no-op without a process group): the whole job's time."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_ours(args, rank, world, dist):
     import torch
     import hcipy_gb300 as hg
@@ -413,11 +423,7 @@ def run_ours(args, rank, world, dist):
         dist.barrier()
     clocks = sampler.stop()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = sum(step_ms)
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(step_ms), dist, dev)
     value = world * args.steps / (total_ms * 1e-3)
     ms_per_step = total_ms / args.steps
     gpu_launches = launches  # our kernels only (the L2 flush is a torch fill, not counted)
@@ -439,11 +445,7 @@ def run_ours(args, rank, world, dist):
         img_host.copy_(step(e_d), non_blocking=True)
     t1.record(stream)
     t1.synchronize()
-    e2e_ms = t0.elapsed_time(t1)
-    if dist:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(t0.elapsed_time(t1), dist, dev)
     e2e_value = world * e2e_steps / (e2e_ms * 1e-3)
 
     if rank != 0:
