@@ -47,6 +47,7 @@ def parse_args():
     p.add_argument('--cpu-seconds', type=float, default=10.0)
     p.add_argument('--grad-steps', type=int, default=20, help='timed DM-gradient steps (0: skip that leg)')
     p.add_argument('--no-atmosphere', action='store_true', help='skip the atmospheric-layer leg')
+    p.add_argument('--no-graph', action='store_true', help='launch the step from Python instead of a CUDA graph')
     return p.parse_args()
 
 
@@ -395,6 +396,23 @@ def run_ours(args, rank, world, dist):
         img = step(e_dev)
     torch.cuda.synchronize()
 
+    # -- the step as a CUDA graph: plans, workspaces and tiles exist after the warm-up -----------------
+    graph = None
+    if not args.no_graph:
+        static_e = e_dev.clone()
+        side = torch.cuda.Stream()
+        side.wait_stream(stream)
+        with torch.cuda.stream(side):
+            for _ in range(2):
+                step(static_e)
+        stream.wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        launches_captured = hg.launch_count()
+        with torch.cuda.graph(graph):
+            static_img = step(static_e)
+        launches_per_replay = hg.launch_count() - launches_captured
+        torch.cuda.synchronize()
+
     # -- device-resident timing: per-step events, L2 flushed between steps outside the events --------
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -404,19 +422,31 @@ def run_ours(args, rank, world, dist):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    trace_kind = hg._lib.HX_TRACE_SPLIT_GEMM if args.precision == 'split' else hg._lib.HX_TRACE_SIMT_GEMM
-    hg._lib.trace_read(trace_kind, reset=True)
-    hg._lib.trace_enable(True)  # CUDA events around every GEMM launch, on the launching stream
     launches0 = hg.launch_count()
     wall0 = time.perf_counter()
     for i in range(args.steps):
         flush.fill_(float(i))
         starts[i].record(stream)
-        img = step(e_dev)
+        if graph is not None:
+            graph.replay()
+        else:
+            img = step(e_dev)
         ends[i].record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
-    launches = hg.launch_count() - launches0
+    launches = hg.launch_count() - launches0 + (launches_per_replay * args.steps if graph is not None else 0)
+    if graph is not None:
+        img = static_img
+
+    # -- kernel timing for the roofline: the same steps without the graph, CUDA events around every GEMM
+    #    launch on its stream (hx_trace_enable); the kernels are the ones the graph replays ------------
+    trace_kind = hg._lib.HX_TRACE_SPLIT_GEMM if args.precision == 'split' else hg._lib.HX_TRACE_SIMT_GEMM
+    hg._lib.trace_read(trace_kind, reset=True)
+    hg._lib.trace_enable(True)
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        step(e_dev)
+    torch.cuda.synchronize()
     hg._lib.trace_enable(False)
     k_launches, k_ms, k_cmacs = hg._lib.trace_read(trace_kind, reset=True)
     if dist:
@@ -426,7 +456,7 @@ def run_ours(args, rank, world, dist):
     total_ms = max_over_ranks(sum(step_ms), dist, dev)
     value = world * args.steps / (total_ms * 1e-3)
     ms_per_step = total_ms / args.steps
-    gpu_launches = launches  # our kernels only (the L2 flush is a torch fill, not counted)
+    gpu_launches = launches  # our kernels only (the L2 flush is a torch fill, not counted); graph replays count theirs
 
     # -- end to end through the public API with host buffers ------------------------------------------
     e_host = torch.from_numpy(w['E'].astype(np.complex64)).pin_memory()
@@ -501,6 +531,7 @@ def run_ours(args, rank, world, dist):
                    'pupil': args.pupil, 'fpm_grid': int(fpm_grid.dims[0]), 'image': int(focal.dims[0]),
                    'batch': 1, 'precision': args.precision, 'field_dtype': 'complex64',
                    'tiles': 'autotuned during the warm-up (hx_autotune)',
+                   'launch': 'CUDA graph of the step, replayed' if not args.no_graph else 'Python launches',
                    'l2': 'flushed between steps (256 MiB write outside the per-step events)',
                    'parallelism': 'replicas' if world > 1 else 'single-gpu'},
         'roofline': {'bound': bound, 'achieved': achieved_tflops, 'peak': peak, 'unit': 'TFLOP/s',
