@@ -459,24 +459,52 @@ def run_ours(args, rank, world, dist):
     gpu_launches = launches  # our kernels only (the L2 flush is a torch fill, not counted); graph replays count theirs
 
     # -- end to end through the public API with host buffers ------------------------------------------
+    # Every step uploads its pupil field from pinned host memory and reads its image back.  The copies run on
+    # their own streams, double-buffered, so step i+1's upload and step i-1's download overlap step i's
+    # transforms (as a streaming user would run them); the timed region spans all three streams.
     e_host = torch.from_numpy(w['E'].astype(np.complex64)).pin_memory()
-    img_host = torch.empty(focal.size, dtype=img.dtype).pin_memory()  # complex128 for the split form
+    img_host = [torch.empty(focal.size, dtype=img.dtype).pin_memory() for _ in range(2)]  # complex128 (split)
     e2e_steps = max(10, min(args.steps, 100))
-    for _ in range(3):
-        img_host.copy_(step(e_host.to(dev, non_blocking=True)), non_blocking=True)
+    h2d, d2h = torch.cuda.Stream(), torch.cuda.Stream()
+    d_in = [torch.empty_like(e_dev) for _ in range(2)]
+    in_ready = [torch.cuda.Event() for _ in range(2)]
+    in_free = [torch.cuda.Event() for _ in range(2)]
+    out_done = [torch.cuda.Event() for _ in range(2)]
+
+    def e2e_run(n):
+        used = [False, False]
+        for i in range(n):
+            b = i % 2
+            if used[b]:
+                h2d.wait_event(in_free[b])
+            with torch.cuda.stream(h2d):
+                d_in[b].copy_(e_host, non_blocking=True)
+                in_ready[b].record(h2d)
+            stream.wait_event(in_ready[b])
+            res = step(d_in[b])
+            in_free[b].record(stream)
+            used[b] = True
+            d2h.wait_stream(stream)
+            with torch.cuda.stream(d2h):
+                res.record_stream(d2h)
+                img_host[b].copy_(res, non_blocking=True)
+                out_done[b].record(d2h)
+        stream.wait_stream(d2h)
+
+    e2e_run(4)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     t0.record(stream)
-    for _ in range(e2e_steps):
-        e_d = e_host.to(dev, non_blocking=True)
-        img_host.copy_(step(e_d), non_blocking=True)
+    h2d.wait_event(t0)
+    e2e_run(e2e_steps)
     t1.record(stream)
     t1.synchronize()
     e2e_ms = max_over_ranks(t0.elapsed_time(t1), dist, dev)
     e2e_value = world * e2e_steps / (e2e_ms * 1e-3)
+    img_host = img_host[(e2e_steps - 1) % 2]
 
     if rank != 0:
         return
