@@ -48,6 +48,8 @@ def parse_args():
     p.add_argument('--grad-steps', type=int, default=20, help='timed DM-gradient steps (0: skip that leg)')
     p.add_argument('--no-atmosphere', action='store_true', help='skip the atmospheric-layer leg')
     p.add_argument('--no-graph', action='store_true', help='launch the step from Python instead of a CUDA graph')
+    p.add_argument('--broadband-frames', type=int, default=256,
+                   help='frames of the broadband-through-turbulence leg (0: skip it)')
     return p.parse_args()
 
 
@@ -57,7 +59,7 @@ def workload(args):
 
 
 def flops_per_propagation(w):
-    from oracle.fourier import mft_cmacs
+    from hcipy_gb300.workloads import mft_complex_macs as mft_cmacs
     nx, ny = (int(d) for d in w['pupil'].dims)
     nu, nv = (int(d) for d in w['fpm_grid'].dims)
     fu, fv = (int(d) for d in w['focal'].dims)
@@ -360,6 +362,128 @@ def run_atmosphere(args, dev, peaks):
     }
 
 
+def run_broadband(args, dev, peaks):
+    """Broadband imaging through turbulence: 21 wavelengths over 20 % bandwidth, each on its own diffraction-scaled
+    focal grid (284^2 ... 232^2, q=4, 32 lambda0/lambda), a 1024^2 pupil of 8 m behind three float32 infinite
+    layers (r0 0.1/0.2/0.3 m, L0 25 m, winds 10/15/25 m/s in three directions), 1 ms frames.  A frame evolves the
+    layers (extrusions with host-drawn noise, quintic shifts, the summed screen) and replays one CUDA graph that
+    holds, per wavelength, the phase of the summed screen and the matrix Fourier transform onto that wavelength's
+    grid; the split GEMMs run with the tiles the autotuner picked during the capture's warm-up."""
+    import torch
+    import hcipy_gb300 as hg
+    from hcipy_gb300 import _lib, workloads
+    w = workloads.broadband_turbulence_workload()
+    pupil, wls, grids = w['pupil'], w['wavelengths'], w['focal_grids']
+    t0 = time.perf_counter()
+    layers = [hg.InfiniteAtmosphericLayer(pupil, hg.Cn_squared_from_fried_parameter(lay['r0'], 500e-9), L0=w['L0'],
+                                          velocity=lay['velocity'], seed=21 + i, dtype=torch.float32)
+              for i, lay in enumerate(w['layers'])]
+    atm = hg.MultiLayerAtmosphere(layers)
+    init_s = time.perf_counter() - t0
+    ap = torch.from_numpy(w['aperture'].astype(np.complex64)).to(dev)
+    nx, ny = (int(d) for d in pupil.dims)
+    cmacs = sum(workloads.mft_complex_macs(nx, ny, int(g.dims[0]), int(g.dims[1])) for g in grids)
+    frames, dt = args.broadband_frames, w['frame_time']
+    legs = {}
+    for precision in ('fp32', 'split'):
+        imager = hg.BroadbandImager(pupil, wls, grids, focal_length=w['focal_length'], precision=precision,
+                                    pre=atm.forward)
+        atm.reset()
+        imager.capture(ap)
+        t = 0.0
+        for _ in range(3):
+            t += dt
+            atm.evolve_until(t)
+            imager.replay(ap)
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+        launches0 = hg.launch_count()
+        ev[0].record()
+        for _ in range(frames):
+            t += dt
+            atm.evolve_until(t)
+            imager.replay(ap)
+        ev[1].record()
+        ev[1].synchronize()
+        launches = hg.launch_count() - launches0
+        # the two halves of a frame on their own
+        ev[2].record()
+        for _ in range(frames):
+            imager.replay(ap)
+        ev[3].record()
+        for _ in range(frames):
+            t += dt
+            atm.evolve_until(t)
+        ev[5].record()
+        ev[5].synchronize()
+        frame_ms = ev[0].elapsed_time(ev[1]) / frames
+        graph_ms = ev[2].elapsed_time(ev[3]) / frames
+        atm_ms = ev[3].elapsed_time(ev[5]) / frames
+        # accuracy at the centre wavelength against the float64 oracle, on the field the device propagated
+        k = len(wls) // 2
+        from hcipy_gb300.kernels import apply_phase
+        e_dev = apply_phase(ap, atm.combined_screen(), 1.0 / wls[k])
+        img = imager.replay(ap)[k].cpu().numpy()
+        from oracle import optics
+        ref = optics.fraunhofer_forward(e_dev.cpu().numpy().astype(np.complex128), oracle_grid(pupil),
+                                        oracle_grid(grids[k]), wavelength=wls[k], focal_length=w['focal_length'])
+        if precision == 'split':
+            # the same graph with the wavelengths one after the other on one stream, for comparison
+            seq = hg.BroadbandImager(pupil, wls, grids, focal_length=w['focal_length'], precision=precision,
+                                     pre=atm.forward, streams=1).capture(ap)
+            ev[2].record()
+            for _ in range(frames):
+                seq.replay(ap)
+            ev[3].record()
+            ev[3].synchronize()
+            seq_ms = ev[2].elapsed_time(ev[3]) / frames
+            del seq
+        legs[precision] = {
+            'frames_per_s': 1e3 / frame_ms, 'propagations_per_s': len(wls) * 1e3 / frame_ms, 'frame_ms': frame_ms,
+            'graph_ms_per_frame': graph_ms, 'atmosphere_ms_per_frame': atm_ms,
+            'tflops_in_graph': 8 * cmacs / (graph_ms * 1e-3) / 1e12,
+            'launches_per_frame_outside_graph': launches / frames,
+            'kernels_in_graph': int(imager.graph_kernels),
+            'streams': imager.num_streams,
+            'rel_err_vs_fp64': float(np.linalg.norm(img - ref) / np.linalg.norm(ref)),
+        }
+        del imager
+    # host baseline: the reference algorithm on the host cores (matrices precomputed per wavelength, as the
+    # reference's propagator cache holds them), one frame's propagations over a bounded sample of wavelengths
+    from oracle import fourier
+    scr = atm.combined_screen().double().cpu().numpy()
+    apn = w['aperture']
+    x, y = pupil.separated_coords
+    n_done, spent, c_all = 0, 0.0, time.perf_counter()
+    for j in range(len(wls)):
+        uv = oracle_grid(grids[j]).scaled(2 * np.pi / (w['focal_length'] * wls[j]))
+        m1, m2 = fourier.mft_matrices(x, y, *uv.separated_coords)
+        c1 = time.perf_counter()
+        e = (apn * np.exp(1j * scr / wls[j])).reshape(ny, nx)
+        m1 @ (e @ m2)
+        spent += time.perf_counter() - c1
+        n_done += 1
+        if n_done >= 2 and time.perf_counter() - c_all > args.cpu_seconds / 2:
+            break
+    cpu_s_per_prop = spent / n_done
+    return {
+        'workload': '21 wavelengths over 20%% bandwidth, focal grids %d^2..%d^2 (q=4, 32 lambda0/lambda), 1024^2 '
+                    'pupil of 8 m, 3 float32 infinite layers (r0 0.1/0.2/0.3 m, L0 25 m, 10/15/25 m/s), 1 ms '
+                    'frames, %d frames' % (int(grids[0].dims[0]), int(grids[-1].dims[0]), frames),
+        'fp32': legs['fp32'], 'split': legs['split'],
+        'split_over_fp32': legs['split']['frames_per_s'] / legs['fp32']['frames_per_s'],
+        'split_graph_ms_one_stream': seq_ms,
+        'complex_macs_per_frame': int(cmacs),
+        'layer_init_s': init_s,
+        'timing': 'CUDA events on the stream around %d frames; graph_ms: the replays alone; atmosphere_ms: the '
+                  'evolutions alone (host rng draws and launches included)' % frames,
+        'cpu_baseline': {'propagations_per_s': 1.0 / cpu_s_per_prop, 'frames_per_s': 1.0 / (cpu_s_per_prop * len(wls)),
+                         'cores': host_cores(), 'kind': 'port',
+                         'sample': '%d of the 21 wavelengths: phase + two complex128 numpy GEMMs with precomputed '
+                                   'matrices (matrix construction not timed)' % n_done},
+    }
+
+
 def max_over_ranks(value, dist, device):
     """The largest value over all ranks (a no-op without a process group): the whole job's time."""
     if dist is None:
@@ -585,6 +709,8 @@ def run_ours(args, rank, world, dist):
         line['grad_steps'] = run_grad(args, dev)
     if not args.no_atmosphere:
         line['atmosphere'] = run_atmosphere(args, dev, peaks)
+    if args.broadband_frames > 0:
+        line['broadband_turbulence'] = run_broadband(args, dev, peaks)
     print(json.dumps(line), flush=True)
 
 

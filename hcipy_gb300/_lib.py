@@ -29,6 +29,8 @@ HX_BACKWARD = 1
 HX_ADJOINT = 2
 HX_PREC_FP32 = 0
 HX_PREC_SPLIT = 1
+HX_SCHEDULE_LATENCY = 0
+HX_SCHEDULE_THROUGHPUT = 1
 HX_EPI_NONE = 0
 HX_EPI_MUL = 1
 HX_EPI_BABINET = 2
@@ -66,6 +68,8 @@ SIGNATURES = {
                                       c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
     'hx_atmosphere_shift': (c_int, [c_void_p, c_int, c_int, c_int, c_int, P(c_double), P(c_double), c_void_p, c_int,
                                     c_void_p]),
+    'hx_mft_plan_set_schedule': (c_int, [c_void_p, c_int]),
+    'hx_atmosphere_combine': (c_int, [P(c_void_p), c_int, c_ll, c_void_p, c_int, c_void_p]),
     'hx_trace_read': (c_int, [c_int, P(c_ll), P(c_double), P(c_double), c_int]),
     'hx_mft_plan_create': (c_int, [c_int, c_int, c_int, c_int, P(c_double), P(c_double), P(c_double), P(c_double),
                                    P(c_double), P(c_double), P(c_double), P(c_double), c_int, c_int, c_void_p,

@@ -162,6 +162,7 @@ class AtmosphericLayer(OpticalElement):
         self.velocity = velocity
         self.height = height
         self._t = 0
+        self._version = 0  # bumped whenever the device screen changes (combined screens key on it)
 
     @property
     def t(self):
@@ -290,10 +291,17 @@ class InfiniteAtmosphericLayer(AtmosphericLayer):
             screen = self._initial_screen.reshape(self.ny, self.nx)
         else:
             screen = von_karman_screen(self.nx, self.ny, self._delta, self._Cn_squared, self._L0, self.rng)
-        self._ring = torch.from_numpy(np.ascontiguousarray(screen)).to(device='cuda', dtype=self.dtype)
+        ring = torch.from_numpy(np.ascontiguousarray(screen)).to(device='cuda', dtype=self.dtype)
+        if getattr(self, '_ring', None) is not None and self._ring.shape == ring.shape:
+            # in place: a captured CUDA graph that reads these buffers stays valid across resets
+            self._ring.copy_(ring)
+            self._shifted.copy_(ring)
+        else:
+            self._ring = ring
+            self._shifted = ring.clone()
         self._row0 = 0
         self._col0 = 0
-        self._shifted = self._ring.clone()
+        self._version += 1
         self.center = np.zeros(2)
         self._t = 0
 
@@ -326,6 +334,7 @@ class InfiniteAtmosphericLayer(AtmosphericLayer):
                                               int(B.shape[1]), _lib.dptr(noise), _lib.dtype_code(self.dtype),
                                               _lib.dptr(self._work), _lib.stream_handle())
         _lib.check(rc, 'hx_atmosphere_extrude')
+        self._version += 1
         if w == 0:
             self._row0 = (self._row0 - 1) % self.ny
         elif w == 1:
@@ -355,11 +364,7 @@ class InfiniteAtmosphericLayer(AtmosphericLayer):
             std = math.sqrt(self._Cn_squared)
             draws = [self.rng.normal(0, std, size=(self.B_vertical if _WHERE[w] <= 1 else self.B_horizontal).shape[1])
                      for w in plan]
-            width = max(x.size for x in draws)
-            host = np.zeros((len(plan), width))
-            for i, x in enumerate(draws):
-                host[i, :x.size] = x
-            noise = torch.from_numpy(host).to(device='cuda', dtype=self.dtype)
+            noise = self._upload_noise(draws)
             for i, w in enumerate(plan):
                 self._extrude(w, noise[i])
         if self.use_interpolation:
@@ -370,6 +375,36 @@ class InfiniteAtmosphericLayer(AtmosphericLayer):
             taps_row = taps_col = np.array([0, 0, 0, 1.0, 0, 0, 0])
         self._shift(taps_row, taps_col)
 
+    def _upload_noise(self, draws):
+        """The step's noise rows on the device (len(draws) x width, zero-padded), without stalling the host.
+
+        The rows go through one of two pinned host buffers with an asynchronous copy on the current stream, so
+        evolving the layer does not wait for the GPU work queued before it (a copy from pageable memory would);
+        a buffer is refilled only after the event recorded behind its previous copy."""
+        width = max(x.size for x in draws)
+        need = len(draws) * width
+        self._noise_slot = slot = (getattr(self, '_noise_slot', 1) + 1) % 2
+        if not hasattr(self, '_noise_host'):
+            self._noise_host, self._noise_event = [None, None], [None, None]
+            self._noise_dev = None
+        if self._noise_event[slot] is not None:
+            self._noise_event[slot].synchronize()
+        buf = self._noise_host[slot]
+        if buf is None or buf.numel() < need:
+            buf = self._noise_host[slot] = torch.empty(need, dtype=self.dtype, pin_memory=True)
+        if self._noise_dev is None or self._noise_dev.numel() < need:
+            self._noise_dev = torch.empty(need, dtype=self.dtype, device='cuda')
+        host = buf[:need].numpy().reshape(len(draws), width)
+        host[...] = 0
+        for i, x in enumerate(draws):
+            host[i, :x.size] = x
+        dev = self._noise_dev[:need]
+        dev.copy_(buf[:need], non_blocking=True)
+        if self._noise_event[slot] is None:
+            self._noise_event[slot] = torch.cuda.Event()
+        self._noise_event[slot].record()
+        return dev.view(len(draws), width)
+
     def _shift(self, taps_row, taps_col):
         tr = np.ascontiguousarray(taps_row, np.float64)
         tc = np.ascontiguousarray(taps_col, np.float64)
@@ -378,6 +413,7 @@ class InfiniteAtmosphericLayer(AtmosphericLayer):
                                             tr.ctypes.data_as(P), tc.ctypes.data_as(P), _lib.dptr(self._shifted),
                                             _lib.dtype_code(self.dtype), _lib.stream_handle())
         _lib.check(rc, 'hx_atmosphere_shift')
+        self._version += 1
 
     # -- screens -------------------------------------------------------------------------------------------
     @property
@@ -397,24 +433,35 @@ class InfiniteAtmosphericLayer(AtmosphericLayer):
 
 
 class MultiLayerAtmosphere(OpticalElement):
-    """Layers applied in order without inter-layer propagation (atmospheric_model.py:153-310 with
-    scintillation=False)."""
+    """Layers applied without propagation between them (atmospheric_model.py:153-310 with scintillation=False).
+
+    The reference applies the layers one after the other, sorted by height (:185-212, :300-308); without
+    propagation between them the product of their phase factors is the phase factor of the summed screens, so
+    ``forward``/``backward`` sum the layers' screens once (``hx_atmosphere_combine``, into a buffer that keeps
+    its address) and apply one phase kernel.  ``evolve_until`` refreshes the sum, so a CUDA graph that captured
+    ``forward`` replays with the current screens; after evolving a layer on its own, call ``combined_screen()``
+    before replaying such a graph.
+    """
 
     def __init__(self, layers, scintillation=False):
         if scintillation:
             raise NotImplementedError('scintillation needs Fresnel propagation between the layers')
         self.layers = list(layers)
         self._t = 0
+        self._combined = None
+        self._combined_key = None
 
     def evolve_until(self, t):
         for layer in self.layers:
             layer.evolve_until(t)
         self._t = t
+        self.combined_screen()
 
     def reset(self, make_independent_realization=False):
         for layer in self.layers:
             layer.reset(make_independent_realization)
         self._t = 0
+        self.combined_screen()
 
     @property
     def t(self):
@@ -424,19 +471,49 @@ class MultiLayerAtmosphere(OpticalElement):
     def t(self, t):
         self.evolve_until(t)
 
+    def combined_screen(self):
+        """The sum of the layers' current screens (radians at 1 m), a device tensor (npix,)."""
+        screens = [layer._screen_tensor() for layer in self.layers]
+        key = tuple((id(layer), getattr(layer, '_version', None), s.data_ptr())
+                    for layer, s in zip(self.layers, screens))
+        if self._combined is not None and key == self._combined_key and None not in (k[1] for k in key):
+            return self._combined
+        dt = screens[0].dtype
+        if any(s.dtype != dt or s.numel() != screens[0].numel() for s in screens):
+            raise ValueError('the layers must share their grid and screen dtype')
+        if self._combined is None or self._combined.dtype != dt or self._combined.numel() != screens[0].numel():
+            self._combined = torch.empty_like(screens[0].reshape(-1))
+        start = 0
+        while start < len(screens):
+            # up to 8 screens a launch; past the first launch, 7 more plus the running sum
+            part = screens[start:start + (8 if start == 0 else 7)]
+            ptrs = (_lib.ctypes.c_void_p * (len(part) + (start > 0)))()
+            for i, s in enumerate(part):
+                ptrs[i] = _lib.dptr(s)
+            if start > 0:
+                ptrs[len(part)] = _lib.dptr(self._combined)
+            start += len(part)
+            rc = _lib.lib().hx_atmosphere_combine(ptrs, len(ptrs), screens[0].numel(), _lib.dptr(self._combined),
+                                                  _lib.dtype_code(dt), _lib.stream_handle())
+            _lib.check(rc, 'hx_atmosphere_combine')
+        self._combined_key = key
+        return self._combined
+
     def phase_for(self, wavelength):
-        total = None
-        for layer in self.layers:
-            p = layer.phase_for(wavelength).data
-            total = p if total is None else total + p
-        return Field(total, self.layers[0].input_grid)
+        return Field(self.combined_screen() / wavelength, self.layers[0].input_grid)
+
+    def _apply(self, wf, sign):
+        e = as_tensor(wf.electric_field)
+        s = self.combined_screen()
+        if torch.is_grad_enabled() and e.requires_grad:
+            from .autograd import phase_apply
+            out = phase_apply(e, s, sign / wf.wavelength)
+        else:
+            out = apply_phase(e, s, sign / wf.wavelength)
+        return Wavefront(Field(out, wf.electric_field.grid), wf.wavelength)
 
     def forward(self, wavefront):
-        for layer in self.layers:
-            wavefront = layer.forward(wavefront)
-        return wavefront
+        return self._apply(wavefront, 1.0)
 
     def backward(self, wavefront):
-        for layer in reversed(self.layers):
-            wavefront = layer.backward(wavefront)
-        return wavefront
+        return self._apply(wavefront, -1.0)

@@ -28,27 +28,71 @@ class BroadbandImager(object):
     ``forward(e)`` takes a pupil field tensor (..., npix) (or a Field/Wavefront) and returns a list of complex
     image tensors, one per wavelength, each (..., n_focal(lambda)).  ``pre`` is an optional callable
     ``pre(wavefront) -> wavefront`` applied per wavelength before the lens (an atmosphere, a DM).
+
+    The wavelengths' transforms are independent (each has its own plan), and one of them fills only a fraction of
+    the GPU (a 1024^2 -> 256^2 transform is a few dozen output tiles), so ``forward`` runs ``pre`` for every
+    wavelength in order on the calling stream and hands each wavelength's transform to one of ``streams`` side
+    streams: transforms of different wavelengths overlap, and inside a captured graph they become parallel
+    branches.  ``streams=1`` runs everything on the calling stream.  With more than one stream the transforms'
+    split GEMMs use the throughput tile policy (no K split: the other wavelengths fill the GPU).
     """
 
-    def __init__(self, pupil_grid, wavelengths, focal_grids, focal_length=1, precision='fp32', pre=None):
+    def __init__(self, pupil_grid, wavelengths, focal_grids, focal_length=1, precision='fp32', pre=None,
+                 streams=8):
         if len(focal_grids) != len(wavelengths):
             raise ValueError('one focal grid per wavelength is needed')
         self.pupil_grid = pupil_grid
         self.wavelengths = [float(w) for w in wavelengths]
         self.focal_grids = list(focal_grids)
         self.pre = pre
-        self.props = [FraunhoferPropagator(pupil_grid, g, focal_length=focal_length, precision=precision)
-                      for g in self.focal_grids]
+        self.num_streams = max(1, min(int(streams), len(self.focal_grids)))
+        schedule = 'throughput' if self.num_streams > 1 else 'latency'
+        self.props = [FraunhoferPropagator(pupil_grid, g, focal_length=focal_length, precision=precision,
+                                           schedule=schedule) for g in self.focal_grids]
+        self._streams = None
         self._graph = None
 
-    def forward(self, e):
+    def _side_streams(self):
+        if self._streams is None:
+            self._streams = [torch.cuda.Stream() for _ in range(self.num_streams)]
+        return self._streams
+
+    def forward(self, e, concurrent=True):
         t = as_tensor(e.electric_field if isinstance(e, Wavefront) else e)
+        if not concurrent or self.num_streams == 1:
+            out = []
+            for wl, prop in zip(self.wavelengths, self.props):
+                wf = Wavefront(Field(t, self.pupil_grid), wl)
+                if self.pre is not None:
+                    wf = self.pre(wf)
+                out.append(prop.forward(wf).electric_field.data)
+            return out
+        main = torch.cuda.current_stream()
+        streams = self._side_streams()
+        capturing = torch.cuda.is_current_stream_capturing()
         out = []
-        for wl, prop in zip(self.wavelengths, self.props):
+        # Each wavelength's field stays referenced until every side stream has joined: freed earlier, its memory
+        # could go to the next wavelength's field on the calling stream while a side stream still reads it
+        # (record_stream guards that outside a capture; inside one only the reference does).
+        fields = []
+        for i, (wl, prop) in enumerate(zip(self.wavelengths, self.props)):
             wf = Wavefront(Field(t, self.pupil_grid), wl)
             if self.pre is not None:
-                wf = self.pre(wf)
-            out.append(prop.forward(wf).electric_field.data)
+                wf = self.pre(wf)  # in order on the calling stream: ``pre`` may keep state
+            fields.append(wf.electric_field.data)
+            side = streams[i % len(streams)]
+            side.wait_stream(main)
+            with torch.cuda.stream(side):
+                img = prop.forward(wf).electric_field.data
+            if not capturing:
+                # the field was made on the calling stream and is read on ``side``; the image is made on
+                # ``side`` and handed back: tell the allocator about both uses
+                wf.electric_field.data.record_stream(side)
+                img.record_stream(main)
+            out.append(img)
+        for side in streams:
+            main.wait_stream(side)
+        del fields
         return out
 
     __call__ = forward
@@ -56,19 +100,23 @@ class BroadbandImager(object):
     def capture(self, example):
         """Record ``forward`` for inputs shaped like ``example`` in a CUDA graph; ``replay`` then runs it.
 
-        A warm-up call first creates every plan and workspace (plan creation synchronizes and may not be
-        captured)."""
+        Warm-up calls first create every plan and workspace (plan creation synchronizes and may not be
+        captured); the first runs the wavelengths one after the other, so that the split-GEMM autotuner, when it
+        is on, times its candidates on an otherwise idle GPU."""
         t = as_tensor(example.electric_field if isinstance(example, Wavefront) else example)
         self._static_in = t.clone()
         side = torch.cuda.Stream()
         side.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(side):
-            for _ in range(2):
-                self.forward(self._static_in)
+            self.forward(self._static_in, concurrent=False)
+            self.forward(self._static_in)
         torch.cuda.current_stream().wait_stream(side)
+        from ._lib import launch_count
         self._graph = torch.cuda.CUDAGraph()
+        before = launch_count()
         with torch.cuda.graph(self._graph):
             self._static_out = self.forward(self._static_in)
+        self.graph_kernels = launch_count() - before  # library kernels recorded in the graph
         return self
 
     def replay(self, e):

@@ -145,6 +145,40 @@ __global__ void ring_shift_kernel(const T* ring, int ny, int nx, int row0, int c
     }
 }
 
+// out = sum of up to HX_MAX_SCREENS screens (the combined phase of layers applied without propagation between
+// them); 4 elements per thread where the pointers allow 16-byte access.
+constexpr int MAX_SCREENS = 8;
+template <typename T>
+struct ScreenSet {
+    const T* s[MAX_SCREENS];
+};
+
+template <typename T>
+__global__ void combine_screens_kernel(ScreenSet<T> set, int count, long long n, T* out) {
+    const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    if (i >= n) return;
+    if (i + 4 <= n) {
+        T a0 = set.s[0][i], a1 = set.s[0][i + 1], a2 = set.s[0][i + 2], a3 = set.s[0][i + 3];
+        for (int l = 1; l < count; ++l) {
+            const T* p = set.s[l] + i;
+            a0 += p[0];
+            a1 += p[1];
+            a2 += p[2];
+            a3 += p[3];
+        }
+        out[i] = a0;
+        out[i + 1] = a1;
+        out[i + 2] = a2;
+        out[i + 3] = a3;
+    } else {
+        for (long long k = i; k < n; ++k) {
+            T a = set.s[0][k];
+            for (int l = 1; l < count; ++l) a += set.s[l][k];
+            out[k] = a;
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -205,6 +239,28 @@ int hx_atmosphere_shift(const void* ring, int ny, int nx, int row0, int col0, co
     else
         ring_shift_kernel<double><<<grid, block, 0, st>>>((const double*)ring, ny, nx, row0, col0, t, (double*)out);
     return hx::launch_status("ring_shift_kernel");
+}
+
+int hx_atmosphere_combine(const void* const* screens, int count, long long n, void* out, int dtype, void* stream) {
+    HX_CHECK_ARG(screens && out, "hx_atmosphere_combine: NULL pointer");
+    HX_CHECK_ARG(count >= 1 && count <= MAX_SCREENS, "hx_atmosphere_combine: count must be 1..8");
+    HX_CHECK_ARG(n > 0, "hx_atmosphere_combine: n must be positive");
+    HX_CHECK_ARG(dtype == HX_F32 || dtype == HX_F64, "hx_atmosphere_combine: dtype must be HX_F32 or HX_F64");
+    for (int l = 0; l < count; ++l) HX_CHECK_ARG(screens[l], "hx_atmosphere_combine: NULL screen");
+    if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned blocks = (unsigned)hx::ceil_div((n + 3) / 4, 256);
+    hx::TraceScope trace(HX_TRACE_ATMOSPHERE, (double)(count + 1) * (dtype == HX_F32 ? 4 : 8) * (double)n, st);
+    if (dtype == HX_F32) {
+        ScreenSet<float> set{};
+        for (int l = 0; l < count; ++l) set.s[l] = (const float*)screens[l];
+        combine_screens_kernel<float><<<blocks, 256, 0, st>>>(set, count, n, (float*)out);
+    } else {
+        ScreenSet<double> set{};
+        for (int l = 0; l < count; ++l) set.s[l] = (const double*)screens[l];
+        combine_screens_kernel<double><<<blocks, 256, 0, st>>>(set, count, n, (double*)out);
+    }
+    return hx::launch_status("combine_screens_kernel");
 }
 
 }  // extern "C"

@@ -317,6 +317,14 @@ int hx_mft_plan_destroy(hx_mft_plan* p) {
     return HX_OK;
 }
 
+int hx_mft_plan_set_schedule(hx_mft_plan* p, int schedule) {
+    HX_CHECK_ARG(p != nullptr, "hx_mft_plan_set_schedule: plan is NULL");
+    HX_CHECK_ARG(schedule == HX_SCHEDULE_LATENCY || schedule == HX_SCHEDULE_THROUGHPUT,
+                 "hx_mft_plan_set_schedule: unknown schedule %d", schedule);
+    if (p->split) hx::split_mft_set_schedule(p->split, schedule);
+    return HX_OK;
+}
+
 int hx_autotune(int on) {
     hx::split_autotune(on);
     return HX_OK;

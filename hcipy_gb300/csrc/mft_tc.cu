@@ -944,9 +944,16 @@ std::vector<TileChoice> tile_candidates(long long m_tiles, int N, int grid_z, in
 // CTA): more CTAs share the epilogue and the last CTA of a tile reads fewer partial bytes.
 // HX_SPLIT_TILE="bn[,ksplit]" overrides the choice (tuning); with the autotuner on, a measured choice for the
 // same GEMM shape takes precedence (see launch_gemm).
-TileChoice choose_tile(long long m_tiles, int N, int grid_z, int ktiles) {
+// Under HX_SCHEDULE_THROUGHPUT the GEMM shares the GPU with concurrent ones (other streams or graph branches
+// fill the SMs), so no K split is taken (its partial sums and fix-up are extra work once the GPU is full) and the
+// wider tile that pads the output columns least is used.
+TileChoice choose_tile(long long m_tiles, int N, int grid_z, int ktiles, int schedule) {
     int fbn, fks;
     forced_tiles(&fbn, &fks);
+    if (schedule == HX_SCHEDULE_THROUGHPUT && !fbn && !fks) {
+        const int bn = N <= 64 ? 64 : (round_up(N, 112) < round_up(N, 128) ? 112 : 128);
+        return make_choice(m_tiles, N, grid_z, ktiles, bn, 1);
+    }
     const int sms = sm_count();
     const long long tiles128 = m_tiles * (long long)ceil_div(N, 128) * grid_z;
     const int bn = fbn ? fbn : (N > 64 && 4 * tiles128 >= 3LL * sms ? 128 : 64);
@@ -965,11 +972,28 @@ struct GemmShape {
 };
 
 struct TunedEntry {
-    TileChoice best;
     int n = 0;                 // candidates measured
-    int bn[8], ksplit[8];
+    TileChoice cand[8];
     float ms[8];               // best of two timed launches each
 };
+
+// The kept candidate of a measured shape.  Latency: the fastest.  Throughput: the least SM time, the duration
+// times the SMs its CTAs occupy (one resident CTA per SM), which is what it takes from concurrent GEMMs.
+TileChoice pick_tuned(const TunedEntry& e, int schedule) {
+    const int sms = sm_count();
+    int best = 0;
+    double best_cost = 1e300;
+    for (int k = 0; k < e.n; ++k) {
+        double cost = e.ms[k];
+        if (schedule == HX_SCHEDULE_THROUGHPUT)
+            cost *= (double)std::min<long long>(e.cand[k].tiles * e.cand[k].ksplit, (long long)sms);
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = k;
+        }
+    }
+    return e.cand[best];
+}
 
 std::atomic<int> g_autotune{0};
 std::mutex g_tune_mu;
@@ -1038,7 +1062,7 @@ int launch_choice(GemmArgs& g, const SliceMat& A, const SliceMat& B, const TileC
 // stream and keeps the fastest.  The launches write the same result each time (the epilogue maxima are
 // idempotent).
 int tune(GemmArgs& g, const SliceMat& A, const SliceMat& B, const GemmShape& key, int grid_z, float* partial,
-         unsigned int* counters, cudaStream_t st, TileChoice* best) {
+         unsigned int* counters, cudaStream_t st, TunedEntry* out) {
     const std::vector<TileChoice> cands = tile_candidates(key.m_tiles, key.N, key.grid_z, key.ktiles);
     cudaEvent_t ev[3];
     for (int i = 0; i < 3; ++i) {
@@ -1049,7 +1073,6 @@ int tune(GemmArgs& g, const SliceMat& A, const SliceMat& B, const GemmShape& key
         }
     }
     TunedEntry entry;
-    float best_ms = 1e30f;
     int rc = HX_OK;
     for (const TileChoice& c : cands) {
         if ((rc = launch_choice(g, A, B, c, grid_z, partial, counters, 0.0, false, st)) != HX_OK) break;
@@ -1064,19 +1087,18 @@ int tune(GemmArgs& g, const SliceMat& A, const SliceMat& B, const GemmShape& key
         cudaEventElapsedTime(&t2, ev[1], ev[2]);
         const float ms = std::min(t1, t2);
         if (entry.n < 8) {
-            entry.bn[entry.n] = c.bn;
-            entry.ksplit[entry.n] = c.ksplit;
+            entry.cand[entry.n] = c;
             entry.ms[entry.n] = ms;
             ++entry.n;
-        }
-        if (ms < best_ms) {
-            best_ms = ms;
-            *best = c;
         }
     }
     for (int i = 0; i < 3; ++i) cudaEventDestroy(ev[i]);
     if (rc != HX_OK) return rc;
-    entry.best = *best;
+    if (entry.n == 0) {
+        set_error("autotune: no tile candidate");
+        return HX_ERR_INVALID;
+    }
+    *out = entry;
     std::lock_guard<std::mutex> lock(g_tune_mu);
     g_tuned[key] = entry;
     return HX_OK;
@@ -1084,7 +1106,7 @@ int tune(GemmArgs& g, const SliceMat& A, const SliceMat& B, const GemmShape& key
 
 // partial / counters are sized for every candidate (carve_ws), so the autotuner may pick any of them.
 int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, TileChoice c, int grid_z, float* partial,
-                unsigned int* counters, double cmacs, cudaStream_t st) {
+                unsigned int* counters, double cmacs, int schedule, cudaStream_t st) {
     if (A.kpitch != B.kpitch) {
         set_error("internal: split GEMM K mismatch (%d vs %d)", A.kpitch, B.kpitch);
         return HX_ERR_INVALID;
@@ -1100,13 +1122,17 @@ int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, TileChoice c,
             std::lock_guard<std::mutex> lock(g_tune_mu);
             auto it = g_tuned.find(key);
             if (it != g_tuned.end()) {
-                c = it->second.best;
+                c = pick_tuned(it->second, schedule);
                 found = true;
             }
         }
         cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
         cudaStreamIsCapturing(st, &cap);
-        if (!found && cap == cudaStreamCaptureStatusNone) HX_TRY(tune(g, A, B, key, grid_z, partial, counters, st, &c));
+        if (!found && cap == cudaStreamCaptureStatusNone) {
+            TunedEntry entry;
+            HX_TRY(tune(g, A, B, key, grid_z, partial, counters, st, &entry));
+            c = pick_tuned(entry, schedule);
+        }
     }
     return launch_choice(g, A, B, c, grid_z, partial, counters, cmacs, true, st);
 }
@@ -1131,6 +1157,7 @@ struct SplitMftPlan {
     SliceMat m1b, m2b;       // backward: A of G1 (rows 2 ny64, K nv), B of G2 (rows nx64, K nu)
     SliceMat m1a, m2a;       // adjoint (own copies only for non-uniform weights)
     int* status = nullptr;
+    int schedule = HX_SCHEDULE_LATENCY;  // tile policy of its GEMMs
 };
 
 namespace {
@@ -1201,8 +1228,8 @@ void carve_ws(Carver& c, const SplitMftPlan* p, int direction, int batch, Ws& w)
         g1_rows = p->m1b.rows, g1_n = p->nu, g1_z = batch, g1_kt = p->m1b.kpitch / BK;
         g2_rows = w.s2.rows, g2_n = p->nx, g2_z = 1, g2_kt = w.s2.kpitch / BK;
     }
-    w.c1 = choose_tile(g1_rows / BM, g1_n, g1_z, g1_kt);
-    w.c2 = choose_tile(g2_rows / BM, g2_n, g2_z, g2_kt);
+    w.c1 = choose_tile(g1_rows / BM, g1_n, g1_z, g1_kt, p->schedule);
+    w.c2 = choose_tile(g2_rows / BM, g2_n, g2_z, g2_kt, p->schedule);
     // split-K workspace for every candidate tile of both GEMMs, so the layout does not depend on the choice
     size_t part = 0;
     long long tiles = 0;
@@ -1246,7 +1273,7 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
         g1.colmax = w.t_max;
         g1.colmax_rows_per_field = ny;
         g1.colmax_field_stride = nu64;
-        HX_TRY(launch_gemm(g1, w.s1, p->m2f, w.c1, 1, w.partial, w.counters, (double)rows * nu * nx, st));
+        HX_TRY(launch_gemm(g1, w.s1, p->m2f, w.c1, 1, w.partial, w.counters, (double)rows * nu * nx, p->schedule, st));
         // G2: out[b] = alpha M1f . T[b] with the fused epilogue.
         HX_TRY(launch_slice_cols(w.t, ny, nu, batch, (long long)ny * nu, w.t_max, nu64, w.s2, (int)nu64, st));
         GemmArgs g2 = base_args(p->status);
@@ -1268,7 +1295,7 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
         g2.rowmax_z = nv;
         g2.colmax = out_colmax;
         g2.colmax_z = nu64;
-        return launch_gemm(g2, p->m1f, w.s2, w.c2, batch, w.partial, w.counters, (double)nv * nu * ny * batch, st);
+        return launch_gemm(g2, p->m1f, w.s2, w.c2, batch, w.partial, w.counters, (double)nv * nu * ny * batch, p->schedule, st);
     }
     const SliceMat& m1 = direction == HX_BACKWARD ? p->m1b : p->m1a;
     const SliceMat& m2 = direction == HX_BACKWARD ? p->m2b : p->m2a;
@@ -1293,7 +1320,7 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
     g1.out_z = (long long)ny * nu;
     g1.rowmax = w.t_max;
     g1.rowmax_z = ny;
-    HX_TRY(launch_gemm(g1, m1, w.s1, w.c1, batch, w.partial, w.counters, (double)ny * nu * nv * batch, st));
+    HX_TRY(launch_gemm(g1, m1, w.s1, w.c1, batch, w.partial, w.counters, (double)ny * nu * nv * batch, p->schedule, st));
     // G2: out = alpha T . M2, stacked over the batch, with the fused epilogue.
     HX_TRY(launch_slice_rows(w.t, nu, rows, nu, w.t_max, w.s2, st));
     GemmArgs g2 = base_args(p->status);
@@ -1312,7 +1339,7 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
     g2.colmax = out_colmax;
     g2.colmax_rows_per_field = ny;
     g2.colmax_field_stride = round_up(nx, 64);
-    return launch_gemm(g2, w.s2, m2, w.c2, 1, w.partial, w.counters, (double)rows * nx * nu, st);
+    return launch_gemm(g2, w.s2, m2, w.c2, 1, w.partial, w.counters, (double)rows * nx * nu, p->schedule, st);
 }
 
 }  // namespace
@@ -1462,6 +1489,10 @@ int split_mft_status(const SplitMftPlan* p, int reset) {
     return h;
 }
 
+void split_mft_set_schedule(SplitMftPlan* p, int schedule) {
+    if (p) p->schedule = schedule;
+}
+
 void split_autotune(int on) { g_autotune.store(on ? 1 : 0, std::memory_order_relaxed); }
 
 int split_autotune_entries() {
@@ -1480,8 +1511,8 @@ int split_autotune_entry(int i, long long* shape, int* n, int* bn, int* ksplit, 
     shape[3] = it->first.ktiles;
     *n = it->second.n;
     for (int k = 0; k < it->second.n; ++k) {
-        bn[k] = it->second.bn[k];
-        ksplit[k] = it->second.ksplit[k];
+        bn[k] = it->second.cand[k].bn;
+        ksplit[k] = it->second.cand[k].ksplit;
         ms[k] = it->second.ms[k];
     }
     return HX_OK;

@@ -27,6 +27,8 @@ int split_lyot_execute(const SplitMftPlan* fpm, const SplitMftPlan* img, int bat
 // Status word of the bounded device waits (HX_OK or HX_ERR_TIMEOUT); synchronizes with the device.
 int split_mft_status(const SplitMftPlan* p, int reset);
 void split_mft_destroy(SplitMftPlan* p);
+// Tile policy of the plan's GEMMs: HX_SCHEDULE_LATENCY or HX_SCHEDULE_THROUGHPUT.
+void split_mft_set_schedule(SplitMftPlan* p, int schedule);
 // Autotuner of the split GEMM tiles (process-wide): on/off, number of measured shapes, forget them.
 void split_autotune(int on);
 int split_autotune_entries();

@@ -114,6 +114,7 @@ def _scalar_weight(grid):
 # ---------------------------------------------------------------------------
 
 PRECISIONS = {'fp32': _lib.HX_PREC_FP32, 'split': _lib.HX_PREC_SPLIT}
+SCHEDULES = {'latency': _lib.HX_SCHEDULE_LATENCY, 'throughput': _lib.HX_SCHEDULE_THROUGHPUT}
 
 
 class _MftPlan(object):
@@ -168,6 +169,9 @@ class _MftPlan(object):
                                         _lib.dptr(workspace), nbytes, _lib.stream_handle())
         _lib.check(rc, 'hx_mft_execute_io')
 
+    def set_schedule(self, code):
+        _lib.check(self.lib.hx_mft_plan_set_schedule(self.handle, code), 'hx_mft_plan_set_schedule')
+
     def status(self, reset=True):
         """Status of the plan's bounded device waits (0 = fine); synchronizes with the device."""
         return int(self.lib.hx_mft_plan_status(self.handle, 1 if reset else 0))
@@ -190,11 +194,13 @@ class MatrixFourierTransform(FourierTransform):
     returns complex128, since its results hold more than a complex64 can.  ``precompute_matrices`` and
     ``allocate_intermediate`` are accepted for API compatibility: the phase
     matrices are always kept on the device and the intermediate is scratch from
-    torch's caching allocator.
+    torch's caching allocator.  ``schedule`` ('latency', default, or 'throughput') is the
+    tile policy of the split GEMMs: 'throughput' for transforms that run beside
+    others (several streams, parallel graph branches), see ``hx_mft_plan_set_schedule``.
     """
 
     def __init__(self, input_grid, output_grid, precompute_matrices=None, allocate_intermediate=None,
-                 precision='fp32'):
+                 precision='fp32', schedule='latency'):
         self.check_if_supported(input_grid, output_grid)
         self.input_grid = input_grid
         self.output_grid = output_grid
@@ -206,6 +212,9 @@ class MatrixFourierTransform(FourierTransform):
         if precision not in PRECISIONS:
             raise ValueError('precision must be one of %s' % sorted(PRECISIONS))
         self.precision = precision
+        if schedule not in SCHEDULES:
+            raise ValueError('schedule must be one of %s' % sorted(SCHEDULES))
+        self._schedule = schedule
 
         xs = [np.asarray(c, np.float64) for c in input_grid.separated_coords]
         us = [np.asarray(c, np.float64) for c in output_grid.separated_coords]
@@ -234,8 +243,21 @@ class MatrixFourierTransform(FourierTransform):
         plan = self._plans.get(key)
         if plan is None:
             plan = _MftPlan(*self._coords, self._win, self._wout, code, prec)
+            plan.set_schedule(SCHEDULES[self._schedule])
             self._plans[key] = plan
         return plan
+
+    @property
+    def schedule(self):
+        return self._schedule
+
+    @schedule.setter
+    def schedule(self, schedule):
+        if schedule not in SCHEDULES:
+            raise ValueError('schedule must be one of %s' % sorted(SCHEDULES))
+        self._schedule = schedule
+        for plan in self._plans.values():
+            plan.set_schedule(SCHEDULES[schedule])
 
     def _run(self, field, src_grid, dst_grid, direction, alpha, epilogue=_lib.HX_EPI_NONE, mask=None, src=None,
              out=None):

@@ -17,15 +17,16 @@ def _differentiable(field):
 class FraunhoferPropagator(AgnosticOpticalElement):
     """A perfect lens from its front to its back focal plane (hcipy/propagation/fraunhofer.py:7-88).
 
-    ``precision`` ('fp32' or 'split') is forwarded to the matrix Fourier
-    transform when the planner picks one.
+    ``precision`` ('fp32' or 'split') and ``schedule`` ('latency' or 'throughput')
+    are forwarded to the matrix Fourier transform when the planner picks one.
     """
 
-    def __init__(self, input_grid, output_grid, focal_length=1, precision='fp32'):
+    def __init__(self, input_grid, output_grid, focal_length=1, precision='fp32', schedule='latency'):
         self._input_grid = input_grid
         self._output_grid = output_grid
         self._focal_length = focal_length
         self.precision = precision
+        self.schedule = schedule
         AgnosticOpticalElement.__init__(self, grid_dependent=True, wavelength_dependent=True)
 
     def make_instance(self, instance_data, input_grid, output_grid, wavelength):
@@ -33,8 +34,9 @@ class FraunhoferPropagator(AgnosticOpticalElement):
         focal_length = self.evaluate_parameter(self.focal_length, input_grid, output_grid, wavelength)
         instance_data.uv_grid = output_grid.scaled(2 * np.pi / (focal_length * wavelength))
         ft = make_fourier_transform(input_grid, instance_data.uv_grid)
-        if isinstance(ft, MatrixFourierTransform) and self.precision != 'fp32':
-            ft = MatrixFourierTransform(input_grid, instance_data.uv_grid, precision=self.precision)
+        if isinstance(ft, MatrixFourierTransform) and (self.precision != 'fp32' or self.schedule != 'latency'):
+            ft = MatrixFourierTransform(input_grid, instance_data.uv_grid, precision=self.precision,
+                                        schedule=self.schedule)
         instance_data.fourier_transform = ft
         instance_data.norm_factor = 1 / (1j * focal_length * wavelength)
 

@@ -13,6 +13,40 @@ import numpy as np
 from .field import make_pupil_grid, make_focal_grid
 
 
+def mft_complex_macs(nx, ny, nu, nv):
+    """Complex multiply-accumulates of one matrix Fourier transform (ny x nx) -> (nv x nu) as two GEMMs,
+    E . M2 then M1 . (E M2) (the order of hcipy/fourier/matrix_fourier_transform.py:282-292)."""
+    return ny * nx * nu + nv * ny * nu
+
+
+def broadband_turbulence_workload(pupil_n=1024, diameter=8.0, num_wavelengths=21, bandwidth=0.2, q=4,
+                                  num_airy=32, reference_wavelength=500e-9,
+                                  layers=((0.1, 10.0, 0.0), (0.2, 15.0, 120.0), (0.3, 25.0, 240.0)), L0=25.0,
+                                  frame_time=1e-3):  # noqa: N803
+    """Broadband imaging through a three-layer frozen-flow atmosphere.
+
+    A ``pupil_n``^2 pupil of ``diameter`` meters; ``num_wavelengths`` wavelengths spanning ``bandwidth`` around
+    ``reference_wavelength``, each imaged on its own diffraction-scaled focal grid (q samples per
+    lambda0/D, num_airy lambda0/lambda radius, in lambda0/D units, so the focal length is D / lambda0); layers
+    given as (r0 in m at 500 nm, wind speed m/s, wind direction deg), outer scale ``L0`` m, frames
+    ``frame_time`` s apart.  Returns the grids and parameters; the layers themselves are built by the caller
+    (they need the GPU)."""
+    from .broadband import diffraction_scaled_focal_grids
+    pupil = make_pupil_grid(pupil_n, diameter)
+    rel = np.linspace(1 - bandwidth / 2, 1 + bandwidth / 2, num_wavelengths)
+    return {
+        'pupil': pupil,
+        'aperture': circular_aperture(pupil, diameter),
+        'wavelengths': rel * reference_wavelength,
+        'focal_grids': diffraction_scaled_focal_grids(q, num_airy, rel, 1.0),
+        'focal_length': diameter / reference_wavelength,
+        'layers': [{'r0': r0, 'velocity': (v * math.cos(math.radians(a)), v * math.sin(math.radians(a)))}
+                   for r0, v, a in layers],
+        'L0': L0,
+        'frame_time': frame_time,
+    }
+
+
 def circular_aperture(grid, diameter, center=(0.0, 0.0)):
     """1 inside the circle of ``diameter`` (boundary inclusive), else 0, as in generic.py:31-44."""
     x, y = grid.points_list()

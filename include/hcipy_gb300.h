@@ -58,6 +58,10 @@ extern "C" {
 #define HX_PREC_FP32 0  /* FP32 CUDA-core complex GEMM (HX_C64) or FP64 (HX_C128) */
 #define HX_PREC_SPLIT 1 /* split-operand tensor-core GEMM on tcgen05 */
 
+/* Tile policy of a plan's GEMMs (no counterpart in the reference). */
+#define HX_SCHEDULE_LATENCY 0    /* fill the GPU with this transform alone (splits K for small shapes) */
+#define HX_SCHEDULE_THROUGHPUT 1 /* other transforms run beside it: least SM time, no K split */
+
 /* Message of the last failure on this thread ("" if none). */
 HX_API const char* hx_last_error(void);
 /* Library version as major*10000 + minor*100 + patch. */
@@ -165,6 +169,12 @@ HX_API int hx_lyot_execute(const hx_mft_plan* fpm_plan, const hx_mft_plan* img_p
  * HX_ERR_TIMEOUT when a wait of the tensor-core GEMM gave up (its CTA then
  * returned without writing).  Synchronizes with the device; reset != 0 clears it. */
 HX_API int hx_mft_plan_status(const hx_mft_plan* plan, int reset);
+
+/* Tile policy of the plan's GEMMs, HX_SCHEDULE_LATENCY (default) or HX_SCHEDULE_THROUGHPUT, for plans whose
+ * transforms run concurrently with others (several streams, or parallel branches of a CUDA graph): small
+ * transforms then take the tile with the least SM time instead of splitting K to fill the GPU alone, and the
+ * autotuner's measurements are ranked by duration x occupied SMs.  FP32 plans accept and ignore it. */
+HX_API int hx_mft_plan_set_schedule(hx_mft_plan* plan, int schedule);
 
 /* Tile autotuner of the split tensor-core GEMMs (process-wide; no counterpart in the reference).  When on,
  * the first execution of each GEMM shape times every candidate tile (64 or 128 output columns, with and
@@ -318,6 +328,12 @@ HX_API int hx_atmosphere_extrude(void* ring, int ny, int nx, int row0, int col0,
  * taps are host arrays of 7 float64). */
 HX_API int hx_atmosphere_shift(const void* ring, int ny, int nx, int row0, int col0, const double* taps_row,
                                const double* taps_col, void* out, int dtype, void* stream);
+/* out (n) = the sum of count (1..8) screens of n HX_F32 or HX_F64 values; screens is a host array of device
+ * pointers.  The phase of layers applied in sequence without propagation between them
+ * (MultiLayerAtmosphere.forward with scintillation off, hcipy/atmosphere/atmospheric_model.py:264-280) is the
+ * phase of this sum, so one phase application replaces one per layer. */
+HX_API int hx_atmosphere_combine(const void* const* screens, int count, long long n, void* out, int dtype,
+                                 void* stream);
 
 #ifdef __cplusplus
 }

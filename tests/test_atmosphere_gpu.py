@@ -126,3 +126,67 @@ def test_layer_full_size_extrusion_matches_oracle():
         screen = oatm.extrude(screen, (1024, 1024), where, a, b, idx, noise)
         layer._extrude(where, torch.from_numpy(noise).cuda())
     assert rel_err(layer.achromatic_screen.numpy(), screen) < 1e-12
+
+
+class _StaticLayer(hg.AtmosphericLayer):
+    """A layer whose screen is a fixed device tensor (radians at 1 m)."""
+
+    def __init__(self, grid, screen):
+        hg.AtmosphericLayer.__init__(self, grid, 1.0)
+        self._s = screen
+
+    def _screen_tensor(self):
+        return self._s
+
+
+def test_multilayer_combined_screen_sums_the_layers():
+    """hx_atmosphere_combine: three screens summed in layer order equal torch's left-to-right sum exactly; ten
+    screens take two launches (8, then 2 more plus the running sum) and agree to rounding; float64 too."""
+    grid = hg.make_pupil_grid(40, 1.0)
+    gen = torch.Generator(device='cuda').manual_seed(4)
+    for dtype in (torch.float32, torch.float64):
+        s = [torch.randn(grid.size, device='cuda', dtype=dtype, generator=gen) for _ in range(10)]
+        atm3 = hg.MultiLayerAtmosphere([_StaticLayer(grid, x) for x in s[:3]])
+        assert torch.equal(atm3.combined_screen(), s[0] + s[1] + s[2])
+        atm10 = hg.MultiLayerAtmosphere([_StaticLayer(grid, x) for x in s])
+        ref = torch.stack(s).double().sum(0)
+        tol = 1e-6 if dtype == torch.float32 else 1e-14
+        assert rel_err(atm10.combined_screen().double().cpu().numpy(), ref.cpu().numpy()) < tol
+    odd = hg.make_pupil_grid(13, 1.0)  # 169 values: the last thread takes the scalar tail
+    s = [torch.randn(odd.size, device='cuda', generator=gen) for _ in range(2)]
+    assert torch.equal(hg.MultiLayerAtmosphere([_StaticLayer(odd, x) for x in s]).combined_screen(), s[0] + s[1])
+
+
+def test_multilayer_float32_forward_and_tracking():
+    """Three float32 infinite layers: one phase application of the summed screen equals the reference's
+    layer-by-layer products to float32 rounding of the phase; the sum follows a layer evolved on its own and
+    keeps its address (a captured graph stays valid), also across reset()."""
+    grid = hg.make_pupil_grid(48, 2.0)
+    layers = [hg.InfiniteAtmosphericLayer(grid, hg.Cn_squared_from_fried_parameter(r0, 500e-9), L0=20,
+                                          velocity=v, seed=7 + i, dtype=torch.float32)
+              for i, (r0, v) in enumerate(((0.1, (10.0, 0.0)), (0.2, (-7.5, 13.0)), (0.3, (-12.5, -21.7))))]
+    atm = hg.MultiLayerAtmosphere(layers)
+    atm.evolve_until(0.01)
+    wl = 700e-9
+    rng = np.random.default_rng(2)
+    e = (rng.standard_normal(grid.size) + 1j * rng.standard_normal(grid.size)).astype(np.complex64)
+    wf = hg.Wavefront(hg.Field(torch.from_numpy(e).cuda(), grid), wl)
+    seq = wf
+    for layer in layers:
+        seq = layer.forward(seq)
+    out = atm.forward(wf).electric_field.numpy()
+    phase = sum(layer.phase_for(wl).numpy().astype(np.float64) for layer in layers)
+    assert np.max(np.abs(phase)) > 1.0  # a phase large enough for its rounding to show
+    assert rel_err(out, seq.electric_field.numpy()) < 2e-5
+    assert rel_err(out, e * np.exp(1j * phase)) < 2e-5
+    buf = atm.combined_screen()
+    before = buf.clone()
+    layers[2].evolve_until(0.03)
+    after = atm.combined_screen()
+    assert after.data_ptr() == buf.data_ptr() and not torch.equal(after, before)
+    expect = layers[0]._screen_tensor() + layers[1]._screen_tensor() + layers[2]._screen_tensor()
+    assert torch.equal(after, expect)
+    ptrs = [layer._shifted.data_ptr() for layer in layers]
+    atm.reset()
+    assert [layer._shifted.data_ptr() for layer in layers] == ptrs
+    assert atm.combined_screen().data_ptr() == buf.data_ptr()

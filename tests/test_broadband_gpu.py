@@ -68,3 +68,36 @@ def test_graph_with_atmosphere_and_autotuner():
         assert any(not torch.equal(a, b) for a, b in zip(first, second))
     finally:
         _lib.autotune(False)
+
+
+def test_broadband_through_multilayer_atmosphere():
+    """The broadband workload's form at a small size: three float32 layers ahead of uneven focal grids, the
+    graph captured once and replayed per frame after the layers evolve; each replay equals the direct call and,
+    at every wavelength, the float64 oracle on the field the device propagated."""
+    from hcipy_gb300 import workloads
+    from hcipy_gb300.kernels import apply_phase
+    w = workloads.broadband_turbulence_workload(pupil_n=96, diameter=2.0, num_wavelengths=5, q=3.3, num_airy=8)
+    pupil, wls, grids = w['pupil'], w['wavelengths'], w['focal_grids']
+    assert len({int(g.dims[0]) for g in grids}) > 1
+    layers = [hg.InfiniteAtmosphericLayer(pupil, hg.Cn_squared_from_fried_parameter(lay['r0'], 500e-9),
+                                          L0=w['L0'], velocity=lay['velocity'], seed=3 + i, dtype=torch.float32)
+              for i, lay in enumerate(w['layers'])]
+    atm = hg.MultiLayerAtmosphere(layers)
+    ap = torch.from_numpy(w['aperture'].astype(np.complex64)).cuda()
+    for precision, tol in (('fp32', 3e-6), ('split', 2e-8)):
+        atm.reset()
+        imager = hg.BroadbandImager(pupil, wls, grids, focal_length=w['focal_length'], precision=precision,
+                                    pre=atm.forward).capture(ap)
+        assert imager.graph_kernels >= 2 * len(wls)
+        t = 0.0
+        for _ in range(3):
+            t += 4 * w['frame_time']
+            atm.evolve_until(t)
+            replayed = [x.clone() for x in imager.replay(ap)]
+            direct = imager(ap)
+            for a, b in zip(replayed, direct):
+                assert torch.equal(a, b)
+        for wl, g, img in zip(wls, grids, replayed):
+            e = apply_phase(ap, atm.combined_screen(), 1.0 / wl).cpu().numpy().astype(np.complex128)
+            ref = ooptics.fraunhofer_forward(e, _og(pupil), _og(g), wavelength=wl, focal_length=w['focal_length'])
+            assert rel_err(img.cpu().numpy(), ref) < tol, (precision, wl, rel_err(img.cpu().numpy(), ref))

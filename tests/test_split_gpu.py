@@ -149,3 +149,28 @@ def test_split_complex128_wide_range():
         ref = ofourier.mft_forward(e[i], xg, xg, ug, ug, gi.weights)
         assert rel_err(out[i], ref) < 2e-8, (scales[i], rel_err(out[i], ref))
     assert split._plan(torch.complex64).status() == 0
+
+
+def test_split_throughput_schedule_all_directions():
+    """The throughput tile policy (no K split, least padded tile) on a shape that the latency policy splits:
+    forward, backward and adjoint against float64, and switching the schedule of an existing plan."""
+    pupil = hg.make_pupil_grid(256, 1.0)
+    focal = hg.make_focal_grid(3.7, 19)  # 140^2: the throughput policy takes 112-column tiles
+    rng = np.random.default_rng(8)
+    e = (rng.standard_normal(pupil.size) + 1j * rng.standard_normal(pupil.size)).astype(np.complex64)
+    f = (rng.standard_normal(focal.size) + 1j * rng.standard_normal(focal.size)).astype(np.complex64)
+    x, y = pupil.separated_coords
+    u, v = focal.separated_coords
+    ref_f = ofourier.mft_forward(e.astype(complex), x, y, u, v, pupil.weights)
+    ref_b = ofourier.mft_backward(f.astype(complex), x, y, u, v, focal.weights)
+    ref_a = ofourier.mft_adjoint(f.astype(complex), x, y, u, v, pupil.weights)
+    mft = hg.MatrixFourierTransform(pupil, focal, precision='split', schedule='throughput')
+    et, ft = torch.from_numpy(e).cuda(), torch.from_numpy(f).cuda()
+    assert rel_err(mft.forward(et).numpy(), ref_f) < 2e-8
+    assert rel_err(mft.backward(ft).numpy(), ref_b) < 2e-8
+    assert rel_err(mft.adjoint(ft).numpy(), ref_a) < 2e-8
+    mft.schedule = 'latency'
+    assert rel_err(mft.forward(et).numpy(), ref_f) < 2e-8
+    assert mft._plan(torch.complex64).status() == 0
+    with pytest.raises(ValueError):
+        mft.schedule = 'fastest'
