@@ -20,8 +20,12 @@ namespace {
 
 using cd = std::complex<double>;
 
-std::vector<int> factor_radices(int n) {
+// Radices of a length-n transform, largest first.  allow16: radix 16 for power-of-two factors (float lines, whose
+// threads hold 16 points: one 16-point butterfly per thread and stage).
+std::vector<int> factor_radices(int n, bool allow16 = false) {
     std::vector<int> r;
+    if (allow16 && (n & (n - 1)) == 0)
+        while (n % 16 == 0 && n > 1) { r.push_back(16); n /= 16; }
     while (n % 8 == 0 && n > 1) { r.push_back(8); n /= 8; }
     while (n % 4 == 0) { r.push_back(4); n /= 4; }
     while (n % 2 == 0) { r.push_back(2); n /= 2; }
@@ -87,12 +91,12 @@ int launch_shape(int M, const std::vector<int>& radices, int nlines, int batch, 
     a.pitch = lpc > 1 ? M + 1 : M;
     a.M = M;
     a.nstages = (int)radices.size();
-    if (a.nstages > 16) {
+    if (a.nstages > 12) {
         set_error("internal: %d FFT stages", a.nstages);
         return HX_ERR_UNSUPPORTED;
     }
     a.radix_code = 0;
-    for (size_t i = 0; i < radices.size(); ++i) a.radix_code |= (unsigned long long)radices[i] << (4 * i);
+    for (size_t i = 0; i < radices.size(); ++i) a.radix_code |= (unsigned long long)radices[i] << (5 * i);
     *threads = thr;
     *smem = (size_t)smem_elems(lpc * a.pitch) * sizeof(typename cplx<T>::type);
     return HX_OK;
@@ -129,8 +133,8 @@ template <typename T>
 int run_line(const LineArgs<T>& a, int threads, size_t smem, int sign, bool conv, int batch, cudaStream_t s) {
     bool mixed = false;
     unsigned long long code = a.radix_code;
-    for (int i = 0; i < a.nstages; ++i, code >>= 4) {
-        const int r = (int)(code & 15ull);
+    for (int i = 0; i < a.nstages; ++i, code >>= 5) {
+        const int r = (int)(code & 31ull);
         if (r == 3 || r == 5 || r == 7) mixed = true;
     }
     return mixed ? run_line_m<T, true>(a, threads, smem, sign, conv, batch, s)
@@ -246,15 +250,16 @@ struct AxisTables {
 
 template <typename T>
 int make_axis(AxisTables& ax, int N, cudaStream_t s) {
+    constexpr bool r16 = sizeof(T) == 4;
     ax.N = N;
-    ax.radices = factor_radices(N);
+    ax.radices = factor_radices(N, r16);
     if (!ax.radices.empty()) {
         ax.M = N;
         return make_twiddles<T>(ax.tw, N, s);
     }
     ax.bluestein = true;
     ax.M = next_pow2(2 * N - 1);
-    ax.radices = factor_radices(ax.M);
+    ax.radices = factor_radices(ax.M, r16);
     HX_TRY(make_twiddles<T>(ax.tw, ax.M, s));
     std::vector<cd> b(N);
     for (int n = 0; n < N; ++n) {
@@ -809,7 +814,7 @@ int hx_czt_plan_create(int n, int m, double w_re, double w_im, double a_re, doub
     p->m = m;
     p->dtype = dtype;
     p->M = hx::next_pow2(n + m - 1);
-    p->radices = hx::factor_radices(p->M);
+    p->radices = hx::factor_radices(p->M, dtype == HX_C64);
     p->esize = dtype == HX_C64 ? sizeof(float2) : sizeof(double2);
     if (p->M > hx::max_points<double>(false)) {
         delete p;

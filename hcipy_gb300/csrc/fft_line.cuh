@@ -37,7 +37,7 @@ struct LineArgs {
     int lines_per_cta;
     int pitch;            // shared-memory stride between lines (>= M)
     int nstages;
-    unsigned long long radix_code;  // radix of stage s in bits [4s, 4s+4)
+    unsigned long long radix_code;  // radix of stage s in bits [5s, 5s+5)
     const Cx* tw;         // M entries, exp(-2 pi i t / M)
     // load
     const Cx* in;
@@ -144,6 +144,73 @@ struct Dft<T, 8, SIGN> {
             v[2 * m] = a[m];
             v[2 * m + 1] = b[m];
         }
+    }
+};
+
+// z times exp(SIGN 2 pi i m / 16).
+template <typename T, int SIGN, int MM>
+__device__ __forceinline__ typename cplx<T>::type w16(typename cplx<T>::type z) {
+    constexpr int m = MM % 16;
+    if constexpr (m == 0) {
+        return z;
+    } else if constexpr (m == 4) {
+        return c_rot<SIGN>(z);
+    } else if constexpr (m == 8) {
+        return c_scale(z, T(-1));
+    } else if constexpr (m == 12) {
+        return c_rot<-SIGN>(z);
+    } else {
+        // cos and sin of 2 pi m / 16 = m pi / 8 from cos(pi/8), sin(pi/8) and cos(pi/4)
+        constexpr double c8 = 0.92387953251128675613, s8 = 0.38268343236508977173, h = 0.70710678118654752440;
+        constexpr double cs = m == 1 ? c8 : m == 2 ? h : m == 3 ? s8 : m == 5 ? -s8 : m == 6 ? -h : m == 7 ? -c8
+                            : m == 9 ? -c8 : m == 10 ? -h : m == 11 ? -s8 : m == 13 ? s8 : m == 14 ? h : c8;
+        constexpr double sn = m == 1 ? s8 : m == 2 ? h : m == 3 ? c8 : m == 5 ? c8 : m == 6 ? h : m == 7 ? s8
+                            : m == 9 ? -s8 : m == 10 ? -h : m == 11 ? -c8 : m == 13 ? -c8 : m == 14 ? -h : -s8;
+        const T c = T(cs), sg = T(SIGN * sn);
+        typename cplx<T>::type r;
+        r.x = c * z.x - sg * z.y;
+        r.y = c * z.y + sg * z.x;
+        return r;
+    }
+}
+
+// 16 points as 4 x 4: n = 4 n1 + n2, k = k1 + 4 k2; four 4-point DFTs over n1 (in place: slot n2 + 4 k1), the
+// twiddles W16^(n2 k1), four 4-point DFTs over n2 (slots 4 k1 + k2), and the transposition k1 + 4 k2 <- 4 k1 + k2
+// as a renaming of registers.
+template <typename T, int SIGN>
+struct Dft<T, 16, SIGN> {
+    template <typename Cx>
+    __device__ __forceinline__ static void dft4_at(Cx* v, int i0, int st) {
+        Cx t[4] = {v[i0], v[i0 + st], v[i0 + 2 * st], v[i0 + 3 * st]};
+        Dft<T, 4, SIGN>::run(t);
+        v[i0] = t[0];
+        v[i0 + st] = t[1];
+        v[i0 + 2 * st] = t[2];
+        v[i0 + 3 * st] = t[3];
+    }
+    template <typename Cx>
+    __device__ __forceinline__ static void run(Cx* v) {
+#pragma unroll
+        for (int n2 = 0; n2 < 4; ++n2) dft4_at(v, n2, 4);
+        v[5] = w16<T, SIGN, 1>(v[5]);
+        v[9] = w16<T, SIGN, 2>(v[9]);
+        v[13] = w16<T, SIGN, 3>(v[13]);
+        v[6] = w16<T, SIGN, 2>(v[6]);
+        v[10] = w16<T, SIGN, 4>(v[10]);
+        v[14] = w16<T, SIGN, 6>(v[14]);
+        v[7] = w16<T, SIGN, 3>(v[7]);
+        v[11] = w16<T, SIGN, 6>(v[11]);
+        v[15] = w16<T, SIGN, 9>(v[15]);
+#pragma unroll
+        for (int k1 = 0; k1 < 4; ++k1) dft4_at(v, 4 * k1, 1);
+        // v[4 k1 + k2] holds X[k1 + 4 k2]
+        Cx x[16];
+#pragma unroll
+        for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+            for (int k2 = 0; k2 < 4; ++k2) x[k1 + 4 * k2] = v[4 * k1 + k2];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) v[k] = x[k];
     }
 };
 
@@ -284,11 +351,37 @@ __device__ __forceinline__ void fft_stage(typename cplx<T>::type* buf, int M, in
             const int base = line * pitch;
 #pragma unroll
             for (int r = 0; r < R; ++r) v[i][r] = buf[sidx(base + j + r * nb)];
+            if constexpr (R == 16) {
+                // W^r for r < 16 from four table entries W, W^2, W^4, W^8 (at most three products deep).
+                const int ks = k * stride;
+                Cx w1 = tw[ks], w2 = tw[2 * ks], w4 = tw[4 * ks], w8 = tw[8 * ks];
+                if (SIGN > 0) {
+                    w1.y = -w1.y;
+                    w2.y = -w2.y;
+                    w4.y = -w4.y;
+                    w8.y = -w8.y;
+                }
+                const Cx w3 = c_mul(w2, w1);
+                Cx wl[8];
+                wl[1] = w1;
+                wl[2] = w2;
+                wl[3] = w3;
+                wl[4] = w4;
+                wl[5] = c_mul(w4, w1);
+                wl[6] = c_mul(w4, w2);
+                wl[7] = c_mul(w4, w3);
 #pragma unroll
-            for (int r = 1; r < R; ++r) {
-                Cx w = tw[r * k * stride];
-                if (SIGN > 0) w.y = -w.y;
-                v[i][r] = c_mul(v[i][r], w);
+                for (int r = 1; r < 8; ++r) v[i][r] = c_mul(v[i][r], wl[r]);
+                v[i][8] = c_mul(v[i][8], w8);
+#pragma unroll
+                for (int r = 1; r < 8; ++r) v[i][8 + r] = c_mul(v[i][8 + r], c_mul(w8, wl[r]));
+            } else {
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    Cx w = tw[r * k * stride];
+                    if (SIGN > 0) w.y = -w.y;
+                    v[i][r] = c_mul(v[i][r], w);
+                }
             }
             Dft<T, R, SIGN>::run(v[i]);
             dst[i] = base + jd * Ns * R + k;
@@ -311,8 +404,15 @@ __device__ __forceinline__ void fft_smem(typename cplx<T>::type* buf, const Line
     unsigned long long code = a.radix_code;
 #pragma unroll 1
     for (int s = 0; s < a.nstages; ++s) {
-        const int R = (int)(code & 15ull);
-        code >>= 4;
+        const int R = (int)(code & 31ull);
+        code >>= 5;
+        if constexpr (!MIXED && sizeof(T) == 4) {
+            if (R == 16) {
+                fft_stage<T, 16, SIGN, false>(buf, a.M, a.pitch, lines, Ns, a.tw);
+                Ns *= R;
+                continue;
+            }
+        }
         if (R == 8) fft_stage<T, 8, SIGN, MIXED>(buf, a.M, a.pitch, lines, Ns, a.tw);
         else if (R == 4) fft_stage<T, 4, SIGN, MIXED>(buf, a.M, a.pitch, lines, Ns, a.tw);
         else if (R == 2) fft_stage<T, 2, SIGN, MIXED>(buf, a.M, a.pitch, lines, Ns, a.tw);
