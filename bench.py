@@ -48,6 +48,7 @@ def parse_args():
     p.add_argument('--grad-steps', type=int, default=20, help='timed DM-gradient steps (0: skip that leg)')
     p.add_argument('--no-atmosphere', action='store_true', help='skip the atmospheric-layer leg')
     p.add_argument('--no-graph', action='store_true', help='launch the step from Python instead of a CUDA graph')
+    p.add_argument('--no-small', action='store_true', help='skip the 256^2 Fraunhofer and the FFT-family legs')
     p.add_argument('--broadband-frames', type=int, default=256,
                    help='frames of the broadband-through-turbulence leg (0: skip it)')
     return p.parse_args()
@@ -365,7 +366,7 @@ def run_atmosphere(args, dev, peaks):
 def run_broadband(args, dev, peaks):
     """Broadband imaging through turbulence: 21 wavelengths over 20 % bandwidth, each on its own diffraction-scaled
     focal grid (284^2 ... 232^2, q=4, 32 lambda0/lambda), a 1024^2 pupil of 8 m behind three float32 infinite
-    layers (r0 0.1/0.2/0.3 m, L0 25 m, winds 10/15/25 m/s in three directions), 1 ms frames.  A frame evolves the
+    layers (r0 0.1/0.2/0.3 m, L0 25 m, winds 10/15/25 m/s along x, seeds 5/6/7), 1 ms frames.  A frame evolves the
     layers (extrusions with host-drawn noise, quintic shifts, the summed screen) and replays one CUDA graph that
     holds, per wavelength, the phase of the summed screen and the matrix Fourier transform onto that wavelength's
     grid; the split GEMMs run with the tiles the autotuner picked during the capture's warm-up."""
@@ -376,8 +377,8 @@ def run_broadband(args, dev, peaks):
     pupil, wls, grids = w['pupil'], w['wavelengths'], w['focal_grids']
     t0 = time.perf_counter()
     layers = [hg.InfiniteAtmosphericLayer(pupil, hg.Cn_squared_from_fried_parameter(lay['r0'], 500e-9), L0=w['L0'],
-                                          velocity=lay['velocity'], seed=21 + i, dtype=torch.float32)
-              for i, lay in enumerate(w['layers'])]
+                                          velocity=lay['velocity'], seed=lay['seed'], dtype=torch.float32)
+              for lay in w['layers']]
     atm = hg.MultiLayerAtmosphere(layers)
     init_s = time.perf_counter() - t0
     ap = torch.from_numpy(w['aperture'].astype(np.complex64)).to(dev)
@@ -468,7 +469,8 @@ def run_broadband(args, dev, peaks):
     cpu_s_per_prop = spent / n_done
     return {
         'workload': '21 wavelengths over 20%% bandwidth, focal grids %d^2..%d^2 (q=4, 32 lambda0/lambda), 1024^2 '
-                    'pupil of 8 m, 3 float32 infinite layers (r0 0.1/0.2/0.3 m, L0 25 m, 10/15/25 m/s), 1 ms '
+                    'pupil of 8 m, 3 float32 infinite layers (r0 0.1/0.2/0.3 m, L0 25 m, 10/15/25 m/s along x, seeds '
+                    '5/6/7), 1 ms '
                     'frames, %d frames' % (int(grids[0].dims[0]), int(grids[-1].dims[0]), frames),
         'fp32': legs['fp32'], 'split': legs['split'],
         'split_over_fp32': legs['split']['frames_per_s'] / legs['fp32']['frames_per_s'],
@@ -482,6 +484,129 @@ def run_broadband(args, dev, peaks):
                          'sample': '%d of the 21 wavelengths: phase + two complex128 numpy GEMMs with precomputed '
                                    'matrices (matrix construction not timed)' % n_done},
     }
+
+
+def run_small_fraunhofer(args, dev, peaks):
+    """A 256^2 pupil (Zernike 2-21 at 0.1 rad RMS) onto a 128^2 focal grid (q=4, num_airy=16): 12,582,912 complex
+    MACs per propagation, a launch-latency-bound size.  Propagations/s through FraunhoferPropagator.forward with
+    Python launches and replayed from a CUDA graph of 64 propagations, FP32 and split precision."""
+    import torch
+    import hcipy_gb300 as hg
+    from hcipy_gb300 import workloads
+    from oracle import optics
+    w = workloads.fraunhofer_workload()
+    pupil, focal = w['pupil'], w['focal']
+    e = torch.from_numpy(w['E'].astype(np.complex64)).to(dev)
+    ref = optics.fraunhofer_forward(w['E'].astype(np.complex64).astype(np.complex128), oracle_grid(pupil),
+                                    oracle_grid(focal))
+    nx, ny = (int(d) for d in pupil.dims)
+    cmacs = workloads.mft_complex_macs(nx, ny, int(focal.dims[0]), int(focal.dims[1]))
+    out = {'workload': '256^2 pupil, Zernike 2-21 at 0.1 rad RMS -> 128^2 focal grid (q=4, num_airy=16)',
+           'complex_macs': int(cmacs)}
+    for precision in ('fp32', 'split'):
+        prop = hg.FraunhoferPropagator(pupil, focal, precision=precision)
+        wf = hg.Wavefront(hg.Field(e, pupil), 1.0)
+        for _ in range(5):
+            img = prop.forward(wf).electric_field.data
+        torch.cuda.synchronize()
+        n = 200
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record()
+        for _ in range(n):
+            prop.forward(wf)
+        ev[1].record()
+        ev[1].synchronize()
+        py_us = ev[0].elapsed_time(ev[1]) / n * 1e3
+        graph = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            prop.forward(wf)
+        torch.cuda.current_stream().wait_stream(side)
+        per_graph = 64
+        with torch.cuda.graph(graph):
+            for _ in range(per_graph):
+                prop.forward(wf)
+        graph.replay()
+        torch.cuda.synchronize()
+        reps = 10
+        ev[2].record()
+        for _ in range(reps):
+            graph.replay()
+        ev[3].record()
+        ev[3].synchronize()
+        g_us = ev[2].elapsed_time(ev[3]) / (reps * per_graph) * 1e3
+        err = float(np.linalg.norm(img.cpu().numpy() - ref) / np.linalg.norm(ref))
+        out[precision] = {'propagations_per_s_python': 1e6 / py_us, 'propagations_per_s_graph': 1e6 / g_us,
+                          'us_per_propagation_graph': g_us, 'tflops_graph': 8 * cmacs / (g_us * 1e-6) / 1e12,
+                          'rel_err_vs_fp64': err}
+    from oracle import fourier
+    x, y = pupil.separated_coords
+    uv = oracle_grid(focal)
+    m1, m2 = fourier.mft_matrices(x, y, *uv.separated_coords)
+    e_h = w['E'].astype(np.complex64).reshape(ny, nx)
+    m1, m2 = m1.astype(np.complex64), m2.astype(np.complex64)
+    k, c0 = 0, time.perf_counter()
+    while k < 20 or time.perf_counter() - c0 < 1.0:
+        m1 @ (e_h @ m2)
+        k += 1
+    out['cpu_baseline'] = {'propagations_per_s': k / (time.perf_counter() - c0), 'cores': host_cores(), 'kind': 'port',
+                           'sample': '%d propagations, complex64 numpy GEMMs with precomputed matrices' % k}
+    return out
+
+
+def run_fft_family(args, dev, peaks):
+    """A 1024^2 pupil of 8 m behind a von Karman screen (r0 0.15 m, L0 20 m) at 1.6 um: the zero-padded FFT to
+    4096^2 (q=4) and angular-spectrum propagation over 0.5 m and 5 m (2048^2 padded).  Per-call time with CUDA
+    events, the line-FFT passes bracketed by events on their stream, and the HBM rate of the algorithmic bytes
+    (input + output, complex64)."""
+    import torch
+    import hcipy_gb300 as hg
+    from hcipy_gb300 import _lib, workloads
+    w = workloads.turbulent_pupil_workload()
+    pupil = w['pupil']
+    e = torch.from_numpy(w['E'].astype(np.complex64)).to(dev)
+    hbm = peaks.get('hbm_gbs', 6800.0)
+    fft = hg.FastFourierTransform(pupil, q=4, fov=1)
+    wf = hg.Wavefront(hg.Field(e, pupil), w['wavelength'])
+    cases = [('fft_1024_to_4096', lambda: fft.forward(e), 8 * (pupil.size + fft.output_grid.size))]
+    for d in (0.5, 5.0):
+        asp = hg.AngularSpectrumPropagator(pupil, d)
+        cases.append(('asp_%gm' % d, (lambda a: lambda: a.forward(wf))(asp), 8 * 2 * pupil.size))
+    out = {'workload': '1024^2 pupil of 8 m, von Karman r0 0.15 m, L0 20 m, lambda 1.6 um; padded FFT q=4 -> 4096^2; '
+                       'angular spectrum 0.5 m and 5 m (2048^2 padded)'}
+    for name, fn, nbytes in cases:
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        n = 20
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        _lib.trace_read(_lib.HX_TRACE_FFT, reset=True)
+        _lib.trace_enable(True)
+        e0.record()
+        for _ in range(n):
+            fn()
+        e1.record()
+        e1.synchronize()
+        _lib.trace_enable(False)
+        k, ms, _ = _lib.trace_read(_lib.HX_TRACE_FFT, reset=True)
+        call_us = e0.elapsed_time(e1) / n * 1e3
+        pass_us = ms / n * 1e3
+        out[name] = {'us_per_call': call_us, 'pass_us_per_call': pass_us, 'passes_per_call': k // n,
+                     'algorithmic_bytes': int(nbytes), 'GBps': nbytes / (pass_us * 1e-6) / 1e9,
+                     'frac_of_hbm': nbytes / (pass_us * 1e-6) / 1e9 / hbm}
+    # accuracy of the padded FFT against the float64 oracle
+    from oracle import fourier
+    plan = fourier.FFTPlan(oracle_grid(pupil), 4, 1)
+    ref = plan.forward(w['E'].astype(np.complex64).astype(np.complex128))
+    got = fft.forward(e).numpy()
+    out['fft_1024_to_4096']['rel_err_vs_fp64'] = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+    c0 = time.perf_counter()
+    plan.forward(w['E'])
+    out['cpu_baseline'] = {'fft_1024_to_4096_ms': (time.perf_counter() - c0) * 1e3, 'cores': 1, 'kind': 'port',
+                           'sample': 'one padded FFT, numpy pocketfft on complex128 (the reference pads in complex128)'}
+    out['peak_note'] = 'hbm_gbs of measured' if 'hbm_gbs' in peaks else 'fallback'
+    return out
 
 
 def max_over_ranks(value, dist, device):
@@ -711,6 +836,9 @@ def run_ours(args, rank, world, dist):
         line['atmosphere'] = run_atmosphere(args, dev, peaks)
     if args.broadband_frames > 0:
         line['broadband_turbulence'] = run_broadband(args, dev, peaks)
+    if not args.no_small:
+        line['fraunhofer_256'] = run_small_fraunhofer(args, dev, peaks)
+        line['fft_family_1024'] = run_fft_family(args, dev, peaks)
     print(json.dumps(line), flush=True)
 
 

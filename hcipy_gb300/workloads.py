@@ -21,14 +21,14 @@ def mft_complex_macs(nx, ny, nu, nv):
 
 def broadband_turbulence_workload(pupil_n=1024, diameter=8.0, num_wavelengths=21, bandwidth=0.2, q=4,
                                   num_airy=32, reference_wavelength=500e-9,
-                                  layers=((0.1, 10.0, 0.0), (0.2, 15.0, 120.0), (0.3, 25.0, 240.0)), L0=25.0,
+                                  layers=((0.1, 10.0, 0.0, 5), (0.2, 15.0, 0.0, 6), (0.3, 25.0, 0.0, 7)), L0=25.0,
                                   frame_time=1e-3):  # noqa: N803
     """Broadband imaging through a three-layer frozen-flow atmosphere.
 
     A ``pupil_n``^2 pupil of ``diameter`` meters; ``num_wavelengths`` wavelengths spanning ``bandwidth`` around
     ``reference_wavelength``, each imaged on its own diffraction-scaled focal grid (q samples per
     lambda0/D, num_airy lambda0/lambda radius, in lambda0/D units, so the focal length is D / lambda0); layers
-    given as (r0 in m at 500 nm, wind speed m/s, wind direction deg), outer scale ``L0`` m, frames
+    given as (r0 in m at 500 nm, wind speed m/s, wind direction deg, seed), outer scale ``L0`` m, frames
     ``frame_time`` s apart.  Returns the grids and parameters; the layers themselves are built by the caller
     (they need the GPU)."""
     from .broadband import diffraction_scaled_focal_grids
@@ -40,8 +40,8 @@ def broadband_turbulence_workload(pupil_n=1024, diameter=8.0, num_wavelengths=21
         'wavelengths': rel * reference_wavelength,
         'focal_grids': diffraction_scaled_focal_grids(q, num_airy, rel, 1.0),
         'focal_length': diameter / reference_wavelength,
-        'layers': [{'r0': r0, 'velocity': (v * math.cos(math.radians(a)), v * math.sin(math.radians(a)))}
-                   for r0, v, a in layers],
+        'layers': [{'r0': r0, 'velocity': (v * math.cos(math.radians(a)), v * math.sin(math.radians(a))),
+                    'seed': seed} for r0, v, a, seed in layers],
         'L0': L0,
         'frame_time': frame_time,
     }
@@ -113,6 +113,28 @@ def lyot_workload(pupil_n=2048, fpm_q=8, fpm_num_airy=32, occulter_radius=4.0, s
     stop = circular_aperture(pupil, stop_diameter)
     focal = make_focal_grid(final_q, final_num_airy)
     return dict(pupil=pupil, aperture=aperture, E=e, fpm_grid=fpm_grid, fpm=fpm, stop=stop, focal=focal)
+
+
+def fraunhofer_workload(pupil_n=256, q=4, num_airy=16, rms_rad=0.1, seed=0):
+    """Small Fraunhofer propagation: a ``pupil_n``^2 circular pupil with Zernike 2-21 aberrations at ``rms_rad`` RMS
+    (seed 0) onto a q=4, num_airy=16 focal grid (128^2)."""
+    pupil = make_pupil_grid(pupil_n, 1)
+    aperture = circular_aperture(pupil, 1.0)
+    e = aperture * np.exp(1j * zernike_phase(pupil, 1.0, 2, 21, rms_rad, seed))
+    return dict(pupil=pupil, aperture=aperture, E=e, focal=make_focal_grid(q, num_airy))
+
+
+def turbulent_pupil_workload(pupil_n=1024, diameter=8.0, r0=0.15, L0=20.0, wavelength=1.6e-6, seed=1):  # noqa: N803
+    """A ``pupil_n``^2 circular pupil of ``diameter`` m behind a von Karman phase screen (r0 at 500 nm, outer
+    scale L0) seen at ``wavelength``: the input of the padded-FFT and angular-spectrum workloads."""
+    from .atmosphere import Cn_squared_from_fried_parameter, von_karman_screen
+    pupil = make_pupil_grid(pupil_n, diameter)
+    aperture = circular_aperture(pupil, diameter)
+    rng = np.random.default_rng(seed)
+    screen = von_karman_screen(pupil_n, pupil_n, np.asarray(pupil.delta, np.float64),
+                               Cn_squared_from_fried_parameter(r0, 500e-9), L0, rng)
+    e = aperture * np.exp(1j * np.asarray(screen).ravel() / wavelength)
+    return dict(pupil=pupil, aperture=aperture, E=e, wavelength=wavelength)
 
 
 def dark_hole_mask(focal, r_in=3.0, r_out=15.0):
