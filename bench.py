@@ -48,6 +48,7 @@ def parse_args():
     p.add_argument('--grad-steps', type=int, default=20, help='timed DM-gradient steps (0: skip that leg)')
     p.add_argument('--no-atmosphere', action='store_true', help='skip the atmospheric-layer leg')
     p.add_argument('--no-graph', action='store_true', help='launch the step from Python instead of a CUDA graph')
+    p.add_argument('--no-autotune', action='store_true', help='built-in tile choice instead of measured tiles')
     p.add_argument('--no-small', action='store_true', help='skip the 256^2 Fraunhofer and the FFT-family legs')
     p.add_argument('--broadband-frames', type=int, default=256,
                    help='frames of the broadband-through-turbulence leg (0: skip it)')
@@ -243,7 +244,7 @@ def run_grad(args, dev):
         loss.backward()
         return loss, a.grad
 
-    hg.autotune(True)
+    hg.autotune(not args.no_autotune)
     for _ in range(3):
         step()
     torch.cuda.synchronize()
@@ -640,7 +641,9 @@ def run_ours(args, rank, world, dist):
         return prop.forward(lyot.forward(wf)).electric_field.data
 
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
-    hg.autotune(True)  # the warm-up measures the tile candidates of each GEMM shape once
+    # the warm-up measures the tile candidates of each GEMM shape once (not under a profiler, whose replays
+    # distort the timings: --no-autotune keeps the built-in tile choice)
+    hg.autotune(not args.no_autotune)
     for _ in range(max(args.warmup, 3)):
         img = step(e_dev)
     torch.cuda.synchronize()
@@ -807,7 +810,8 @@ def run_ours(args, rank, world, dist):
         'config': {'workload': 'lyot-coronagraph 2048^2 pupil -> 512^2 FPM grid -> 512^2 image (3 MFTs)',
                    'pupil': args.pupil, 'fpm_grid': int(fpm_grid.dims[0]), 'image': int(focal.dims[0]),
                    'batch': 1, 'precision': args.precision, 'field_dtype': 'complex64',
-                   'tiles': 'autotuned during the warm-up (hx_autotune)',
+                   'tiles': ('autotuned during the warm-up (hx_autotune)' if not args.no_autotune
+                             else 'built-in choice'),
                    'launch': 'CUDA graph of the step, replayed' if not args.no_graph else 'Python launches',
                    'l2': 'flushed between steps (256 MiB write outside the per-step events)',
                    'parallelism': 'replicas' if world > 1 else 'single-gpu'},

@@ -174,36 +174,60 @@ int cgemm_nn(int M, int N, int K, typename cplx<T>::type alpha,
              const typename cplx<T>::type* A, long long lda, long long strideA,
              const typename cplx<T>::type* B, long long ldb, long long strideB,
              typename cplx<T>::type* C, long long ldc, long long strideC,
-             int batch, cudaStream_t stream, Epilogue<typename cplx<T>::type> epi = {});
+             int batch, cudaStream_t stream, Epilogue<typename cplx<T>::type> epi = {}, bool throughput = false);
 
-template <>
-inline int cgemm_nn<float>(int M, int N, int K, float2 alpha, const float2* A, long long lda, long long sA,
-                           const float2* B, long long ldb, long long sB, float2* C, long long ldc, long long sC,
-                           int batch, cudaStream_t stream, Epilogue<float2> epi) {
-    constexpr int BM = 128, BN = 64, BK = 8, TM = 8, TN = 4;
+// Tile of C per CTA: the widest tile whose grid still gives every SM two CTAs, since a small transform on the
+// widest tile would leave most of the 152 SMs idle (a 256^2 -> 128^2 MFT is 4 CTAs of 128 x 64).  Narrow tiles
+// read more shared memory per FMA but occupy the GPU.  With throughput = true (concurrent transforms fill the GPU)
+// the widest tile is kept.
+inline int simt_tile_level(int M, int N, int batch, int levels, const int* bm, const int* bn) {
+    const long long want = 2LL * num_sms();
+    for (int l = 0; l < levels; ++l)
+        if ((long long)ceil_div(N, bn[l]) * ceil_div(M, bm[l]) * batch >= want) return l;
+    return levels - 1;
+}
+
+template <typename T, int BM, int BN, int BK, int TM, int TN>
+int launch_simt(int M, int N, int K, typename cplx<T>::type alpha, const typename cplx<T>::type* A, long long lda,
+                long long sA, const typename cplx<T>::type* B, long long ldb, long long sB,
+                typename cplx<T>::type* C, long long ldc, long long sC, int batch, cudaStream_t stream,
+                Epilogue<typename cplx<T>::type> epi) {
     dim3 grid(ceil_div(N, BN), ceil_div(M, BM), batch);
     if (grid.y > 65535u || batch > 65535) {
         set_error("cgemm: problem too large for one launch (M=%d, batch=%d)", M, batch);
         return HX_ERR_UNSUPPORTED;
     }
     TraceScope trace(HX_TRACE_SIMT_GEMM, (double)M * N * K * batch, stream);
-    cgemm_nn_simt<float, BM, BN, BK, TM, TN><<<grid, 256, 0, stream>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, epi);
-    return launch_status("cgemm_nn_simt<float>");
+    cgemm_nn_simt<T, BM, BN, BK, TM, TN><<<grid, 256, 0, stream>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc,
+                                                                   sC, epi);
+    return launch_status(sizeof(T) == 4 ? "cgemm_nn_simt<float>" : "cgemm_nn_simt<double>");
+}
+
+template <>
+inline int cgemm_nn<float>(int M, int N, int K, float2 alpha, const float2* A, long long lda, long long sA,
+                           const float2* B, long long ldb, long long sB, float2* C, long long ldc, long long sC,
+                           int batch, cudaStream_t stream, Epilogue<float2> epi, bool throughput) {
+    static const int bm[3] = {128, 64, 32}, bn[3] = {64, 32, 32};
+    switch (throughput ? 0 : simt_tile_level(M, N, batch, 3, bm, bn)) {
+        case 0: return launch_simt<float, 128, 64, 8, 8, 4>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, batch,
+                                                             stream, epi);
+        case 1: return launch_simt<float, 64, 32, 8, 4, 2>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, batch,
+                                                           stream, epi);
+        default: return launch_simt<float, 32, 32, 8, 2, 2>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, batch,
+                                                            stream, epi);
+    }
 }
 
 template <>
 inline int cgemm_nn<double>(int M, int N, int K, double2 alpha, const double2* A, long long lda, long long sA,
                             const double2* B, long long ldb, long long sB, double2* C, long long ldc, long long sC,
-                            int batch, cudaStream_t stream, Epilogue<double2> epi) {
-    constexpr int BM = 64, BN = 64, BK = 8, TM = 4, TN = 4;
-    dim3 grid(ceil_div(N, BN), ceil_div(M, BM), batch);
-    if (grid.y > 65535u || batch > 65535) {
-        set_error("zgemm: problem too large for one launch (M=%d, batch=%d)", M, batch);
-        return HX_ERR_UNSUPPORTED;
-    }
-    TraceScope trace(HX_TRACE_SIMT_GEMM, (double)M * N * K * batch, stream);
-    cgemm_nn_simt<double, BM, BN, BK, TM, TN><<<grid, 256, 0, stream>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, epi);
-    return launch_status("cgemm_nn_simt<double>");
+                            int batch, cudaStream_t stream, Epilogue<double2> epi, bool throughput) {
+    static const int bm[2] = {64, 32}, bn[2] = {64, 32};
+    if (throughput || simt_tile_level(M, N, batch, 2, bm, bn) == 0)
+        return launch_simt<double, 64, 64, 8, 4, 4>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, batch, stream,
+                                                    epi);
+    return launch_simt<double, 32, 32, 8, 2, 2>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, batch, stream,
+                                                epi);
 }
 
 }  // namespace hx

@@ -52,6 +52,19 @@ inline int launch_status(const char* what) {
 
 inline unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
+// SMs of the current device (cached per device).
+inline int num_sms() {
+    static int cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+    if (cache[dev] == 0) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev] = n > 0 ? n : 148;
+    }
+    return cache[dev];
+}
+
 template <typename T> struct cplx;
 template <> struct cplx<float> { using type = float2; };
 template <> struct cplx<double> { using type = double2; };

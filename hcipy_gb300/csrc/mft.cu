@@ -28,6 +28,7 @@ struct hx_mft_plan {
     void* m2a = nullptr;  // nu x nx : exp(+i u x) wx[x]
     bool own_adjoint = false;
     hx::SplitMftPlan* split = nullptr;  // tensor-core operands (HX_PREC_SPLIT)
+    int schedule = HX_SCHEDULE_LATENCY;
 };
 
 namespace {
@@ -95,26 +96,28 @@ int execute_t(const hx_mft_plan* p, int direction, int batch, const void* in_, v
     const Cx one = hx::make_c<T>(T(1), T(0));
     const Cx alpha = hx::make_c<T>((T)are, (T)aim);
     const int nx = p->nx, ny = p->ny, nu = p->nu, nv = p->nv;
+    const bool tp = p->schedule == HX_SCHEDULE_THROUGHPUT;
     hx::Epilogue<Cx> epi;
     epi.kind = epilogue;
     epi.mask = (const Cx*)mask;
     epi.src = (const Cx*)src;
     if (direction == HX_FORWARD) {
         // T (batch*ny x nu) = in (batch*ny x nx) . M2f (nx x nu)
-        HX_TRY(hx::cgemm_nn<T>(batch * ny, nu, nx, one, in, nx, 0, (const Cx*)p->m2f, nu, 0, T1, nu, 0, 1, stream));
+        HX_TRY(hx::cgemm_nn<T>(batch * ny, nu, nx, one, in, nx, 0, (const Cx*)p->m2f, nu, 0, T1, nu, 0, 1, stream, {},
+                               tp));
         // out[b] (nv x nu) = alpha * M1f (nv x ny) . T[b] (ny x nu)
         epi.rows_per_field = nv;
         return hx::cgemm_nn<T>(nv, nu, ny, alpha, (const Cx*)p->m1f, ny, 0, T1, nu, (long long)ny * nu, out, nu,
-                               (long long)nv * nu, batch, stream, epi);
+                               (long long)nv * nu, batch, stream, epi, tp);
     }
     const Cx* m1 = (const Cx*)(direction == HX_BACKWARD ? p->m1b : p->m1a);
     const Cx* m2 = (const Cx*)(direction == HX_BACKWARD ? p->m2b : p->m2a);
     // T[b] (ny x nu) = M1 (ny x nv) . in[b] (nv x nu)
     HX_TRY(hx::cgemm_nn<T>(ny, nu, nv, one, m1, nv, 0, in, nu, (long long)nv * nu, T1, nu, (long long)ny * nu, batch,
-                           stream));
+                           stream, {}, tp));
     // out (batch*ny x nx) = alpha * T (batch*ny x nu) . M2 (nu x nx)
     epi.rows_per_field = ny;
-    return hx::cgemm_nn<T>(batch * ny, nx, nu, alpha, T1, nu, 0, m2, nx, 0, out, nx, 0, 1, stream, epi);
+    return hx::cgemm_nn<T>(batch * ny, nx, nu, alpha, T1, nu, 0, m2, nx, 0, out, nx, 0, 1, stream, epi, tp);
 }
 
 }  // namespace
@@ -321,6 +324,7 @@ int hx_mft_plan_set_schedule(hx_mft_plan* p, int schedule) {
     HX_CHECK_ARG(p != nullptr, "hx_mft_plan_set_schedule: plan is NULL");
     HX_CHECK_ARG(schedule == HX_SCHEDULE_LATENCY || schedule == HX_SCHEDULE_THROUGHPUT,
                  "hx_mft_plan_set_schedule: unknown schedule %d", schedule);
+    p->schedule = schedule;
     if (p->split) hx::split_mft_set_schedule(p->split, schedule);
     return HX_OK;
 }

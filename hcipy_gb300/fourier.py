@@ -195,8 +195,10 @@ class MatrixFourierTransform(FourierTransform):
     ``allocate_intermediate`` are accepted for API compatibility: the phase
     matrices are always kept on the device and the intermediate is scratch from
     torch's caching allocator.  ``schedule`` ('latency', default, or 'throughput') is the
-    tile policy of the split GEMMs: 'throughput' for transforms that run beside
-    others (several streams, parallel graph branches), see ``hx_mft_plan_set_schedule``.
+    tile policy of the GEMMs: 'latency' narrows tiles (CUDA cores) or splits K (tensor
+    cores) until a small transform occupies the GPU; 'throughput' is for transforms that
+    run beside others (several streams, parallel graph branches), see
+    ``hx_mft_plan_set_schedule``.
     """
 
     def __init__(self, input_grid, output_grid, precompute_matrices=None, allocate_intermediate=None,

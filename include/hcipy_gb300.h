@@ -173,7 +173,8 @@ HX_API int hx_mft_plan_status(const hx_mft_plan* plan, int reset);
 /* Tile policy of the plan's GEMMs, HX_SCHEDULE_LATENCY (default) or HX_SCHEDULE_THROUGHPUT, for plans whose
  * transforms run concurrently with others (several streams, or parallel branches of a CUDA graph): small
  * transforms then take the tile with the least SM time instead of splitting K to fill the GPU alone, and the
- * autotuner's measurements are ranked by duration x occupied SMs.  FP32 plans accept and ignore it. */
+ * autotuner's measurements are ranked by duration x occupied SMs; FP32/FP64 plans keep their widest CUDA-core
+ * tile instead of narrowing it to occupy the GPU. */
 HX_API int hx_mft_plan_set_schedule(hx_mft_plan* plan, int schedule);
 
 /* Tile autotuner of the split tensor-core GEMMs (process-wide; no counterpart in the reference).  When on,
