@@ -102,6 +102,10 @@ SIGNATURES = {
     'hx_czt_execute': (c_int, [c_void_p, c_int, c_int, c_void_p, c_ll, c_ll, c_ll, c_void_p, c_ll, c_ll, c_ll,
                                c_void_p]),
     'hx_czt_plan_destroy': (c_int, [c_void_p]),
+    'hx_fresnel_transfer_function': (c_int, [c_int, c_int, c_double, c_double, c_double, c_double, c_double,
+                                             c_double, c_int, c_int, c_void_p, c_void_p]),
+    'hx_fresnel_impulse_response': (c_int, [c_int, c_int, c_double, c_double, c_double, c_double, c_double,
+                                            c_double, c_double, c_int, c_int, c_void_p, c_void_p]),
     'hx_asp_transfer_function': (c_int, [c_int, c_int, c_double, c_double, c_double, c_double, c_double, c_double,
                                          c_int, c_int, c_void_p, c_void_p]),
     'hx_asp_impulse_response': (c_int, [c_int, c_int, c_double, c_double, c_double, c_double, c_double, c_double,

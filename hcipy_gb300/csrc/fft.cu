@@ -1,6 +1,6 @@
 // FFT-family plans: the zero-padded FastFourierTransform, the Fourier filter
-// (FourierFilter / angular-spectrum propagation), the chirp-Z transform, and the
-// angular-spectrum transfer function.  All transforms run fft_line_kernel.
+// (FourierFilter / angular-spectrum and Fresnel propagation), the chirp-Z transform, and the
+// angular-spectrum and Fresnel transfer functions.  All transforms run fft_line_kernel.
 //
 // Reference behaviour restated here:
 //   FastFourierTransform  hcipy/fourier/fast_fourier_transform.py:223-406
@@ -921,9 +921,111 @@ __global__ void asp_ir_kernel(int Nx, int Ny, double zx, double zy, double dx, d
     out[idx] = hx::make_c<T>((T)(re / n), (T)(im / n));
 }
 
+// Fresnel transfer function (hcipy/propagation/fresnel.py:69-80) in FFT order: the mean over os x os dithers of
+// exp(i k d) exp(-i d/(2k) (kx^2 + ky^2)), the constant factor evaluated once.
+template <typename T>
+__global__ void fresnel_tf_kernel(int Nx, int Ny, double zx, double zy, double dx, double dy, double k, double dist,
+                                  int os, typename hx::cplx<T>::type* tf) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)Nx * Ny) return;
+    const int ix = (int)(idx % Nx), iy = (int)(idx / Nx);
+    const int cx = (ix + Nx / 2) % Nx, cy = (iy + Ny / 2) % Ny;
+    const double alpha = -0.5 * dist / k;
+    double re = 0, im = 0;
+    const double dz = 1.0 / os;
+    for (int oy = 0; oy < os; ++oy) {
+        const double ky = zy + cy * dy + (-0.5 + dz / 2 + dz * oy) * dy;
+        for (int ox = 0; ox < os; ++ox) {
+            const double kx = zx + cx * dx + (-0.5 + dz / 2 + dz * ox) * dx;
+            double s, c;
+            sincos(alpha * (kx * kx + ky * ky), &s, &c);
+            re += c;
+            im += s;
+        }
+    }
+    double ps, pc;
+    sincos(k * dist, &ps, &pc);
+    const double n = (double)os * os;
+    re /= n;
+    im /= n;
+    tf[idx] = hx::make_c<T>((T)(pc * re - ps * im), (T)(pc * im + ps * re));
+}
+
+// Fresnel impulse response (fresnel.py:55-67) on a centred regular grid (zero, delta), grid order: the mean over
+// os x os dithers of exp(i k d) / (i lambda d) exp(i k/(2d) (x^2 + y^2)).
+template <typename T>
+__global__ void fresnel_ir_kernel(int Nx, int Ny, double zx, double zy, double dx, double dy, double k, double lambda,
+                                  double dist, int os, typename hx::cplx<T>::type* out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)Nx * Ny) return;
+    const int ix = (int)(idx % Nx), iy = (int)(idx / Nx);
+    const double alpha = 0.5 * k / dist;
+    double re = 0, im = 0;
+    const double dz = 1.0 / os;
+    for (int oy = 0; oy < os; ++oy) {
+        const double y = zy + iy * dy + (-0.5 + dz / 2 + dz * oy) * dy;
+        for (int ox = 0; ox < os; ++ox) {
+            const double x = zx + ix * dx + (-0.5 + dz / 2 + dz * ox) * dx;
+            double s, c;
+            sincos(alpha * (x * x + y * y), &s, &c);
+            re += c;
+            im += s;
+        }
+    }
+    // exp(i k d) / (i lambda d) = (sin(k d) - i cos(k d)) / (lambda d)
+    double ps, pc;
+    sincos(k * dist, &ps, &pc);
+    const double fr = ps / (lambda * dist), fi = -pc / (lambda * dist);
+    const double n = (double)os * os;
+    re /= n;
+    im /= n;
+    out[idx] = hx::make_c<T>((T)(fr * re - fi * im), (T)(fr * im + fi * re));
+}
+
 }  // namespace
 
 extern "C" {
+
+int hx_fresnel_transfer_function(int nx, int ny, double zero_x, double zero_y, double delta_x, double delta_y,
+                                 double wavenumber, double distance, int oversampling, int dtype, void* out,
+                                 void* stream) {
+    HX_CHECK_ARG(nx > 0 && ny > 0 && out != nullptr, "hx_fresnel_transfer_function: bad sizes or NULL output");
+    HX_CHECK_ARG(oversampling >= 1, "hx_fresnel_transfer_function: oversampling must be >= 1");
+    HX_CHECK_ARG(dtype == HX_C64 || dtype == HX_C128, "hx_fresnel_transfer_function: unknown dtype %d", dtype);
+    HX_CHECK_ARG(wavenumber > 0, "hx_fresnel_transfer_function: the wavenumber must be positive");
+    if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long n = (long long)nx * ny;
+    if (dtype == HX_C64)
+        fresnel_tf_kernel<float><<<hx::ceil_div(n, 256), 256, 0, s>>>(nx, ny, zero_x, zero_y, delta_x, delta_y,
+                                                                      wavenumber, distance, oversampling, (float2*)out);
+    else
+        fresnel_tf_kernel<double><<<hx::ceil_div(n, 256), 256, 0, s>>>(nx, ny, zero_x, zero_y, delta_x, delta_y,
+                                                                       wavenumber, distance, oversampling,
+                                                                       (double2*)out);
+    return hx::launch_status("fresnel_tf_kernel");
+}
+
+int hx_fresnel_impulse_response(int nx, int ny, double zero_x, double zero_y, double delta_x, double delta_y,
+                                double wavenumber, double wavelength, double distance, int oversampling, int dtype,
+                                void* out, void* stream) {
+    HX_CHECK_ARG(nx > 0 && ny > 0 && out != nullptr, "hx_fresnel_impulse_response: bad sizes or NULL output");
+    HX_CHECK_ARG(oversampling >= 1, "hx_fresnel_impulse_response: oversampling must be >= 1");
+    HX_CHECK_ARG(dtype == HX_C64 || dtype == HX_C128, "hx_fresnel_impulse_response: unknown dtype %d", dtype);
+    HX_CHECK_ARG(distance != 0 && wavelength > 0, "hx_fresnel_impulse_response: distance and wavelength must be nonzero");
+    if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long n = (long long)nx * ny;
+    if (dtype == HX_C64)
+        fresnel_ir_kernel<float><<<hx::ceil_div(n, 256), 256, 0, s>>>(nx, ny, zero_x, zero_y, delta_x, delta_y,
+                                                                      wavenumber, wavelength, distance, oversampling,
+                                                                      (float2*)out);
+    else
+        fresnel_ir_kernel<double><<<hx::ceil_div(n, 256), 256, 0, s>>>(nx, ny, zero_x, zero_y, delta_x, delta_y,
+                                                                       wavenumber, wavelength, distance, oversampling,
+                                                                       (double2*)out);
+    return hx::launch_status("fresnel_ir_kernel");
+}
 
 int hx_asp_impulse_response(int nx, int ny, double zero_x, double zero_y, double delta_x, double delta_y,
                             double wavenumber, double distance, int oversampling, int dtype, void* out, void* stream) {

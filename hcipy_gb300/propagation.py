@@ -188,3 +188,110 @@ class AngularSpectrumPropagator(AgnosticOpticalElement):
         """angular_spectrum.py:224-240."""
         filtered = instance_data.fourier_filter.backward(wavefront.electric_field)
         return Wavefront(filtered, wavefront.wavelength)
+
+
+class FresnelPropagator(AgnosticOpticalElement):
+    """Monochromatic Fresnel propagation over ``distance`` (hcipy/propagation/fresnel.py:8-164).
+
+    The paraxial transfer function exp(i k d) exp(-i d/(2k) (kx^2 + ky^2)) (native branch, :69-80), or the FFT of
+    the impulse response exp(i k d)/(i lambda d) exp(i k/(2d) r^2) when the grid undersamples it (:51-67), is
+    built on the device in float64, supersampled ``num_oversampling`` times, and applied by a Fourier filter with
+    ``q = zero_padding``.  The input grid is taken from the incoming wavefront.
+    """
+
+    def __init__(self, input_grid, distance, num_oversampling=2, zero_padding=2, refractive_index=1):
+        self._distance = distance
+        self._num_oversampling = num_oversampling
+        self._zero_padding = zero_padding
+        self._refractive_index = refractive_index
+        AgnosticOpticalElement.__init__(self, grid_dependent=True, wavelength_dependent=True)
+
+    def make_instance(self, instance_data, input_grid, output_grid, wavelength):
+        import torch
+        from .fft import FourierFilter, FastFourierTransform
+        from .fourier import make_fft_grid, _is_cartesian
+        if not input_grid.is_regular or not _is_cartesian(input_grid):
+            raise ValueError('The input grid must be a regular, Cartesian grid.')
+        n = self.evaluate_parameter(self.refractive_index, input_grid, output_grid, wavelength)
+        k = 2 * np.pi / wavelength * n
+        delta = np.asarray(input_grid.delta, np.float64)
+        l_max = np.max(np.asarray(input_grid.dims) * delta)
+        os_ = int(round(self.num_oversampling))
+        q = self.zero_padding
+        fourier_grid = make_fft_grid(input_grid, q, 1)
+        lib = _lib.lib()
+        if np.any(delta < wavelength * abs(self.distance) / l_max):
+            enlarged = make_fft_grid(fourier_grid)
+            ez = np.asarray(enlarged.zero, np.float64)
+            ed = np.asarray(enlarged.delta, np.float64)
+            en = [int(d) for d in enlarged.dims]
+            ir = torch.empty(en[0] * en[1], dtype=torch.complex128, device='cuda')
+            rc = lib.hx_fresnel_impulse_response(en[0], en[1], ez[0], ez[1], ed[0], ed[1], k, float(wavelength),
+                                                 float(self.distance), os_, _lib.HX_C128, _lib.dptr(ir),
+                                                 _lib.stream_handle())
+            _lib.check(rc, 'hx_fresnel_impulse_response')
+            tf = FastFourierTransform(enlarged).forward(ir).data
+            instance_data.fourier_filter = FourierFilter(input_grid, tf, q=q)
+        else:
+            fz = np.asarray(fourier_grid.zero, np.float64)
+            fd = np.asarray(fourier_grid.delta, np.float64)
+            fn = [int(d) for d in fourier_grid.dims]
+            tf = torch.empty(fn[0] * fn[1], dtype=torch.complex128, device='cuda')
+            rc = lib.hx_fresnel_transfer_function(fn[0], fn[1], fz[0], fz[1], fd[0], fd[1], k, float(self.distance),
+                                                  os_, _lib.HX_C128, _lib.dptr(tf), _lib.stream_handle())
+            _lib.check(rc, 'hx_fresnel_transfer_function')
+            instance_data.fourier_filter = FourierFilter(input_grid, tf, q=q, fft_order=True)
+
+    @property
+    def distance(self):
+        return self._distance
+
+    @distance.setter
+    def distance(self, distance):
+        self._distance = distance
+        self.clear_cache()
+
+    @property
+    def num_oversampling(self):
+        return self._num_oversampling
+
+    @num_oversampling.setter
+    def num_oversampling(self, num_oversampling):
+        self._num_oversampling = num_oversampling
+        self.clear_cache()
+
+    @property
+    def zero_padding(self):
+        return self._zero_padding
+
+    @zero_padding.setter
+    def zero_padding(self, zero_padding):
+        self._zero_padding = zero_padding
+        self.clear_cache()
+
+    @property
+    def refractive_index(self):
+        return self._refractive_index
+
+    @refractive_index.setter
+    def refractive_index(self, refractive_index):
+        self._refractive_index = refractive_index
+        self.clear_cache()
+
+    def get_input_grid(self, output_grid, wavelength):
+        return output_grid
+
+    def get_output_grid(self, input_grid, wavelength):
+        return input_grid
+
+    @make_agnostic_forward
+    def forward(self, instance_data, wavefront):
+        """fresnel.py:131-147."""
+        filtered = instance_data.fourier_filter.forward(wavefront.electric_field)
+        return Wavefront(filtered, wavefront.wavelength)
+
+    @make_agnostic_backward
+    def backward(self, instance_data, wavefront):
+        """fresnel.py:149-164."""
+        filtered = instance_data.fourier_filter.backward(wavefront.electric_field)
+        return Wavefront(filtered, wavefront.wavelength)

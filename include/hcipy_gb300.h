@@ -284,6 +284,22 @@ HX_API int hx_asp_impulse_response(int nx, int ny, double zero_x, double zero_y,
                             void* stream);
 
 /* ------------------------------------------------------------------------
+ * Fresnel transfer function exp(i k d) exp(-i d/(2k) (kx^2 + ky^2)), averaged over oversampling^2 dithered
+ * sub-samples, in float64 on the padded FFT grid (zero, delta per axis), FFT order
+ * (hcipy/propagation/fresnel.py:69-80 with evaluate_supersampled).
+ * ------------------------------------------------------------------------ */
+HX_API int hx_fresnel_transfer_function(int nx, int ny, double zero_x, double zero_y, double delta_x, double delta_y,
+                                        double wavenumber, double distance, int oversampling, int dtype, void* out,
+                                        void* stream);
+/* Fresnel impulse response exp(i k d)/(i lambda d) exp(i k/(2d) (x^2 + y^2)), averaged over oversampling^2 dithers,
+ * on a regular grid (zero, delta), grid order; the other branch's transfer function is its FFT
+ * (hcipy/propagation/fresnel.py:51-67).  wavenumber k includes the refractive index, wavelength is the vacuum
+ * wavelength of the 1/(i lambda d) factor. */
+HX_API int hx_fresnel_impulse_response(int nx, int ny, double zero_x, double zero_y, double delta_x, double delta_y,
+                                       double wavenumber, double wavelength, double distance, int oversampling,
+                                       int dtype, void* out, void* stream);
+
+/* ------------------------------------------------------------------------
  * Deformable mirror.
  * Surface of nvec command vectors at once: surface[v, p] = sum_a Phi[p, a] actuators[v, a]
  * (DeformableMirror.surface / ModeBasis.linear_combination, hcipy/optics/deformable_mirror.py:251-262,

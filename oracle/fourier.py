@@ -268,3 +268,37 @@ def asp_uses_impulse_branch(input_grid, wavelength, distance):
     """angular_spectrum.py:139-143."""
     l_max = np.max(input_grid.dims * input_grid.delta)
     return bool(np.any(input_grid.delta < wavelength * abs(distance) / l_max))
+
+
+# ---------------------------------------------------------------------------
+# Fresnel propagation -- hcipy/propagation/fresnel.py:45-80
+# ---------------------------------------------------------------------------
+
+def fresnel_uses_impulse_branch(input_grid, wavelength, distance):
+    """fresnel.py:47-50 (the same sampling test as the angular-spectrum propagator)."""
+    return asp_uses_impulse_branch(input_grid, wavelength, distance)
+
+
+def fresnel_transfer_function(internal_grid, wavelength, distance, refractive_index=1, oversampling=2):
+    """Native branch, fresnel.py:69-80: exp(i k d) exp(-i d/(2k) (kx^2 + ky^2)), supersampled."""
+    k = 2 * np.pi / wavelength * refractive_index
+    phase_factor = np.exp(1j * k * distance)
+
+    def tf(kx, ky):
+        return phase_factor * np.exp(-0.5j * distance / k * (kx * kx + ky * ky))
+
+    return supersampled_mean(tf, internal_grid, oversampling)
+
+
+def fresnel_impulse_transfer_function(internal_grid, wavelength, distance, refractive_index=1, oversampling=2):
+    """Impulse-response branch, fresnel.py:51-67: the impulse response exp(i k d)/(i lambda d) exp(i k/(2d) r^2),
+    supersampled on the spatial grid of the Fourier grid, transformed by the (unpadded) FFT."""
+    from .grids import make_fft_grid
+    k = 2 * np.pi / wavelength * refractive_index
+    enlarged = make_fft_grid(internal_grid)
+    phase_factor = np.exp(1j * k * distance) / (1j * wavelength * distance)
+
+    def ir(x, y):
+        return phase_factor * np.exp(0.5j * k / distance * (x * x + y * y))
+
+    return FFTPlan(enlarged).forward(supersampled_mean(ir, enlarged, oversampling))

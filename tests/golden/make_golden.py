@@ -219,6 +219,28 @@ def make_asp_cases(hp, out):
     }
 
 
+def make_fresnel_cases(hp, out):
+    """FresnelPropagator (hcipy/propagation/fresnel.py) in both branches, two zero paddings, two media."""
+    rng = np.random.default_rng(45)
+    cases = [(64, 8.0, 1.6e-6, 0.5, 2, 1.0), (48, 8.0, 1.6e-6, 5000.0, 2, 1.0), (40, 2e-3, 500e-9, 0.05, 3, 1.0),
+             (32, 1e-3, 1e-6, 1.0, 2, 1.0), (36, 1e-3, 1e-6, 0.3, 2, 1.5)]
+    for i, (n, diam, wl, d, q, nref) in enumerate(cases):
+        pupil = hp.make_pupil_grid(n, diam)
+        aperture = hp.make_circular_aperture(diam * 0.9)(pupil)
+        e = aperture * np.exp(1j * rng.standard_normal(pupil.size) * 0.3)
+        prop = hp.FresnelPropagator(pupil, d, zero_padding=q, refractive_index=nref)
+        wf = hp.Wavefront(hp.Field(e, pupil), wl)
+        fwd = prop.forward(wf).electric_field
+        bwd = prop.backward(hp.Wavefront(fwd, wl)).electric_field
+        L_max = np.max(np.asarray(pupil.dims) * pupil.delta)
+        out['fresnel_%d' % i] = {
+            'n': np.int64(n), 'diam': np.float64(diam), 'wavelength': np.float64(wl), 'distance': np.float64(d),
+            'zero_padding': np.int64(q), 'refractive_index': np.float64(nref),
+            'E': e, 'fwd_c128': np.asarray(fwd), 'bwd_c128': np.asarray(bwd),
+            'impulse_branch': np.bool_(bool(np.any(pupil.delta < wl * abs(d) / L_max))),
+        }
+
+
 def make_lyot_case(hp, out):
     """A 128^2 pupil Lyot chain: focal-plane mask radius 4 lambda/D on a q=8 num_airy=8 grid."""
     pupil = hp.make_pupil_grid(128, 1)
@@ -337,6 +359,7 @@ def main():
     make_fft_cases(hp, out)
     make_czt_cases(hp, out)
     make_asp_cases(hp, out)
+    make_fresnel_cases(hp, out)
     make_lyot_case(hp, out)
     make_subpixel_cases(hp, out)
     make_atmosphere_case(hp, out)

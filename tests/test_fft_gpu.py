@@ -130,6 +130,24 @@ def test_angular_spectrum_matches_reference(case):
     assert rel_err(out64, g['fwd_c128']) < 5e-6
 
 
+@pytest.mark.parametrize('case', ['fresnel_0', 'fresnel_1', 'fresnel_2', 'fresnel_3', 'fresnel_4'])
+def test_fresnel_matches_reference(case):
+    """FresnelPropagator against the reference's propagation: both transfer-function branches, zero padding 2
+    and 3, refractive index 1 and 1.5; forward, backward and complex64 fields."""
+    g = load_golden(case)
+    pupil = hg.make_pupil_grid(int(g['n']), float(g['diam']))
+    prop = hg.FresnelPropagator(pupil, float(g['distance']), zero_padding=int(g['zero_padding']),
+                                refractive_index=float(g['refractive_index']))
+    wl = float(g['wavelength'])
+    out = prop.forward(hg.Wavefront(hg.Field(g['E'], pupil), wl)).electric_field.numpy()
+    # The phase k d reaches ~2e10 rad at 5 km; its float64 rounding differs from the reference's by ~1e-9 rad.
+    assert rel_err(out, g['fwd_c128']) < 1e-8
+    back = prop.backward(hg.Wavefront(hg.Field(g['fwd_c128'], pupil), wl)).electric_field.numpy()
+    assert rel_err(back, g['bwd_c128']) < 1e-8
+    out64 = prop.forward(hg.Wavefront(hg.Field(g['E'].astype(np.complex64), pupil), wl)).electric_field.numpy()
+    assert out64.dtype == np.complex64 and rel_err(out64, g['fwd_c128']) < 5e-6
+
+
 def test_planner_choices():
     """The default planner makes the reference's choices (hcipy tests/test_fourier.py planner cases, with the
     reference's own cost model): an FFT for a 128^2 pupil at q=1, an MFT at q=8 fov=0.3, a zoom FFT for 1024^2 at

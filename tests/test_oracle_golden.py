@@ -109,6 +109,22 @@ def test_asp_oracle(case):
     assert rel_err(plan.apply(g['fwd_c128'], adjoint=True), g['bwd_c128']) < 1e-10
 
 
+@pytest.mark.parametrize('case', ['fresnel_0', 'fresnel_1', 'fresnel_2', 'fresnel_3', 'fresnel_4'])
+def test_fresnel_oracle(case):
+    """Both branches of the Fresnel transfer function (fresnel.py:45-80) through the Fourier filter with the
+    case's zero padding, against the reference's propagation."""
+    g = load_golden(case)
+    pupil = grids.make_pupil_grid(int(g['n']), float(g['diam']))
+    wl, d, q, nref = float(g['wavelength']), float(g['distance']), int(g['zero_padding']), float(g['refractive_index'])
+    impulse = fourier.fresnel_uses_impulse_branch(pupil, wl, d)
+    assert impulse == bool(g['impulse_branch'])
+    internal = grids.make_fft_grid(pupil, q, 1)
+    make_tf = fourier.fresnel_impulse_transfer_function if impulse else fourier.fresnel_transfer_function
+    plan = fourier.FourierFilterPlan(pupil, make_tf(internal, wl, d, nref), q=q)
+    assert rel_err(plan.apply(g['E']), g['fwd_c128']) < 1e-10
+    assert rel_err(plan.apply(g['fwd_c128'], adjoint=True), g['bwd_c128']) < 1e-10
+
+
 def test_lyot_oracle():
     g = load_golden('lyot')
     pupil, fpm_grid, focal = grid_from(g, 'pupil'), grid_from(g, 'fpm'), grid_from(g, 'focal')
