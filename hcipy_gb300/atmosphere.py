@@ -433,23 +433,52 @@ class InfiniteAtmosphericLayer(AtmosphericLayer):
 
 
 class MultiLayerAtmosphere(OpticalElement):
-    """Layers applied without propagation between them (atmospheric_model.py:153-310 with scintillation=False).
+    """Layers applied in sequence (atmospheric_model.py:153-310).
 
-    The reference applies the layers one after the other, sorted by height (:185-212, :300-308); without
-    propagation between them the product of their phase factors is the phase factor of the summed screens, so
-    ``forward``/``backward`` sum the layers' screens once (``hx_atmosphere_combine``, into a buffer that keeps
-    its address) and apply one phase kernel.  ``evolve_until`` refreshes the sum, so a CUDA graph that captured
-    ``forward`` replays with the current screens; after evolving a layer on its own, call ``combined_screen()``
-    before replaying such a graph.
+    Without scintillation the reference applies the layers one after the other, sorted by height (:185-212,
+    :300-308); with no propagation between them the product of their phase factors is the phase factor of the
+    summed screens, so ``forward``/``backward`` sum the layers' screens once (``hx_atmosphere_combine``, into a
+    buffer that keeps its address) and apply one phase kernel.  ``evolve_until`` refreshes the sum, so a CUDA
+    graph that captured ``forward`` replays with the current screens; after evolving a layer on its own, call
+    ``combined_screen()`` before replaying such a graph.
+
+    With ``scintillation=True`` the layers are applied from the highest down with a Fresnel propagation over the
+    height difference between consecutive layers and from the lowest layer to the ground (:191-210).
     """
 
     def __init__(self, layers, scintillation=False):
-        if scintillation:
-            raise NotImplementedError('scintillation needs Fresnel propagation between the layers')
         self.layers = list(layers)
+        self._scintillation = bool(scintillation)
         self._t = 0
         self._combined = None
         self._combined_key = None
+        self._elements = None
+
+    @property
+    def scintillation(self):
+        return self._scintillation
+
+    @scintillation.setter
+    def scintillation(self, scintillation):
+        self._scintillation = bool(scintillation)
+        self._elements = None
+
+    def calculate_propagators(self):
+        """The element sequence of the scintillating form (atmospheric_model.py:185-212)."""
+        from .propagation import FresnelPropagator
+        heights = np.array([layer.height for layer in self.layers], np.float64)
+        order = np.argsort(-heights, kind='stable')
+        h = heights[order]
+        grid = self.layers[0].input_grid
+        elements = []
+        for i, j in enumerate(order):
+            elements.append(self.layers[j])
+            if i < len(order) - 1:
+                elements.append(FresnelPropagator(grid, h[i] - h[i + 1]))
+        if h[-1] > 0:
+            elements.append(FresnelPropagator(grid, h[-1]))
+        self._elements = elements
+        return elements
 
     def evolve_until(self, t):
         for layer in self.layers:
@@ -500,6 +529,8 @@ class MultiLayerAtmosphere(OpticalElement):
         return self._combined
 
     def phase_for(self, wavelength):
+        if self._scintillation:
+            raise ValueError('Cannot get the unwrapped phase for an atmosphere with scintillation.')
         return Field(self.combined_screen() / wavelength, self.layers[0].input_grid)
 
     def _apply(self, wf, sign):
@@ -513,7 +544,17 @@ class MultiLayerAtmosphere(OpticalElement):
         return Wavefront(Field(out, wf.electric_field.grid), wf.wavelength)
 
     def forward(self, wavefront):
+        if self._scintillation:
+            elements = self._elements or self.calculate_propagators()
+            for el in elements:
+                wavefront = el.forward(wavefront)
+            return wavefront
         return self._apply(wavefront, 1.0)
 
     def backward(self, wavefront):
+        if self._scintillation:
+            elements = self._elements or self.calculate_propagators()
+            for el in reversed(elements):
+                wavefront = el.backward(wavefront)
+            return wavefront
         return self._apply(wavefront, -1.0)

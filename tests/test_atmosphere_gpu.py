@@ -190,3 +190,45 @@ def test_multilayer_float32_forward_and_tracking():
     atm.reset()
     assert [layer._shifted.data_ptr() for layer in layers] == ptrs
     assert atm.combined_screen().data_ptr() == buf.data_ptr()
+
+
+def test_multilayer_scintillation_matches_oracle_chain():
+    """scintillation=True: layers from the highest down with Fresnel propagation over each height difference
+    (atmospheric_model.py:185-212), against the oracle's phase screens and Fresnel filters, forward and backward."""
+    from oracle import fourier as ofourier
+    from oracle import grids as ogrids
+    grid = hg.make_pupil_grid(64, 1.0)
+    rng = np.random.default_rng(12)
+    wl = 1e-6
+    screens = [rng.standard_normal(grid.size) * 2e-7 for _ in range(3)]
+    heights = [5000.0, 0.0, 2000.0]
+    layers = []
+    for s, h in zip(screens, heights):
+        layer = _StaticLayer(grid, torch.from_numpy(s).cuda())
+        layer.height = h
+        layers.append(layer)
+    atm = hg.MultiLayerAtmosphere(layers, scintillation=True)
+    with pytest.raises(ValueError):
+        atm.phase_for(wl)
+    e = np.exp(1j * 0.2 * rng.standard_normal(grid.size))
+    out = atm.forward(hg.Wavefront(hg.Field(e, grid), wl)).electric_field.numpy()
+    back = atm.backward(hg.Wavefront(hg.Field(out, grid), wl)).electric_field.numpy()
+    og = ogrids.make_pupil_grid(64, 1.0)
+    internal = ogrids.make_fft_grid(og, 2, 1)
+
+    def fresnel(x, d, adjoint=False):
+        assert not ofourier.fresnel_uses_impulse_branch(og, wl, d)
+        return ofourier.FourierFilterPlan(og, ofourier.fresnel_transfer_function(internal, wl, d), q=2).apply(
+            x, adjoint=adjoint)
+
+    ref = e * np.exp(1j * screens[0] / wl)
+    ref = fresnel(ref, 3000.0) * np.exp(1j * screens[2] / wl)
+    ref = fresnel(ref, 2000.0) * np.exp(1j * screens[1] / wl)
+    assert rel_err(out, ref) < 1e-8
+    rb = out * np.exp(-1j * screens[1] / wl)
+    rb = fresnel(rb, 2000.0, adjoint=True) * np.exp(-1j * screens[2] / wl)
+    rb = fresnel(rb, 3000.0, adjoint=True) * np.exp(-1j * screens[0] / wl)
+    assert rel_err(back, rb) < 1e-8
+    atm.scintillation = False
+    assert rel_err(atm.forward(hg.Wavefront(hg.Field(e, grid), wl)).electric_field.numpy(),
+                   e * np.exp(1j * sum(screens) / wl)) < 1e-12

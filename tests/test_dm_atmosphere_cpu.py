@@ -120,3 +120,22 @@ def test_oracle_lyot_adjoint_and_gradient():
         am_[i] -= h
         fd = (oo.dm_lyot_loss_grad(ch, inf, ap, ap_, roi)[0] - oo.dm_lyot_loss_grad(ch, inf, ap, am_, roi)[0]) / (2 * h)
         assert abs(fd - g[i]) < 1e-7 * np.abs(g).max()
+
+
+def test_scintillation_element_order():
+    """The scintillating multi-layer sequence (atmospheric_model.py:185-212): layers from the highest down, a
+    Fresnel propagation over each height difference, and one to the ground when the lowest layer is above it."""
+    import hcipy_gb300 as hg
+
+    class Stub(object):
+        def __init__(self, h):
+            self.height = h
+            self.input_grid = hg.make_pupil_grid(8, 1.0)
+
+    a, b, c = Stub(5000.0), Stub(0.0), Stub(2000.0)
+    els = hg.MultiLayerAtmosphere([a, b, c], scintillation=True).calculate_propagators()
+    assert els[0] is a and els[2] is c and els[4] is b and len(els) == 5
+    assert [e.distance for e in (els[1], els[3])] == [3000.0, 2000.0]
+    assert all(isinstance(e, hg.FresnelPropagator) for e in (els[1], els[3]))
+    els = hg.MultiLayerAtmosphere([Stub(300.0), Stub(1000.0)], scintillation=True).calculate_propagators()
+    assert [getattr(e, 'distance', None) for e in els] == [None, 700.0, None, 300.0]
