@@ -58,6 +58,25 @@ def mft_apply(ft, x, direction, alpha):
     return _MftFunction.apply(x, ft, direction, complex(alpha))
 
 
+class _LinearFunction(torch.autograd.Function):
+    """y = op(x) for a linear operator with a known adjoint: the gradient of x is adjoint(gradient of y)."""
+
+    @staticmethod
+    def forward(ctx, x, op, adjoint):
+        ctx.adjoint = adjoint
+        ctx.in_dtype = x.dtype
+        return op(x)
+
+    @staticmethod
+    def backward(ctx, g):
+        return ctx.adjoint(g.contiguous()).to(ctx.in_dtype), None, None
+
+
+def linear_apply(x, op, adjoint):
+    """op(x), differentiable in x through ``adjoint`` (callables on device tensors)."""
+    return _LinearFunction.apply(x, op, adjoint)
+
+
 class _PhaseFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, e, s, scale):

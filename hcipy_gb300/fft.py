@@ -148,6 +148,18 @@ class FastFourierTransform(FourierTransform):
         """fast_fourier_transform.py:367-406."""
         return self._run(field, self.output_grid, self.input_grid, _lib.HX_BACKWARD)
 
+    @property
+    def adjoint_scale(self):
+        """forward = scale Post Crop F Pad Pre with unit-modulus phase factors and the unnormalised DFT F, whose
+        adjoint F^H is N times the normalised inverse; ``backward`` divides by scale and N, so the adjoint of
+        ``forward`` is scale^2 N ``backward``.  Not part of the reference API."""
+        return self._scale**2 * float(np.prod(self._n_int))
+
+    def adjoint(self, field):
+        """The conjugate transpose of ``forward``; not part of the reference API."""
+        out = self.backward(field)
+        return Field(out.data * self.adjoint_scale, self.input_grid)
+
     @classmethod
     def check_if_supported(cls, input_grid, output_grid):
         get_fft_parameters(output_grid, input_grid)

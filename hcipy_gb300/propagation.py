@@ -8,6 +8,31 @@ from .fourier import make_fourier_transform, MatrixFourierTransform
 from .optics import AgnosticOpticalElement, Wavefront, make_agnostic_forward, make_agnostic_backward
 
 
+def _adjoint_scale(ft):
+    """c with forward^H = c backward for the FFT-family transforms the planner may pick."""
+    scale = getattr(ft, 'adjoint_scale', None)
+    if scale is None:
+        raise NotImplementedError('gradients through a %s are not implemented' % type(ft).__name__)
+    return scale
+
+
+def _adjoint_of_forward(ft):
+    c = _adjoint_scale(ft)
+    return lambda g: ft.backward(g).data * c
+
+
+def _filter_apply(ff, wavefront, adjoint):
+    """The Fourier filter (or, with adjoint, its backward: the conjugate transfer function, which is the exact
+    adjoint of the filter) on the wavefront's field, differentiable when the field requires grad."""
+    e = wavefront.electric_field
+    fwd, adj = (ff.backward, ff.forward) if adjoint else (ff.forward, ff.backward)
+    if _differentiable(e):
+        from .autograd import linear_apply
+        res = linear_apply(e.data, lambda t: fwd(t).data, lambda g: adj(g).data)
+        return Wavefront(Field(res, e.grid), wavefront.wavelength)
+    return Wavefront(fwd(e), wavefront.wavelength)
+
+
 def _differentiable(field):
     """True when autograd records operations on this field's tensor."""
     t = field.data if isinstance(field, Field) else field
@@ -68,10 +93,14 @@ class FraunhoferPropagator(AgnosticOpticalElement):
                                  wavefront.wavelength)
             res = ft._run(e, ft.input_grid, ft.output_grid, _lib.HX_FORWARD, alpha)
         else:
+            norm = instance_data.norm_factor
             if _differentiable(e):
-                raise NotImplementedError('gradients through an FFT-based Fraunhofer propagator are not implemented; '
-                                          'use grids that make the planner choose the matrix Fourier transform')
-            res = ft.forward(e) * instance_data.norm_factor
+                from .autograd import linear_apply
+                adj = _adjoint_of_forward(ft)
+                res = linear_apply(e.data, lambda t: ft.forward(t).data * norm,
+                                   lambda g: adj(g) * np.conj(norm))
+                return Wavefront(Field(res, instance_data.output_grid), wavefront.wavelength)
+            res = ft.forward(e) * norm
         return Wavefront(Field(res.data, instance_data.output_grid), wavefront.wavelength)
 
     @make_agnostic_backward
@@ -87,9 +116,15 @@ class FraunhoferPropagator(AgnosticOpticalElement):
                                  wavefront.wavelength)
             res = ft._run(e, ft.output_grid, ft.input_grid, _lib.HX_BACKWARD, alpha)
         else:
+            norm = instance_data.norm_factor
             if _differentiable(e):
-                raise NotImplementedError('gradients through an FFT-based Fraunhofer propagator are not implemented')
-            res = ft.backward(e) / instance_data.norm_factor
+                from .autograd import linear_apply
+                fwd_scale = _adjoint_scale(ft)
+                # backward = forward^H / c, so its adjoint is forward / c
+                res = linear_apply(e.data, lambda t: ft.backward(t).data / norm,
+                                   lambda g: ft.forward(g).data / (fwd_scale * np.conj(norm)))
+                return Wavefront(Field(res, instance_data.input_grid), wavefront.wavelength)
+            res = ft.backward(e) / norm
         return Wavefront(Field(res.data, instance_data.input_grid), wavefront.wavelength)
 
 
@@ -179,15 +214,13 @@ class AngularSpectrumPropagator(AgnosticOpticalElement):
 
     @make_agnostic_forward
     def forward(self, instance_data, wavefront):
-        """angular_spectrum.py:206-222."""
-        filtered = instance_data.fourier_filter.forward(wavefront.electric_field)
-        return Wavefront(filtered, wavefront.wavelength)
+        """angular_spectrum.py:206-222; differentiable (the adjoint of the filter is its backward)."""
+        return _filter_apply(instance_data.fourier_filter, wavefront, adjoint=False)
 
     @make_agnostic_backward
     def backward(self, instance_data, wavefront):
-        """angular_spectrum.py:224-240."""
-        filtered = instance_data.fourier_filter.backward(wavefront.electric_field)
-        return Wavefront(filtered, wavefront.wavelength)
+        """angular_spectrum.py:224-240; differentiable."""
+        return _filter_apply(instance_data.fourier_filter, wavefront, adjoint=True)
 
 
 class FresnelPropagator(AgnosticOpticalElement):
@@ -286,12 +319,10 @@ class FresnelPropagator(AgnosticOpticalElement):
 
     @make_agnostic_forward
     def forward(self, instance_data, wavefront):
-        """fresnel.py:131-147."""
-        filtered = instance_data.fourier_filter.forward(wavefront.electric_field)
-        return Wavefront(filtered, wavefront.wavelength)
+        """fresnel.py:131-147; differentiable (the adjoint of the filter is its backward)."""
+        return _filter_apply(instance_data.fourier_filter, wavefront, adjoint=False)
 
     @make_agnostic_backward
     def backward(self, instance_data, wavefront):
-        """fresnel.py:149-164."""
-        filtered = instance_data.fourier_filter.backward(wavefront.electric_field)
-        return Wavefront(filtered, wavefront.wavelength)
+        """fresnel.py:149-164; differentiable."""
+        return _filter_apply(instance_data.fourier_filter, wavefront, adjoint=True)
