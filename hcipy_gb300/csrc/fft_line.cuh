@@ -456,50 +456,62 @@ __global__ void __launch_bounds__(kFftThreads) fft_line_kernel(const __grid_cons
     const Cx zero = make_c<T>(T(0), T(0));
 
     // ---- load ----
-    // U elements per thread per round (8 in float, 4 in double to stay within 128 registers): their global loads
-    // are all issued before any shared store, so a thread keeps U requests in flight instead of one.
+    // The buffer is zeroed with 16-byte stores, then only the valid inputs are read and scattered: for a
+    // zero-padded transform most FFT points are padding, and inverting the index map (input p -> FFT index j)
+    // visits the inputs alone.  U inputs per thread per round (8 in float, 4 in double to stay within 128
+    // registers): their global loads are all issued before any shared store.
     constexpr int U = sizeof(T) == 4 ? 8 : 4;
-    const int nload = lines * a.M;
     const bool line_fast = (a.in_es != 1);
-    const bool pow2_m = (a.M & (a.M - 1)) == 0;
-    const int lg_m = __ffs(a.M) - 1;
     // Index shifts reduced once, so each element needs one conditional subtraction instead of a modulo.
     const int ladd = ((a.load_add % a.n_log) + a.n_log) % a.n_log;
     const int soff = ((a.out_offset + a.store_add) % a.out_mod + a.out_mod) % a.out_mod;
+    {
+        const int nwords = smem_elems(lines * a.pitch) * (int)sizeof(Cx) / 16;
+        float4* b4 = reinterpret_cast<float4*>(buf);
+        for (int x = threadIdx.x; x < nwords; x += blockDim.x) b4[x] = make_float4(0.f, 0.f, 0.f, 0.f);
+        // a tail of fewer than 16 bytes (an odd number of float2 elements)
+        const int tail = smem_elems(lines * a.pitch) - nwords * 16 / (int)sizeof(Cx);
+        if ((int)threadIdx.x < tail) buf[nwords * 16 / (int)sizeof(Cx) + threadIdx.x] = zero;
+    }
+    __syncthreads();
+    // valid inputs p in [p_lo, p_hi): the FFT index j = (p + in_offset - load_add) mod n_log lies in [0, n_log)
+    const int p_lo = max(0, -a.in_offset);
+    const int p_hi = min(a.in_count, a.n_log - a.in_offset);
+    const int cnt = max(0, p_hi - p_lo);
+    const int nload = lines * cnt;
+    int jbase = p_lo + a.in_offset - ladd;  // FFT index of p_lo, in (-n_log, n_log)
+    if (jbase < 0) jbase += a.n_log;
+    const bool pow2_c = cnt > 0 && (cnt & (cnt - 1)) == 0;
+    const int lg_c = __ffs(cnt) - 1;
     for (int i0 = threadIdx.x; i0 < nload; i0 += U * blockDim.x) {
         Cx val[U];
         int dst[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int i = i0 + u * blockDim.x;
-            val[u] = zero;
             dst[u] = -1;
             if (i < nload) {
-                int ll, j;
+                int ll, pp;
                 if (line_fast) {
-                    if (lines == 1) { ll = 0; j = i; }
-                    else if (lines == 2) { ll = i & 1; j = i >> 1; }
-                    else { ll = i % lines; j = i / lines; }
-                } else if (pow2_m) {
-                    ll = i >> lg_m;
-                    j = i & (a.M - 1);
+                    if (lines == 1) { ll = 0; pp = i; }
+                    else if (lines == 2) { ll = i & 1; pp = i >> 1; }
+                    else { ll = i % lines; pp = i / lines; }
+                } else if (pow2_c) {
+                    ll = i >> lg_c;
+                    pp = i & (cnt - 1);
                 } else {
-                    ll = i / a.M;
-                    j = i - ll * a.M;
+                    ll = i / cnt;
+                    pp = i - ll * cnt;
                 }
+                int j = jbase + pp;
+                if (j >= a.n_log) j -= a.n_log;
+                const int p = p_lo + pp;
+                const long long l = l0 + ll;
+                Cx v = in[l * a.in_ls + (long long)p * a.in_es];
+                if (a.pre) v = c_mul(v, a.pre[l * a.pre_ls + p]);
+                if (a.chirp_in) v = c_mul(v, a.chirp_in[j]);
+                val[u] = v;
                 dst[u] = ll * a.pitch + j;
-                if (j < a.n_log) {
-                    int pa = j + ladd;
-                    if (pa >= a.n_log) pa -= a.n_log;
-                    const int p = pa - a.in_offset;
-                    if (p >= 0 && p < a.in_count) {
-                        const long long l = l0 + ll;
-                        Cx v = in[l * a.in_ls + (long long)p * a.in_es];
-                        if (a.pre) v = c_mul(v, a.pre[l * a.pre_ls + p]);
-                        if (a.chirp_in) v = c_mul(v, a.chirp_in[j]);
-                        val[u] = v;
-                    }
-                }
             }
         }
 #pragma unroll
@@ -529,22 +541,21 @@ __global__ void __launch_bounds__(kFftThreads) fft_line_kernel(const __grid_cons
     const bool line_fast_out = (a.out_es != 1);
     for (int i0 = threadIdx.x; i0 < nstore; i0 += U * blockDim.x) {
         Cx post[U];
+        int lls[U], kks[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int i = i0 + u * blockDim.x;
             post[u] = make_c<T>(T(1), T(0));
-            if (a.post && i < nstore) {
-                int ll, kk;
-                store_coords(i, lines, line_fast_out, a.out_count, ll, kk);
-                post[u] = a.post[(long long)(l0 + ll) * a.post_ls + (long long)kk * a.post_es];
+            lls[u] = -1;
+            if (i < nstore) {
+                store_coords(i, lines, line_fast_out, a.out_count, lls[u], kks[u]);
+                if (a.post) post[u] = a.post[(long long)(l0 + lls[u]) * a.post_ls + (long long)kks[u] * a.post_es];
             }
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            const int i = i0 + u * blockDim.x;
-            if (i >= nstore) continue;
-            int ll, kk;
-            store_coords(i, lines, line_fast_out, a.out_count, ll, kk);
+            if (lls[u] < 0) continue;
+            const int ll = lls[u], kk = kks[u];
             int src = soff + kk;
             if (src >= a.out_mod) src -= a.out_mod;
             Cx val = c_mul(buf[sidx(ll * a.pitch + src)], a.scale);
