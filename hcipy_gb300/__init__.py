@@ -12,7 +12,7 @@ from .optics import (Wavefront, OpticalElement, AgnosticOpticalElement, Apodizer
                      make_agnostic_forward, make_agnostic_backward)
 from .propagation import FraunhoferPropagator, AngularSpectrumPropagator, FresnelPropagator
 from .fft import FastFourierTransform, ChirpZTransform, ZoomFastFourierTransform, FourierFilter
-from .coronagraphy import LyotCoronagraph
+from .coronagraphy import LyotCoronagraph, MultiScaleCoronagraph, VortexCoronagraph
 from .deformable_mirror import (ModeBasis, DeformableMirror, make_actuator_positions,
                                 make_gaussian_influence_functions, find_illuminated_actuators)
 from .atmosphere import (AtmosphericLayer, InfiniteAtmosphericLayer, MultiLayerAtmosphere,
@@ -27,7 +27,8 @@ __all__ = [
     'make_fft_grid', 'get_fft_parameters', 'is_fft_grid',
     'Wavefront', 'OpticalElement', 'AgnosticOpticalElement', 'Apodizer', 'PhaseApodizer',
     'make_agnostic_forward', 'make_agnostic_backward',
-    'FraunhoferPropagator', 'AngularSpectrumPropagator', 'FresnelPropagator', 'LyotCoronagraph', 'HXError',
+    'FraunhoferPropagator', 'AngularSpectrumPropagator', 'FresnelPropagator', 'LyotCoronagraph',
+    'MultiScaleCoronagraph', 'VortexCoronagraph', 'HXError',
     'launch_count',
     'FastFourierTransform', 'ChirpZTransform', 'ZoomFastFourierTransform', 'FourierFilter',
     'ModeBasis', 'DeformableMirror', 'make_actuator_positions', 'make_gaussian_influence_functions',

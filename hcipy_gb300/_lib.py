@@ -164,6 +164,10 @@ def stream_handle(stream=None):
 
 
 def dptr(t):
+    """Device address of a tensor's data.  A conjugate view (``t.conj()``) shares the memory of its base and only
+    flags the conjugation, which a kernel cannot see: such views are refused (resolve them first)."""
+    if t.is_complex() and t.is_conj():
+        raise ValueError('a lazily conjugated tensor was passed to the library; call resolve_conj() first')
     return ctypes.c_void_p(t.data_ptr())
 
 

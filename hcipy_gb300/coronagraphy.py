@@ -117,3 +117,112 @@ class LyotCoronagraph(OpticalElement):
         wf_foc = Wavefront(wf_foc.electric_field - masked, wavefront.wavelength)
         pup = self.prop.backward(wf_foc)
         return Wavefront(wf.electric_field - pup.electric_field, wavefront.wavelength)
+
+
+class MultiScaleCoronagraph(OpticalElement):
+    """A focal-plane phase mask resolved on nested focal grids (hcipy/coronagraphy/multi_scale.py:10-161).
+
+    Level 0 applies the mask on the q=2 FFT grid of the pupil as a Fourier filter; level i > 0 samples a window of
+    ``window_size`` pixels around the centre of level i-1 ``scaling_factor`` times finer, with the part already
+    applied by the coarser levels subtracted from its mask (a Tukey window tapers each level's hand-over), and
+    propagates it with a forward and an inverse matrix Fourier transform at unit wavelength and focal length.
+    Here each finer level is two MFT launches with the mask product fused into the first and the accumulation
+    into the Lyot-plane field fused into the second (``L <- L + P^-1(M P(E))``).  The masks are built on the
+    device in float64 with this package's FFT and MFT.  Lyot-plane fields follow the input bit depth.
+    """
+
+    def __init__(self, input_grid, complex_mask, lyot_stop=None, q=1024, scaling_factor=4, window_size=32):
+        from scipy.signal import windows
+        from .fft import FastFourierTransform, FourierFilter
+        from .field import make_focal_grid
+        import math
+        self.input_grid = input_grid
+        pupil_diameter = np.asarray(input_grid.dims, np.float64) * np.asarray(input_grid.delta, np.float64)
+        if hasattr(lyot_stop, 'forward') or lyot_stop is None:
+            self.lyot_stop = lyot_stop
+        else:
+            self.lyot_stop = Apodizer(lyot_stop)
+        levels = int(math.ceil(math.log(q / 2) / math.log(scaling_factor))) + 1
+        qs = [2 * scaling_factor**i for i in range(levels)]
+        num_airys = [tuple(n / 2 for n in input_grid.dims)]
+        for i in range(1, levels):
+            num_airys.append(tuple(na * window_size / (2 * qs[i - 1] * na) for na in num_airys[i - 1]))
+        self.focal_grids, self.focal_masks = [], []
+        self._mfts = [None]
+        dev = torch.device('cuda')
+        for i in range(levels):
+            focal_grid = make_focal_grid(qs[i], num_airys[i], pupil_diameter=pupil_diameter, reference_wavelength=1,
+                                         focal_length=1)
+            mask = np.asarray(complex_mask(focal_grid), np.complex128).ravel().copy()
+            if i != levels - 1:
+                w = np.outer(windows.tukey(window_size, 1, False), windows.tukey(window_size, 1, False))
+                shape = (int(focal_grid.dims[1]), int(focal_grid.dims[0]))
+                w = np.pad(w, tuple((n_foc - n_w) // 2 for n_foc, n_w in zip(shape, w.shape)), 'constant').ravel()
+                mask *= 1 - w
+            mask_t = torch.from_numpy(mask).to(dev)
+            for j in range(i):
+                fft = FastFourierTransform(self.focal_grids[j])
+                mft = MatrixFourierTransform(focal_grid, fft.output_grid)
+                mask_t = mask_t - mft.backward(fft.forward(self.focal_masks[j].data)).data
+            self.focal_grids.append(focal_grid)
+            self.focal_masks.append(Field(mask_t, focal_grid))
+            if i == 0:
+                self._filter = FourierFilter(input_grid, mask_t, qs[0])
+            else:
+                self._mfts.append(MatrixFourierTransform(input_grid, focal_grid.scaled(2 * np.pi)))
+        self._masks = {}
+
+    def _mask(self, i, dtype, conj):
+        key = (i, dtype, conj)
+        m = self._masks.get(key)
+        if m is None:
+            m = self.focal_masks[i].data
+            m = (m.conj() if conj else m).to(dtype).contiguous().resolve_conj()
+            self._masks[key] = m
+        return m
+
+    def _propagate(self, e, conj):
+        """L = F(E) + sum_i P_i^-1(M_i P_i(E)) (conj: the conjugate masks and the backward filter)."""
+        lyot = (self._filter.backward(e) if conj else self._filter.forward(e)).data
+        # Fraunhofer at unit wavelength and focal length: norm 1/(i f lambda) = -i (fraunhofer.py:32-38)
+        norm = -1j
+        for i in range(1, len(self.focal_masks)):
+            ft = self._mfts[i]
+            a_fwd = complex(ft._w_in_scalar) * norm
+            a_bwd = complex(ft._w_out_scalar / (2 * np.pi)**2) / norm
+            focal = ft._run(e, ft.input_grid, ft.output_grid, _lib.HX_FORWARD, a_fwd, epilogue=_lib.HX_EPI_MUL,
+                            mask=self._mask(i, e.dtype, conj)).data
+            # lyot <- lyot - (-a_bwd) M1b focal M2b: the Babinet epilogue without a stop accumulates in place
+            ft._run(focal, ft.output_grid, ft.input_grid, _lib.HX_BACKWARD, -a_bwd, epilogue=_lib.HX_EPI_BABINET,
+                    src=lyot, out=lyot)
+        return lyot
+
+    def forward(self, wavefront):
+        """multi_scale.py:95-128."""
+        e = as_tensor(wavefront.electric_field).contiguous()
+        lyot = Wavefront(Field(self._propagate(e, False), self.input_grid), wavefront.wavelength)
+        if self.lyot_stop is not None:
+            lyot = self.lyot_stop.forward(lyot)
+        return lyot
+
+    def backward(self, wavefront):
+        """multi_scale.py:130-161: the same chain with the conjugate masks."""
+        if self.lyot_stop is not None:
+            wavefront = self.lyot_stop.backward(wavefront)
+        e = as_tensor(wavefront.electric_field).contiguous()
+        return Wavefront(Field(self._propagate(e, True), self.input_grid), wavefront.wavelength)
+
+
+class VortexCoronagraph(MultiScaleCoronagraph):
+    """A scalar vortex of ``charge`` (hcipy/coronagraphy/vortex.py:12-15): the mask exp(i charge theta), zero at
+    the singularity, on the multi-scale focal grids."""
+
+    def __init__(self, input_grid, charge, lyot_stop=None, q=1024, scaling_factor=4, window_size=32):
+        self.charge = charge
+
+        def complex_mask(grid):
+            x, y = grid.points_list()
+            centre = np.hypot(x, y) <= 0.5e-9  # make_circular_aperture(1e-9), boundary inclusive
+            return np.exp(1j * charge * np.arctan2(y, x)) * (1 - centre)
+
+        MultiScaleCoronagraph.__init__(self, input_grid, complex_mask, lyot_stop, q, scaling_factor, window_size)

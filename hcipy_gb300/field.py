@@ -433,6 +433,8 @@ def as_tensor(x, device='cuda'):
         t = torch.from_numpy(np.ascontiguousarray(arr))
     if t.device.type != 'cuda':
         t = t.to(device, non_blocking=False)
+    if t.is_complex() and t.is_conj():  # a lazy conjugate view: the kernels read memory, so materialise it
+        t = t.resolve_conj()
     return t
 
 

@@ -102,7 +102,7 @@ def _broadcast_mask(mask, grid, dtype):
         m = m.reshape(1).expand(grid.size)
     if m.shape[-1] != grid.size or m.numel() != grid.size:
         raise ValueError('A fused mask must be one field of the destination grid.')
-    return m.reshape(grid.size).contiguous()
+    return m.reshape(grid.size).contiguous().resolve_conj()
 
 
 def _scalar_weight(grid):

@@ -241,6 +241,26 @@ def make_fresnel_cases(hp, out):
         }
 
 
+def make_vortex_cases(hp, out):
+    """VortexCoronagraph (hcipy/coronagraphy/vortex.py:12-15 on multi_scale.py:10-161): charge 2 and 4, the
+    Lyot-plane field of an aberrated circular pupil, and the backward propagation of a random Lyot-plane field."""
+    rng = np.random.default_rng(46)
+    for i, (n, charge, q, sf, ws) in enumerate([(64, 2, 64, 4, 32), (48, 4, 32, 2, 16)]):
+        pupil = hp.make_pupil_grid(n, 1.0)
+        aperture = hp.make_circular_aperture(1.0)(pupil)
+        e = aperture * np.exp(1j * 0.05 * rng.standard_normal(pupil.size))
+        vortex = hp.VortexCoronagraph(pupil, charge, q=q, scaling_factor=sf, window_size=ws)
+        lyot = vortex.forward(hp.Wavefront(hp.Field(e, pupil), 1.0)).electric_field
+        g = random_field(rng, pupil)
+        back = vortex.backward(hp.Wavefront(hp.Field(g, pupil), 1.0)).electric_field
+        rec = {'n': np.int64(n), 'charge': np.int64(charge), 'q': np.int64(q), 'scaling_factor': np.int64(sf),
+               'window_size': np.int64(ws), 'E': e, 'lyot_c128': np.asarray(lyot), 'G': g,
+               'back_c128': np.asarray(back), 'levels': np.int64(len(vortex.focal_masks))}
+        for k, m in enumerate(vortex.focal_masks):
+            rec['mask_%d' % k] = np.asarray(m)
+        out['vortex_%d' % i] = rec
+
+
 def make_lyot_case(hp, out):
     """A 128^2 pupil Lyot chain: focal-plane mask radius 4 lambda/D on a q=8 num_airy=8 grid."""
     pupil = hp.make_pupil_grid(128, 1)
@@ -360,6 +380,7 @@ def main():
     make_czt_cases(hp, out)
     make_asp_cases(hp, out)
     make_fresnel_cases(hp, out)
+    make_vortex_cases(hp, out)
     make_lyot_case(hp, out)
     make_subpixel_cases(hp, out)
     make_atmosphere_case(hp, out)
