@@ -487,6 +487,57 @@ def run_broadband(args, dev, peaks):
     }
 
 
+def run_dm_probes(args, dev):
+    """Pair-wise DM probing, the electric-field-conjugation measurement step: the unprobed field and four probe
+    shapes applied with both signs (9 command vectors) through the DM (952 Gaussian actuators on a 512^2 pupil),
+    the Lyot coronagraph (512^2 focal-plane-mask grid) and the lens (256^2 image), intensities out; the whole
+    batch replayed from one CUDA graph (hcipy_gb300.CapturedCall) with new commands each iteration."""
+    import torch
+    import hcipy_gb300 as hg
+    from hcipy_gb300 import workloads
+    w = workloads.dm_gradient_workload()
+    pupil, fpm_grid, focal = w['pupil'], w['fpm_grid'], w['focal']
+    lyot = hg.LyotCoronagraph(pupil, hg.Field(w['fpm'], fpm_grid), hg.Field(w['stop'], pupil),
+                              precision=args.precision)
+    prop = hg.FraunhoferPropagator(pupil, focal, precision=args.precision)
+    dm = hg.DeformableMirror(w['influence'])
+    e0 = torch.from_numpy(w['aperture'].astype(np.complex64)).to(dev)
+    nact = w['influence'].num_modes
+    rng = np.random.default_rng(9)
+    probes = rng.standard_normal((4, nact)) * 2e-3
+    base = w['actuators'][0]
+    cmds = [base] + [base + sgn * p for p in probes for sgn in (1, -1)]
+    cmd = torch.from_numpy(np.asarray(cmds, np.float32)).to(dev)
+
+    def measure(c):
+        dm.actuators = c
+        e = dm.forward(hg.Wavefront(hg.Field(e0, pupil), 1.0))
+        img = prop.forward(lyot.forward(e)).electric_field.data
+        return img.real**2 + img.imag**2
+
+    hg.autotune(not args.no_autotune)
+    direct = measure(cmd).clone()
+    graph = hg.CapturedCall(measure, cmd)
+    replay = graph(cmd).clone()
+    same = bool(torch.equal(direct, replay))
+    n = 50
+    new = [cmd + 1e-4 * torch.randn_like(cmd) for _ in range(4)]
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for i in range(n):
+        graph(new[i % 4])
+    t1.record()
+    t1.synchronize()
+    ms = t0.elapsed_time(t1) / n
+    return {
+        'workload': '9 command vectors (unprobed + 4 probes x 2 signs) -> 952-actuator DM on 512^2 -> Lyot (512^2 '
+                    'FPM grid) -> 256^2 intensity',
+        'probe_sets_per_s': 1e3 / ms, 'propagations_per_s': 9 * 1e3 / ms, 'ms_per_probe_set': ms,
+        'kernels_in_graph': int(graph.graph_kernels), 'graph_equals_direct': same, 'precision': args.precision,
+    }
+
+
 def run_small_fraunhofer(args, dev, peaks):
     """A 256^2 pupil (Zernike 2-21 at 0.1 rad RMS) onto a 128^2 focal grid (q=4, num_airy=16): 12,582,912 complex
     MACs per propagation, a launch-latency-bound size.  Propagations/s through FraunhoferPropagator.forward with
@@ -841,6 +892,7 @@ def run_ours(args, rank, world, dist):
     if args.broadband_frames > 0:
         line['broadband_turbulence'] = run_broadband(args, dev, peaks)
     if not args.no_small:
+        line['dm_probes'] = run_dm_probes(args, dev)
         line['fraunhofer_256'] = run_small_fraunhofer(args, dev, peaks)
         line['fft_family_1024'] = run_fft_family(args, dev, peaks)
     print(json.dumps(line), flush=True)

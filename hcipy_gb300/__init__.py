@@ -12,6 +12,7 @@ from .optics import (Wavefront, OpticalElement, AgnosticOpticalElement, Apodizer
                      make_agnostic_forward, make_agnostic_backward)
 from .propagation import FraunhoferPropagator, AngularSpectrumPropagator, FresnelPropagator
 from .fft import FastFourierTransform, ChirpZTransform, ZoomFastFourierTransform, FourierFilter
+from .graphs import CapturedCall
 from .coronagraphy import LyotCoronagraph, MultiScaleCoronagraph, VortexCoronagraph
 from .deformable_mirror import (ModeBasis, DeformableMirror, make_actuator_positions,
                                 make_gaussian_influence_functions, find_illuminated_actuators)
@@ -28,7 +29,7 @@ __all__ = [
     'Wavefront', 'OpticalElement', 'AgnosticOpticalElement', 'Apodizer', 'PhaseApodizer',
     'make_agnostic_forward', 'make_agnostic_backward',
     'FraunhoferPropagator', 'AngularSpectrumPropagator', 'FresnelPropagator', 'LyotCoronagraph',
-    'MultiScaleCoronagraph', 'VortexCoronagraph', 'HXError',
+    'MultiScaleCoronagraph', 'VortexCoronagraph', 'CapturedCall', 'HXError',
     'launch_count',
     'FastFourierTransform', 'ChirpZTransform', 'ZoomFastFourierTransform', 'FourierFilter',
     'ModeBasis', 'DeformableMirror', 'make_actuator_positions', 'make_gaussian_influence_functions',

@@ -101,3 +101,34 @@ def test_broadband_through_multilayer_atmosphere():
             e = apply_phase(ap, atm.combined_screen(), 1.0 / wl).cpu().numpy().astype(np.complex128)
             ref = ooptics.fraunhofer_forward(e, _og(pupil), _og(g), wavelength=wl, focal_length=w['focal_length'])
             assert rel_err(img.cpu().numpy(), ref) < tol, (precision, wl, rel_err(img.cpu().numpy(), ref))
+
+
+def test_captured_dm_probes():
+    """A batch of DM probe commands through the DM, the Lyot coronagraph and the lens, recorded once as a CUDA
+    graph (CapturedCall): replays equal the direct call for each new set of commands."""
+    from hcipy_gb300 import workloads
+    w = workloads.dm_gradient_workload(pupil_n=128, n_act=12, nvec=3, fpm_q=4, fpm_num_airy=12, final_q=3.3,
+                                       final_num_airy=10)
+    pupil = w['pupil']
+    lyot = hg.LyotCoronagraph(pupil, hg.Field(w['fpm'], w['fpm_grid']), hg.Field(w['stop'], pupil))
+    prop = hg.FraunhoferPropagator(pupil, w['focal'])
+    dm = hg.DeformableMirror(w['influence'])
+    e0 = torch.from_numpy(w['aperture'].astype(np.complex64)).cuda()
+
+    def measure(c):
+        dm.actuators = c
+        e = dm.forward(hg.Wavefront(hg.Field(e0, pupil), 1.0))
+        img = prop.forward(lyot.forward(e)).electric_field.data
+        return img.real**2 + img.imag**2
+
+    cmd = torch.from_numpy(w['actuators'].astype(np.float32)).cuda()
+    graph = hg.CapturedCall(measure, cmd)
+    assert graph.graph_kernels > 0
+    for k in range(3):
+        c = cmd * (1 + k)
+        replayed = graph(c).clone()
+        assert torch.equal(replayed, measure(c))
+    first = graph(cmd).clone()
+    assert not torch.equal(first, graph(2 * cmd))
+    with pytest.raises(ValueError):
+        graph(cmd, cmd)
