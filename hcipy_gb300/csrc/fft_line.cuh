@@ -175,8 +175,8 @@ __device__ __forceinline__ typename cplx<T>::type w16(typename cplx<T>::type z) 
 }
 
 // 16 points as 4 x 4: n = 4 n1 + n2, k = k1 + 4 k2; four 4-point DFTs over n1 (in place: slot n2 + 4 k1), the
-// twiddles W16^(n2 k1), four 4-point DFTs over n2 (slots 4 k1 + k2), and the transposition k1 + 4 k2 <- 4 k1 + k2
-// as a renaming of registers.
+// twiddles W16^(n2 k1), four 4-point DFTs over n2 (slots 4 k1 + k2).  The result is left in slot order:
+// X[k1 + 4 k2] in v[4 k1 + k2] (out_index), and the caller stores it by that map.
 template <typename T, int SIGN>
 struct Dft<T, 16, SIGN> {
     template <typename Cx>
@@ -203,15 +203,9 @@ struct Dft<T, 16, SIGN> {
         v[15] = w16<T, SIGN, 9>(v[15]);
 #pragma unroll
         for (int k1 = 0; k1 < 4; ++k1) dft4_at(v, 4 * k1, 1);
-        // v[4 k1 + k2] holds X[k1 + 4 k2]
-        Cx x[16];
-#pragma unroll
-        for (int k1 = 0; k1 < 4; ++k1)
-#pragma unroll
-            for (int k2 = 0; k2 < 4; ++k2) x[k1 + 4 * k2] = v[4 * k1 + k2];
-#pragma unroll
-        for (int k = 0; k < 16; ++k) v[k] = x[k];
     }
+    // After run(), v[r] holds X[out_index(r)]: the outputs stay in the second pass's order (no register copies).
+    __host__ __device__ static constexpr int out_index(int r) { return (r >> 2) + 4 * (r & 3); }
 };
 
 template <typename T, int SIGN>
@@ -392,7 +386,10 @@ __device__ __forceinline__ void fft_stage(typename cplx<T>::type* buf, int M, in
     for (int i = 0; i < BPT; ++i) {
         if (dst[i] >= 0) {
 #pragma unroll
-            for (int r = 0; r < R; ++r) buf[sidx(dst[i] + r * Ns)] = v[i][r];
+            for (int r = 0; r < R; ++r) {
+                if constexpr (R == 16) buf[sidx(dst[i] + Dft<T, 16, SIGN>::out_index(r) * Ns)] = v[i][r];
+                else buf[sidx(dst[i] + r * Ns)] = v[i][r];
+            }
         }
     }
     __syncthreads();

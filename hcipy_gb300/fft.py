@@ -319,6 +319,19 @@ class ZoomFastFourierTransform(FourierTransform):
         """zoom_fast_fourier_transform.py:95-119."""
         return self._run(field, self.output_grid, self.input_grid, True)
 
+    @property
+    def adjoint_scale(self):
+        """Both directions are exact DFTs on the grids: forward = w_in sum E exp(-i u x), backward = w_out/(2 pi)^d
+        sum F exp(+i u x), so the adjoint of ``forward`` is w_in (2 pi)^d / w_out ``backward``.  Not part of the
+        reference API."""
+        w_in = float(np.prod(np.asarray(self.input_grid.delta, np.float64)))
+        w_out = float(np.prod(np.asarray(self.output_grid.delta, np.float64)))
+        return w_in * (2 * math.pi)**self.ndim / w_out
+
+    def adjoint(self, field):
+        """The conjugate transpose of ``forward``; not part of the reference API."""
+        return Field(self.backward(field).data * self.adjoint_scale, self.input_grid)
+
     @classmethod
     def check_if_supported(cls, input_grid, output_grid):
         if not input_grid.is_regular or not _is_cartesian(input_grid):
