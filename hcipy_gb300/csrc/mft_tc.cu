@@ -768,6 +768,73 @@ __global__ void field_copy_kernel(FieldIO src, FieldIO dst, long long n) {
     }
 }
 
+// L = S (E - alpha T) for one row per CTA, T the inverse transform of the focal-plane field in float-float: the
+// Babinet subtraction and the Lyot stop of the coronagraph (hcipy/coronagraphy/lyot.py:79-90) as a pass of its
+// own.  In the GEMM's epilogue the same arithmetic ran on the epilogue warps of one CTA per SM while the tensor
+// cores idled; here it runs at full occupancy and streams the fields once.  rowmax (optional): the row maximum
+// of max(|Re|, |Im|) as float bits, for the slicing of the next transform.
+template <int SRC, int OUT>
+__global__ void babinet_rows_kernel(FieldIO t, FieldIO src, const float2* __restrict__ stop, cff alpha, int ny, int nx,
+                                    FieldIO out, unsigned int* rowmax) {
+    const long long row = blockIdx.x;
+    const long long base = row * nx;
+    const float2* srow = stop ? stop + (row % ny) * nx : nullptr;
+    const bool real_alpha = alpha.im.hi == 0.0f && alpha.im.lo == 0.0f;
+    const bool imag_alpha = alpha.re.hi == 0.0f && alpha.re.lo == 0.0f;
+    float mx = 0.0f;
+    // U columns per thread per round, all loads issued before the arithmetic
+    constexpr int U = 4;
+    for (int c0 = threadIdx.x; c0 < nx; c0 += U * blockDim.x) {
+        cff v[U], e[U];
+        float2 mk[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int c = c0 + u * blockDim.x;
+            if (c < nx) {
+                v[u] = load_fmt<FMT_FF>(t, base + c);
+                e[u] = load_fmt<SRC>(src, base + c);
+                mk[u] = srow ? __ldg(&srow[c]) : make_float2(1.0f, 0.0f);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int c = c0 + u * blockDim.x;
+            if (c >= nx) continue;
+            cff w = real_alpha   ? cff{ff_mul(v[u].re, alpha.re), ff_mul(v[u].im, alpha.re)}
+                    : imag_alpha ? cff{ff_neg(ff_mul(v[u].im, alpha.im)), ff_mul(v[u].re, alpha.im)}
+                                 : cff_mul(v[u], alpha);
+            w = {ff_add(e[u].re, ff_neg(w.re)), ff_add(e[u].im, ff_neg(w.im))};
+            if (srow) w = mk[u].y == 0.0f ? cff{ff_mulf(w.re, mk[u].x), ff_mulf(w.im, mk[u].x)} : cff_mul_c64(w, mk[u]);
+            store_fmt<OUT>(out, base + c, w);
+            mx = fmaxf(mx, fmaxf(fabsf(w.re.hi), fabsf(w.im.hi)));
+        }
+    }
+    if (!rowmax) return;
+    __shared__ float red[32];
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) mx = fmaxf(mx, red[w]);
+        rowmax[row] = __float_as_uint(mx);
+    }
+}
+
+template <int SRC>
+int launch_babinet_src(FieldIO t, FieldIO src, const float2* stop, cff alpha, long long rows, int ny, int nx,
+                       FieldIO out, int out_fmt, unsigned int* rowmax, cudaStream_t st) {
+    if (rows > 2147483647LL) {
+        set_error("Lyot plane too large");
+        return HX_ERR_UNSUPPORTED;
+    }
+    const dim3 grid((unsigned)rows);
+    if (out_fmt == FMT_FF) babinet_rows_kernel<SRC, FMT_FF><<<grid, 256, 0, st>>>(t, src, stop, alpha, ny, nx, out, rowmax);
+    else if (out_fmt == FMT_C128)
+        babinet_rows_kernel<SRC, FMT_C128><<<grid, 256, 0, st>>>(t, src, stop, alpha, ny, nx, out, rowmax);
+    else babinet_rows_kernel<SRC, FMT_C64><<<grid, 256, 0, st>>>(t, src, stop, alpha, ny, nx, out, rowmax);
+    return launch_status("babinet_rows_kernel");
+}
+
 // ---- host side ------------------------------------------------------------------------------------
 
 inline long long round_up(long long x, long long m) { return (x + m - 1) / m * m; }
@@ -1463,11 +1530,26 @@ int split_lyot_execute(const SplitMftPlan* fpm, const SplitMftPlan* img, int bat
     // E_f = P(E) (1 - M), kept in float-float with its column maxima.
     HX_TRY(split_mft_run(fpm, HX_FORWARD, batch, fe, nullptr, ef, af_re, af_im, HX_EPI_MUL, one_minus_fpm, none,
                          nullptr, ef_colmax, inner, st));
-    // L = S (E - P^-1(E_f)): straight into the caller's Lyot-plane buffer when no image follows, else in
-    // float-float with its row maxima for the image transform.
+    // T = P^-1(E_f) in float-float (a plain epilogue: the GEMM's epilogue warps are few), then
+    // L = S (E - alpha T) in a row pass: straight into the caller's Lyot-plane buffer when no image follows,
+    // else in float-float (in place) with its row maxima for the image transform.
     const bool direct = lyot_out && !img;
-    HX_TRY(split_mft_run(fpm, HX_BACKWARD, batch, ef, ef_colmax, direct ? output_field(lyot_out, lyot_dtype) : lp,
-                         ab_re, ab_im, HX_EPI_BABINET, stop, fe, direct ? nullptr : lp_rowmax, nullptr, inner, st));
+    HX_TRY(split_mft_run(fpm, HX_BACKWARD, batch, ef, ef_colmax, lp, 1.0, 0.0, HX_EPI_NONE, nullptr, none, nullptr,
+                         nullptr, inner, st));
+    {
+        GemmArgs ga;
+        set_alpha(ga, ab_re, ab_im);
+        const cff alpha = {{ga.alpha[0], ga.alpha[1]}, {ga.alpha[2], ga.alpha[3]}};
+        const FieldIO dst = direct ? output_field(lyot_out, lyot_dtype) : lp;
+        const int out_fmt = direct ? output_fmt(dst) : FMT_FF;
+        const long long rows = (long long)batch * fpm->ny;
+        if (e_dtype == HX_C128)
+            HX_TRY(launch_babinet_src<FMT_C128>(lp, fe, stop, alpha, rows, fpm->ny, fpm->nx, dst, out_fmt,
+                                                direct ? nullptr : lp_rowmax, st));
+        else
+            HX_TRY(launch_babinet_src<FMT_C64>(lp, fe, stop, alpha, rows, fpm->ny, fpm->nx, dst, out_fmt,
+                                               direct ? nullptr : lp_rowmax, st));
+    }
     if (lyot_out && !direct) {
         const long long n = batch * pupil;
         field_copy_kernel<<<ceil_div(n, 512), 256, 0, st>>>(lp, output_field(lyot_out, lyot_dtype), n);
