@@ -227,6 +227,35 @@ __device__ __forceinline__ cff load_field(const FieldIO& f, long long i) {
     return load_fmt<FMT_C64>(f, i);
 }
 
+// Elements i .. i+3 of a field, with 16-byte loads where the addresses allow them.
+__device__ __forceinline__ void load4_field(const FieldIO& f, long long i, cff* v) {
+    if (f.re_hi) {
+        const float* p[4] = {f.re_hi + i, f.re_lo + i, f.im_hi + i, f.im_lo + i};
+        if (((reinterpret_cast<uintptr_t>(p[0]) | reinterpret_cast<uintptr_t>(p[1]) | reinterpret_cast<uintptr_t>(p[2]) |
+              reinterpret_cast<uintptr_t>(p[3])) & 15) == 0) {
+            const float4 rh = *reinterpret_cast<const float4*>(p[0]), rl = *reinterpret_cast<const float4*>(p[1]);
+            const float4 ih = *reinterpret_cast<const float4*>(p[2]), il = *reinterpret_cast<const float4*>(p[3]);
+            v[0] = {{rh.x, rl.x}, {ih.x, il.x}};
+            v[1] = {{rh.y, rl.y}, {ih.y, il.y}};
+            v[2] = {{rh.z, rl.z}, {ih.z, il.z}};
+            v[3] = {{rh.w, rl.w}, {ih.w, il.w}};
+            return;
+        }
+    } else if (!f.c128) {
+        if ((reinterpret_cast<uintptr_t>(f.c64 + i) & 15) == 0) {
+            const float4 a = reinterpret_cast<const float4*>(f.c64 + i)[0];
+            const float4 b = reinterpret_cast<const float4*>(f.c64 + i)[1];
+            v[0] = {{a.x, 0.0f}, {a.y, 0.0f}};
+            v[1] = {{a.z, 0.0f}, {a.w, 0.0f}};
+            v[2] = {{b.x, 0.0f}, {b.y, 0.0f}};
+            v[3] = {{b.z, 0.0f}, {b.w, 0.0f}};
+            return;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = load_field(f, i + j);
+}
+
 __device__ __forceinline__ void store_field(const FieldIO& f, long long i, cff v) {
     if (f.re_hi) store_fmt<FMT_FF>(f, i, v);
     else if (f.c128_out) store_fmt<FMT_C128>(f, i, v);
@@ -631,9 +660,16 @@ __global__ void slice_rows_kernel(FieldIO src, long long ld, int K, int Kp, cons
     if (rowmax) {
         mx = __uint_as_float(rowmax[m]);
     } else {
-        for (int k = threadIdx.x; k < K; k += blockDim.x) {
-            const cff v = load_field(src, (long long)m * ld + k);
-            mx = fmaxf(mx, fmaxf(fabsf(v.re.hi), fabsf(v.im.hi)));
+        for (int k0 = 4 * threadIdx.x; k0 < K; k0 += 4 * blockDim.x) {
+            cff v[4];
+            if (k0 + 4 <= K) {
+                load4_field(src, (long long)m * ld + k0, v);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) v[j] = k0 + j < K ? load_field(src, (long long)m * ld + k0 + j) : cff{};
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) mx = fmaxf(mx, fmaxf(fabsf(v[j].re.hi), fabsf(v[j].im.hi)));
         }
         for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
@@ -654,12 +690,17 @@ __global__ void slice_rows_kernel(FieldIO src, long long ld, int K, int Kp, cons
     // Four consecutive K-elements per thread: 8-byte stores into each plane (Kp and kpitch are multiples of 32).
     for (int k0 = 4 * threadIdx.x; k0 < Kp; k0 += 4 * blockDim.x) {
         __half rs[3][4], is[3][4];
+        cff v[4];
+        if (k0 + 4 <= K) {
+            load4_field(src, (long long)m * ld + k0, v);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) v[j] = k0 + j < K ? load_field(src, (long long)m * ld + k0 + j) : cff{};
+        }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            cff v = {{0.0f, 0.0f}, {0.0f, 0.0f}};
-            if (k0 + j < K) v = load_field(src, (long long)m * ld + k0 + j);
-            slice3(v.re, inv, rs[0][j], rs[1][j], rs[2][j]);
-            slice3(v.im, inv, is[0][j], is[1][j], is[2][j]);
+            slice3(v[j].re, inv, rs[0][j], rs[1][j], rs[2][j]);
+            slice3(v[j].im, inv, is[0][j], is[1][j], is[2][j]);
         }
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
