@@ -8,10 +8,11 @@ from .field import (Field, CartesianGrid, RegularCoords, SeparatedCoords, Unstru
                     make_pupil_grid, make_focal_grid, make_focal_grid_from_pupil_grid)
 from .fourier import (FourierTransform, ComputationalComplexity, MatrixFourierTransform, make_fourier_transform,
                       make_fft_grid, get_fft_parameters, is_fft_grid)
-from .optics import (Wavefront, OpticalElement, AgnosticOpticalElement, Apodizer, PhaseApodizer,
+from .optics import (Wavefront, OpticalElement, AgnosticOpticalElement, Apodizer, PhaseApodizer, SurfaceApodizer,
                      make_agnostic_forward, make_agnostic_backward)
 from .propagation import FraunhoferPropagator, AngularSpectrumPropagator, FresnelPropagator
 from .fft import FastFourierTransform, ChirpZTransform, ZoomFastFourierTransform, FourierFilter
+from .wavefront_sensing import PyramidWavefrontSensorOptics
 from .graphs import CapturedCall
 from .coronagraphy import LyotCoronagraph, MultiScaleCoronagraph, VortexCoronagraph
 from .deformable_mirror import (ModeBasis, DeformableMirror, make_actuator_positions,
@@ -29,7 +30,8 @@ __all__ = [
     'Wavefront', 'OpticalElement', 'AgnosticOpticalElement', 'Apodizer', 'PhaseApodizer',
     'make_agnostic_forward', 'make_agnostic_backward',
     'FraunhoferPropagator', 'AngularSpectrumPropagator', 'FresnelPropagator', 'LyotCoronagraph',
-    'MultiScaleCoronagraph', 'VortexCoronagraph', 'CapturedCall', 'HXError',
+    'MultiScaleCoronagraph', 'VortexCoronagraph', 'PyramidWavefrontSensorOptics', 'SurfaceApodizer',
+    'CapturedCall', 'HXError',
     'launch_count',
     'FastFourierTransform', 'ChirpZTransform', 'ZoomFastFourierTransform', 'FourierFilter',
     'ModeBasis', 'DeformableMirror', 'make_actuator_positions', 'make_gaussian_influence_functions',

@@ -239,3 +239,28 @@ class PhaseApodizer(OpticalElement):
 
     def backward(self, wavefront):
         return self._apply(wavefront, -1.0)
+
+
+class SurfaceApodizer(OpticalElement):
+    """A thin transmissive plate of sag ``surface_sag``: E * exp(+-i (n - 1) sag 2 pi / lambda), n the refractive
+    index (a scalar or a function of the wavelength) (hcipy/optics/apodization.py:64-102)."""
+
+    def __init__(self, surface_sag, refractive_index):
+        self.surface_sag = surface_sag
+        self.refractive_index = refractive_index
+
+    def _get_refractive_index(self, wavelength):
+        return self.refractive_index(wavelength) if callable(self.refractive_index) else self.refractive_index
+
+    def _apply(self, wavefront, sign):
+        from .kernels import apply_phase
+        e = wavefront.electric_field
+        scale = sign * (self._get_refractive_index(wavefront.wavelength) - 1) * 2 * np.pi / wavefront.wavelength
+        sag = as_tensor(self.surface_sag, e.data.device)
+        return Wavefront(Field(apply_phase(e.data, sag, scale), e.grid), wavefront.wavelength)
+
+    def forward(self, wavefront):
+        return self._apply(wavefront, 1.0)
+
+    def backward(self, wavefront):
+        return self._apply(wavefront, -1.0)

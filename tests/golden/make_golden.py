@@ -261,6 +261,26 @@ def make_vortex_cases(hp, out):
         out['vortex_%d' % i] = rec
 
 
+def make_pyramid_case(hp, out):
+    """PyramidWavefrontSensorOptics (hcipy/wavefront_sensing/pyramid.py:94-199): forward of an aberrated pupil at
+    two wavelengths (the pyramid phase depends on the refractive index and the wavenumber), backward of a random
+    field on the sensor's pupil plane."""
+    rng = np.random.default_rng(47)
+    pupil = hp.make_pupil_grid(48, 1.0)
+    wfs_grid = hp.make_pupil_grid(96, 2.0)
+    pwfs = hp.PyramidWavefrontSensorOptics(pupil, wfs_grid, separation=1.0, pupil_diameter=1.0, wavelength_0=1.0,
+                                           refractive_index=lambda wl: 1.5 + 0.01 * (wl - 1.0))
+    aperture = hp.make_circular_aperture(1.0)(pupil)
+    e = aperture * np.exp(0.2j * rng.standard_normal(pupil.size))
+    rec = {'E': e, 'G': random_field(rng, wfs_grid)}
+    for k, wl in enumerate((1.0, 1.2)):
+        rec['fwd_%d' % k] = np.asarray(pwfs.forward(hp.Wavefront(hp.Field(e, pupil), wl)).electric_field)
+        rec['wavelength_%d' % k] = np.float64(wl)
+    rec['bwd'] = np.asarray(pwfs.backward(hp.Wavefront(hp.Field(rec['G'], wfs_grid), 1.0)).electric_field)
+    rec.update(grid_record('focal', pwfs.focal_grid))
+    out['pyramid'] = rec
+
+
 def make_lyot_case(hp, out):
     """A 128^2 pupil Lyot chain: focal-plane mask radius 4 lambda/D on a q=8 num_airy=8 grid."""
     pupil = hp.make_pupil_grid(128, 1)
@@ -381,6 +401,7 @@ def main():
     make_asp_cases(hp, out)
     make_fresnel_cases(hp, out)
     make_vortex_cases(hp, out)
+    make_pyramid_case(hp, out)
     make_lyot_case(hp, out)
     make_subpixel_cases(hp, out)
     make_atmosphere_case(hp, out)
