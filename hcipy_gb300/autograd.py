@@ -140,7 +140,13 @@ class LyotFunction(torch.autograd.Function):
         # v = (1 - M)^* . (P^-1)^H u  : forward-direction transform, mask fused in the epilogue
         v = ft._run(u, ft.input_grid, ft.output_grid, _lib.HX_FORWARD, _conj(a_bwd), epilogue=_lib.HX_EPI_MUL,
                     mask=one_minus.conj()).data
-        # E^* = u - P^H v  : adjoint-direction transform, Babinet subtraction fused
-        res = ft._run(v, ft.output_grid, ft.input_grid, _lib.HX_ADJOINT, _conj(a_fwd), epilogue=_lib.HX_EPI_BABINET,
-                      src=u).data
+        # E^* = u - P^H v  : adjoint-direction transform, then the subtraction.  On the CUDA cores the subtraction
+        # is fused into the last GEMM's epilogue; the tensor-core GEMM's epilogue runs on few warps per SM, so
+        # there it is a separate full-occupancy elementwise pass.
+        if ft.precision == 'split':
+            t = ft._run(v, ft.output_grid, ft.input_grid, _lib.HX_ADJOINT, _conj(a_fwd)).data
+            res = u.to(t.dtype) - t
+        else:
+            res = ft._run(v, ft.output_grid, ft.input_grid, _lib.HX_ADJOINT, _conj(a_fwd),
+                          epilogue=_lib.HX_EPI_BABINET, src=u).data
         return res.to(ctx.in_dtype), None, None
