@@ -52,6 +52,8 @@ def parse_args():
     p.add_argument('--no-small', action='store_true', help='skip the 256^2 Fraunhofer and the FFT-family legs')
     p.add_argument('--broadband-frames', type=int, default=256,
                    help='frames of the broadband-through-turbulence leg (0: skip it)')
+    p.add_argument('--lyot-batch', type=int, default=8,
+                   help='fields per step of the batched Lyot leg, FP32 and split (0: skip it)')
     return p.parse_args()
 
 
@@ -487,6 +489,131 @@ def run_broadband(args, dev, peaks):
     }
 
 
+def run_lyot_batched(args, dev, ref_img, peak_img):
+    """The Lyot workload with a batch of pupil fields per step (field 0 is the headline's field, the others carry
+    extra seeded phase noise of 1 mrad RMS), FP32 and split precision, each step replayed from a CUDA graph: the
+    batched form of the chain, where the transforms stack the fields into larger GEMMs."""
+    import torch
+    import hcipy_gb300 as hg
+    w = workload(args)
+    pupil, fpm_grid, focal = w['pupil'], w['fpm_grid'], w['focal']
+    nb = args.lyot_batch
+    rng = np.random.default_rng(17)
+    e = np.repeat(w['E'][None, :].astype(np.complex64), nb, axis=0)
+    e[1:] *= np.exp(1j * 1e-3 * rng.standard_normal((nb - 1, pupil.size))).astype(np.complex64)
+    e_dev = torch.from_numpy(e).to(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    out = {'workload': 'lyot-coronagraph 2048^2 -> 512^2 FPM grid -> 512^2 image, %d fields per step' % nb,
+           'batch': nb}
+    for precision in ('fp32', 'split'):
+        lyot = hg.LyotCoronagraph(pupil, hg.Field(w['fpm'], fpm_grid), hg.Field(w['stop'], pupil),
+                                  precision=precision)
+        prop = hg.FraunhoferPropagator(pupil, focal, precision=precision)
+
+        def step(x):
+            return prop.forward(lyot.forward(hg.Wavefront(hg.Field(x, pupil), 1.0))).electric_field.data
+
+        hg.autotune(not args.no_autotune)
+        graph = hg.CapturedCall(step, e_dev, warmup=3)
+        img = graph(e_dev)
+        torch.cuda.synchronize()
+        steps = 10
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for i in range(steps):
+            flush.fill_(float(i))
+            ev[i][0].record()
+            graph(e_dev)
+            ev[i][1].record()
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+        leg = {'propagations_per_s': nb * 1e3 / ms, 'ms_per_step': ms, 'kernels_in_graph': int(graph.graph_kernels)}
+        if ref_img is not None:
+            leg['ni_err_max_field0'] = dark_hole_error(img[0].cpu().numpy(), ref_img, focal, peak_img)[0]
+        out[precision] = leg
+        del graph, lyot, prop
+    out['split_over_fp32'] = out['split']['propagations_per_s'] / out['fp32']['propagations_per_s']
+    out['timing'] = 'CUDA events around each graph replay, L2 flushed between steps outside the events'
+    return out
+
+
+def run_efc(args, dev):
+    """Electric-field conjugation on the gradient workload's optics (512^2 pupil, 952-actuator DM, Lyot
+    coronagraph, 256^2 image, dark zone = the 3-12 lambda/D half annulus): the poke Jacobian of every actuator
+    (+-1e-3 lambda pokes: 1904 propagations, 64 actuators per call), its Tikhonov inverse (rcond 1e-2, float64
+    SVD on the device) and ten EFC iterations (gain 0.5) against a seeded 0.02 rad RMS pupil aberration."""
+    import torch
+    import hcipy_gb300 as hg
+    from hcipy_gb300 import workloads
+    from oracle import optics
+    w = workloads.dm_gradient_workload()
+    pupil, fpm_grid, focal = w['pupil'], w['fpm_grid'], w['focal']
+    split = args.precision == 'split'
+    lyot = hg.LyotCoronagraph(pupil, hg.Field(w['fpm'], fpm_grid), hg.Field(w['stop'], pupil),
+                              precision=args.precision)
+    prop = hg.FraunhoferPropagator(pupil, focal, precision=args.precision)
+    dm = hg.DeformableMirror(w['influence'], dtype=torch.float64 if split else torch.float32)
+    cdt = torch.complex128 if split else torch.complex64
+    rdt = torch.float64 if split else torch.float32
+    ap = torch.from_numpy(w['aperture'].astype(np.complex128)).to(dev, cdt)
+    rng = np.random.default_rng(21)
+    ab = torch.from_numpy(w['aperture'] * np.exp(0.02j * rng.standard_normal(pupil.size))).to(dev, cdt)
+    nact = w['influence'].num_modes
+    dz = w['roi']
+
+    def measure(e0):
+        def f(cmds):
+            dm.actuators = cmds
+            return prop.forward(lyot.forward(dm.forward(hg.Wavefront(hg.Field(e0, pupil), 1.0)))).electric_field.data
+        return f
+
+    hg.autotune(not args.no_autotune)
+    hg.poke_jacobian(measure(ap), dz, nact, 1e-3, batch=64, dtype=rdt)  # warm-up: plans, workspaces, tiles
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    jac = hg.poke_jacobian(measure(ap), dz, nact, 1e-3, batch=64, dtype=rdt)
+    torch.cuda.synchronize()
+    t_jac = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    em = hg.inverse_tikhonov(jac, 1e-2)
+    torch.cuda.synchronize()
+    t_inv = time.perf_counter() - t0
+    peak = float(prop.forward(hg.Wavefront(hg.Field(ap, pupil), 1.0)).electric_field.data.abs().max())**2
+    dz_dev = torch.from_numpy(dz).to(dev)
+    one = measure(ab)
+    iters = 10
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist, fields = hg.run_efc(lambda a: one(a[None])[0], dz, em, np.zeros(nact), iters, 0.5)
+    torch.cuda.synchronize()
+    t_loop = time.perf_counter() - t0
+    ni = [float((f[dz_dev].abs()**2).mean()) / peak for f in fields]
+    # host: the same pokes through the reference algorithm's port (complex128, matrices precomputed), a bounded
+    # sample of actuators, extrapolated to all of them
+    chain = optics.LyotChain(oracle_grid(pupil), oracle_grid(fpm_grid), oracle_grid(focal), w['fpm'], w['stop'])
+    inf = w['influence'].transformation_matrix
+    e0 = w['aperture'].astype(np.complex128)
+    c0, done = time.perf_counter(), 0
+    for i in range(nact):
+        for a in (-1e-3, 1e-3):
+            chain(optics.dm_forward(e0, inf[:, i].toarray().ravel() * a, 1.0))
+        done += 1
+        if time.perf_counter() - c0 > args.cpu_seconds / 2:
+            break
+    cpu_per_act = (time.perf_counter() - c0) / done
+    return {
+        'workload': '952-actuator DM on 512^2 -> Lyot (512^2 FPM grid) -> 256^2 image; dark zone 3-12 lambda/D, '
+                    'x > 0 (%d pixels)' % int(dz.sum()),
+        'precision': args.precision, 'jacobian_shape': list(jac.shape),
+        'jacobian_s': t_jac, 'propagations_per_s_in_jacobian': 2 * nact / t_jac,
+        'tikhonov_inverse_s': t_inv, 'efc_iterations': iters, 'efc_ms_per_iteration': 1e3 * t_loop / iters,
+        'dark_zone_ni_first_last': [ni[0], ni[-1]],
+        'timing': 'host wall clock with a device synchronize on both sides',
+        'cpu_baseline': {'jacobian_s_estimate': cpu_per_act * nact, 'cores': host_cores(), 'kind': 'port',
+                         'sample': '%d of %d actuators (2 pokes each) through the numpy port, complex128, '
+                                   'extrapolated' % (done, nact)},
+    }
+
+
 def run_dm_probes(args, dev):
     """Pair-wise DM probing, the electric-field-conjugation measurement step: the unprobed field and four probe
     shapes applied with both signs (9 command vectors) through the DM (952 Gaussian actuators on a 512^2 pupil),
@@ -885,6 +1012,8 @@ def run_ours(args, rank, world, dist):
         line['cpu_baseline'] = cpu
     line['config']['autotuned_tiles'] = [
         {'shape': list(shape), 'best': list(c[0]), 'candidates': len(c)} for shape, c in hg._lib.autotune_table()]
+    if args.lyot_batch > 0:
+        line['lyot_batched'] = run_lyot_batched(args, dev, ref_img, peak_img)
     if args.grad_steps > 0:
         line['grad_steps'] = run_grad(args, dev)
     if not args.no_atmosphere:
@@ -893,6 +1022,7 @@ def run_ours(args, rank, world, dist):
         line['broadband_turbulence'] = run_broadband(args, dev, peaks)
     if not args.no_small:
         line['dm_probes'] = run_dm_probes(args, dev)
+        line['efc'] = run_efc(args, dev)
         line['fraunhofer_256'] = run_small_fraunhofer(args, dev, peaks)
         line['fft_family_1024'] = run_fft_family(args, dev, peaks)
     print(json.dumps(line), flush=True)

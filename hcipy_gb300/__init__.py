@@ -20,6 +20,9 @@ from .deformable_mirror import (ModeBasis, DeformableMirror, make_actuator_posit
 from .atmosphere import (AtmosphericLayer, InfiniteAtmosphericLayer, MultiLayerAtmosphere,
                          Cn_squared_from_fried_parameter, fried_parameter_from_Cn_squared, subpixel_shift)
 from .broadband import BroadbandImager, diffraction_scaled_focal_grids
+from .efc import SVD, inverse_tikhonov, inverse_truncated, inverse_truncated_modal, poke_jacobian, efc_step, run_efc
+from .io import (read_fits, write_fits, read_grid, write_grid, read_field, write_field, read_mode_basis,
+                 write_mode_basis)
 from ._lib import HXError, launch_count, autotune
 
 __all__ = [
@@ -38,4 +41,7 @@ __all__ = [
     'find_illuminated_actuators', 'AtmosphericLayer', 'InfiniteAtmosphericLayer', 'MultiLayerAtmosphere',
     'Cn_squared_from_fried_parameter', 'fried_parameter_from_Cn_squared', 'subpixel_shift',
     'BroadbandImager', 'diffraction_scaled_focal_grids', 'autotune',
+    'SVD', 'inverse_tikhonov', 'inverse_truncated', 'inverse_truncated_modal', 'poke_jacobian', 'efc_step',
+    'run_efc', 'read_fits', 'write_fits', 'read_grid', 'write_grid', 'read_field', 'write_field',
+    'read_mode_basis', 'write_mode_basis',
 ]

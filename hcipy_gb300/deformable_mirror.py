@@ -31,6 +31,11 @@ class ModeBasis(object):
         self.grid = grid
         self._device = {}
 
+    def __getstate__(self):
+        state = dict(self.__dict__)
+        state['_device'] = {}  # device copies are rebuilt on first use
+        return state
+
     @property
     def transformation_matrix(self):
         return self._transformation_matrix

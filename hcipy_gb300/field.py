@@ -454,6 +454,10 @@ class Field(object):
         self.data = as_tensor(data)
         self.grid = grid
 
+    def __reduce__(self):
+        # pickles hold host copies; unpickling uploads them to the device again
+        return (Field, (self.data.detach().cpu(), self.grid))
+
     # -- structure --------------------------------------------------------
     @property
     def tensor_shape(self):

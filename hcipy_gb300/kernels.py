@@ -31,7 +31,11 @@ def apply_phase(e, s, scale):
     be = int(np.prod(shape_e)) if shape_e else 1
     bs = int(np.prod(shape_s)) if shape_s else 1
     batch = max(be, bs)
-    out_shape = (shape_e if be >= bs else shape_s) + (n,)
+    try:
+        lead = tuple(torch.broadcast_shapes(shape_e, shape_s))  # keeps a batch of one given on either side
+    except RuntimeError:
+        lead = shape_e if be >= bs else shape_s
+    out_shape = (lead if int(np.prod(lead)) == batch else (shape_e if be >= bs else shape_s)) + (n,)
     e2, s2 = _batched(e, n), _batched(s, n)
     out = torch.empty(out_shape, dtype=e.dtype, device=e.device)
     rc = _lib.lib().hx_phase_apply(n, batch, be, bs, _lib.dptr(e2), _lib.dtype_code(e.dtype), _lib.dptr(s2),

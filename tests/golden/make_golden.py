@@ -384,6 +384,62 @@ def make_dm_case(hp, out):
     }
 
 
+def make_efc_case(hp, out):
+    """Electric-field conjugation on a 32^2 pupil: a 6x6 Gaussian DM, the Lyot coronagraph (radius 2 lambda/D
+    mask) and the lens onto a 32^2 image; the tutorial's poke Jacobian over a one-sided dark zone (2.5-7 lambda/D,
+    x > 0.5), its Tikhonov inverse (hcipy.inverse_tikhonov), five EFC iterations against a seeded aberration; and
+    the three regularised inverses (hcipy/util/matrix_inversion.py) of a seeded ill-conditioned matrix."""
+    rng = np.random.default_rng(48)
+    pupil = hp.make_pupil_grid(32, 1)
+    aperture = hp.make_circular_aperture(1)(pupil)
+    inf = hp.make_gaussian_influence_functions(pupil, 6, 1 / 6, crosstalk=0.15)
+    dm = hp.DeformableMirror(inf)
+    fpm_grid = hp.make_focal_grid(8, 6)
+    fpm = 1 - hp.make_circular_aperture(4)(fpm_grid)
+    stop = hp.make_circular_aperture(0.9)(pupil)
+    lyot = hp.LyotCoronagraph(pupil, fpm, stop)
+    focal = hp.make_focal_grid(2, 8)
+    prop = hp.FraunhoferPropagator(pupil, focal)
+    r = np.hypot(focal.x, focal.y)
+    dark_zone = (r >= 2.5) & (r <= 7) & (focal.x > 0.5)
+    aberration = np.exp(1j * 0.02 * rng.standard_normal(pupil.size)) * aperture
+    epsilon, rcond, gain = 1e-3, 1e-2, 0.5
+
+    def get_field(actuators, aberrated):
+        dm.actuators = actuators
+        e = aberration if aberrated else aperture.astype(complex)
+        return np.asarray(prop(lyot(dm(hp.Wavefront(hp.Field(e, pupil), 1.0)))).electric_field)
+
+    # the tutorial's poke Jacobian (E(+eps) - E(-eps)) eps / var(+-eps), written out for this case
+    amps = np.linspace(-epsilon, epsilon, 2)
+    cols = []
+    for i in range(dm.num_actuators):
+        resp = sum(a * get_field(a * np.eye(dm.num_actuators)[i], False) for a in amps) / np.var(amps)
+        cols.append(np.concatenate((resp[dark_zone].real, resp[dark_zone].imag)))
+    jac = np.array(cols).T
+    efc_matrix = hp.inverse_tikhonov(jac, rcond)
+    act = np.zeros(dm.num_actuators)
+    history, dz_ni = [], []
+    peak = np.abs(np.asarray(prop(hp.Wavefront(hp.Field(aperture.astype(complex), pupil), 1.0)).electric_field)).max()**2
+    for _ in range(5):
+        e = get_field(act, True)
+        history.append(act.copy())
+        dz_ni.append(np.mean(np.abs(e[dark_zone])**2) / peak)
+        x = np.concatenate((e[dark_zone].real, e[dark_zone].imag))
+        act = act - gain * efc_matrix.dot(x)
+    m = rng.standard_normal((40, 12)) @ np.diag(np.logspace(0, -6, 12)) @ rng.standard_normal((12, 12))
+    out['efc'] = {
+        'influence': np.asarray(inf.transformation_matrix.toarray()), 'aperture': np.asarray(aperture),
+        'aberration': np.asarray(aberration), 'fpm': np.asarray(fpm), 'stop': np.asarray(stop),
+        'dark_zone': np.asarray(dark_zone), 'epsilon': np.float64(epsilon), 'rcond': np.float64(rcond),
+        'gain': np.float64(gain), 'jacobian': jac, 'efc_matrix': efc_matrix, 'actuators': np.array(history),
+        'dark_zone_ni': np.array(dz_ni), 'peak': np.float64(peak),
+        'M': m, 'M_tikhonov': hp.inverse_tikhonov(m, 1e-3), 'M_truncated': hp.inverse_truncated(m, 1e-4),
+        'M_modal': hp.inverse_truncated_modal(m, 5),
+        **grid_record('pupil', pupil), **grid_record('fpm', fpm_grid), **grid_record('focal', focal),
+    }
+
+
 def save(out):
     for name, rec in out.items():
         np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
@@ -406,6 +462,7 @@ def main():
     make_subpixel_cases(hp, out)
     make_atmosphere_case(hp, out)
     make_dm_case(hp, out)
+    make_efc_case(hp, out)
     save(out)
 
 

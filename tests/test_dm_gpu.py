@@ -244,3 +244,17 @@ def test_gradient_matches_oracle_poke_jacobian(precision):
         am[i] -= h
         jac[i] = (oracle_loss(ap) - oracle_loss(am)) / (2 * h)
     assert np.linalg.norm(grad - jac) < 1e-6 * np.linalg.norm(jac), np.linalg.norm(grad - jac) / np.linalg.norm(jac)
+
+
+def test_batch_of_one_keeps_its_dimension():
+    """Commands of shape (1, nact) on an unbatched field give a (1, npix) field, as a batch of one must."""
+    pupil = hg.make_pupil_grid(32, 1)
+    dm = hg.DeformableMirror(hg.make_gaussian_influence_functions(pupil, 6, 1 / 6))
+    e = torch.ones(pupil.size, dtype=torch.complex64, device='cuda')
+    cmd = torch.full((1, dm.num_actuators), 1e-3, device='cuda')
+    dm.actuators = cmd
+    out = dm.forward(hg.Wavefront(hg.Field(e, pupil), 1.0)).electric_field.data
+    assert out.shape == (1, pupil.size)
+    dm.actuators = cmd[0]
+    single = dm.forward(hg.Wavefront(hg.Field(e, pupil), 1.0)).electric_field.data
+    assert single.shape == (pupil.size,) and torch.equal(single, out[0])

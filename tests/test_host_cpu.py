@@ -83,3 +83,18 @@ def test_oracle_grid_factories_agree_with_package():
     b = ogrids.make_focal_grid(2.5, (5, 7))
     np.testing.assert_array_equal(a.dims, b.dims)
     np.testing.assert_allclose(a.zero, b.zero)
+
+
+def test_efc_rejects_mismatched_fields(monkeypatch):
+    """The EFC helpers check the field size against the dark-zone mask on the host, before any device gather
+    (host tensors stand in for the device here)."""
+    import torch
+    from hcipy_gb300 import efc
+    monkeypatch.setattr(efc, '_DEVICE', 'cpu')
+    dz = np.zeros(16, bool)
+    dz[3] = True
+    with pytest.raises(ValueError):
+        efc.efc_step(np.zeros((2, 2)), torch.zeros(1, dtype=torch.complex128), dz, np.zeros(2), 0.5)
+    with pytest.raises(ValueError):
+        efc.poke_jacobian(lambda c: torch.zeros(c.shape[0], 4, dtype=torch.complex128), torch.from_numpy(dz), 2,
+                          1e-3)

@@ -174,3 +174,29 @@ def test_dm_oracle():
     surf = optics.dm_surface(g['influence'], g['actuators'])
     np.testing.assert_allclose(surf, g['surface'], rtol=1e-12, atol=1e-18)
     np.testing.assert_allclose(optics.dm_forward(g['E'], surf, 1.0), g['fwd_c128'], rtol=1e-12, atol=1e-14)
+
+
+def test_efc_oracle():
+    """The regularised inverses and the tutorial's poke Jacobian / EFC loop, restated in numpy, against the
+    reference run on the same seeded 32^2 case."""
+    from oracle import efc
+    g = load_golden('efc')
+    m = g['M']
+    assert rel_err(efc.inverse_tikhonov(m, 1e-3), g['M_tikhonov']) < 1e-10
+    assert rel_err(efc.inverse_truncated(m, 1e-4), g['M_truncated']) < 1e-10
+    assert rel_err(efc.inverse_truncated_modal(m, 5), g['M_modal']) < 1e-10
+    pupil, fpm_grid, focal = grid_from(g, 'pupil'), grid_from(g, 'fpm'), grid_from(g, 'focal')
+    inf, dz = g['influence'], g['dark_zone']
+
+    def field(act, e):
+        e = optics.dm_forward(e, inf @ act, 1.0)
+        return optics.fraunhofer_forward(optics.lyot_forward(e, pupil, fpm_grid, g['fpm'], g['stop']), pupil, focal)
+
+    jac = efc.poke_jacobian(lambda c: field(c, g['aperture'].astype(complex)), dz, inf.shape[1], g['epsilon'])
+    assert rel_err(jac, g['jacobian']) < 1e-8
+    em = efc.inverse_tikhonov(g['jacobian'], g['rcond'])
+    assert rel_err(em, g['efc_matrix']) < 1e-10
+    act = g['actuators'][0]
+    for k in range(1, len(g['actuators'])):
+        act = efc.efc_step(em, field(act, g['aberration']), dz, act, g['gain'])
+        assert rel_err(act, g['actuators'][k]) < 1e-9
