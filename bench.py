@@ -581,6 +581,7 @@ def run_efc(args, dev):
     dz_dev = torch.from_numpy(dz).to(dev)
     one = measure(ab)
     iters = 10
+    hg.run_efc(lambda a: one(a[None])[0], dz, em, np.zeros(nact), 1, 0.5)  # warm-up: single-field plans, tiles
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     hist, fields = hg.run_efc(lambda a: one(a[None])[0], dz, em, np.zeros(nact), iters, 0.5)

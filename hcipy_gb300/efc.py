@@ -32,6 +32,22 @@ def _back(t, as_tensor):
     return t if as_tensor else t.cpu().numpy()
 
 
+def _thin_svd(m):
+    """M = U diag(S) Vt (S descending).  A tall matrix (a Jacobian: twice the dark-zone pixels by the actuators)
+    goes through a QR factorisation first, M = Q R, so the SVD proper runs on the small square R and U = Q U_R;
+    a wide one through its transpose.  On the device the square SVD uses cuSOLVER's QR-iteration driver."""
+    rows, cols = m.shape[-2], m.shape[-1]
+    kw = {'driver': 'gesvd'} if m.is_cuda else {}
+    if rows >= 2 * cols:
+        q, r = torch.linalg.qr(m, mode='reduced')
+        ur, s, vt = torch.linalg.svd(r, full_matrices=False, **kw)
+        return q @ ur, s, vt
+    if cols >= 2 * rows:
+        u, s, vt = _thin_svd(m.mT)
+        return vt.mT, s, u.mT
+    return torch.linalg.svd(m, full_matrices=False, **kw)
+
+
 class SVD(object):
     """Thin singular value decomposition on the device (hcipy/util/singular_value_decomposition.py:7-120).
 
@@ -44,7 +60,7 @@ class SVD(object):
         if matrix is None:
             raise ValueError('You need to supply a matrix.')
         m, self._tensor = _device_matrix(matrix)
-        u, s, vt = torch.linalg.svd(m, full_matrices=False)
+        u, s, vt = _thin_svd(m)
         if num_modes is not None:
             num_modes = int(num_modes)
             u, s, vt = u[:, :num_modes], s[:num_modes], vt[:num_modes]
