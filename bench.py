@@ -1012,7 +1012,8 @@ def run_ours(args, rank, world, dist):
     if cpu is not None:
         line['cpu_baseline'] = cpu
     line['config']['autotuned_tiles'] = [
-        {'shape': list(shape), 'best': list(c[0]), 'candidates': len(c)} for shape, c in hg._lib.autotune_table()]
+        {'shape': list(shape), 'best': list(c[0]), 'measured': [list(x) for x in c]}
+        for shape, c in hg._lib.autotune_table()]
     if args.lyot_batch > 0:
         line['lyot_batched'] = run_lyot_batched(args, dev, ref_img, peak_img)
     if args.grad_steps > 0:

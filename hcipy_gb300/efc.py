@@ -105,7 +105,21 @@ def _factors(matrix, svd):
 
 
 def inverse_tikhonov(M, rcond=1e-15, svd=None):
-    """Tikhonov-regularised inverse (matrix_inversion.py:68-98): Vt^T diag(s / (s^2 + (rcond s_max)^2)) U^T."""
+    """Tikhonov-regularised inverse (matrix_inversion.py:68-98): Vt^T diag(s / (s^2 + (rcond s_max)^2)) U^T.
+
+    The same matrix is (M^T M + a^2 I)^-1 M^T with a = rcond s_max.  For a real M, no decomposition given and
+    rcond >= 1e-4 it is computed that way: the Gram matrix, its largest eigenvalue and a Cholesky solve, all
+    BLAS3-shaped, where the SVD takes ten times longer on the device.  The regularised Gram matrix has condition
+    number at most 1 + rcond^-2, so the float64 result keeps at least 8 significant digits; a smaller rcond,
+    complex matrices or a given ``svd`` go through the SVD as in the reference.
+    """
+    if svd is None and float(rcond) >= 1e-4:
+        m, as_tensor = _device_matrix(M)
+        if not m.is_complex():
+            g = m.mT @ m
+            a2 = float(rcond)**2 * float(torch.linalg.eigvalsh(g)[-1])
+            g.diagonal().add_(a2)
+            return _back(torch.cholesky_solve(m.mT.contiguous(), torch.linalg.cholesky(g)), as_tensor)
     u, s, vt, as_tensor = _factors(M, svd)
     s_inv = s / (s**2 + (float(rcond) * s.max())**2)
     return _back((vt.T * s_inv.to(vt.dtype)) @ u.T, as_tensor)

@@ -98,3 +98,22 @@ def test_efc_rejects_mismatched_fields(monkeypatch):
     with pytest.raises(ValueError):
         efc.poke_jacobian(lambda c: torch.zeros(c.shape[0], 4, dtype=torch.complex128), torch.from_numpy(dz), 2,
                           1e-3)
+
+
+# rcond = 1e-15 is the plain pseudo-inverse of a matrix of condition ~1e8: two SVD algorithms (QR first, or not)
+# agree there only to ~condition x machine epsilon.
+@pytest.mark.parametrize('rcond,tol', [(1e-2, 1e-11), (1e-3, 1e-9), (1e-5, 1e-9), (1e-15, 1e-7)])
+def test_tikhonov_paths_agree_with_the_svd_form(monkeypatch, rcond, tol):
+    """inverse_tikhonov's Gram/Cholesky form (rcond >= 1e-4) and its SVD form (smaller rcond) against the numpy
+    restatement of the reference's SVD formula, on an ill-conditioned matrix (host tensors stand in for the
+    device)."""
+    import torch
+    from conftest import rel_err
+    from hcipy_gb300 import efc
+    from oracle import efc as oefc
+    monkeypatch.setattr(efc, '_DEVICE', 'cpu')
+    rng = np.random.default_rng(5)
+    m = rng.standard_normal((60, 16)) @ np.diag(np.logspace(0, -8, 16)) @ rng.standard_normal((16, 16))
+    assert rel_err(efc.inverse_tikhonov(m, rcond), oefc.inverse_tikhonov(m, rcond)) < tol
+    out = efc.inverse_tikhonov(torch.from_numpy(m), rcond)
+    assert isinstance(out, torch.Tensor) and rel_err(out.numpy(), oefc.inverse_tikhonov(m, rcond)) < tol
