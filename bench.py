@@ -573,10 +573,12 @@ def run_efc(args, dev):
     jac = hg.poke_jacobian(measure(ap), dz, nact, 1e-3, batch=64, dtype=rdt)
     torch.cuda.synchronize()
     t_jac = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    em = hg.inverse_tikhonov(jac, 1e-2)
-    torch.cuda.synchronize()
-    t_inv = time.perf_counter() - t0
+    t_inv = []
+    for _ in range(2):  # the first call also creates the process's solver handles
+        t0 = time.perf_counter()
+        em = hg.inverse_tikhonov(jac, 1e-2)
+        torch.cuda.synchronize()
+        t_inv.append(time.perf_counter() - t0)
     peak = float(prop.forward(hg.Wavefront(hg.Field(ap, pupil), 1.0)).electric_field.data.abs().max())**2
     dz_dev = torch.from_numpy(dz).to(dev)
     one = measure(ab)
@@ -606,7 +608,7 @@ def run_efc(args, dev):
                     'x > 0 (%d pixels)' % int(dz.sum()),
         'precision': args.precision, 'jacobian_shape': list(jac.shape),
         'jacobian_s': t_jac, 'propagations_per_s_in_jacobian': 2 * nact / t_jac,
-        'tikhonov_inverse_s': t_inv, 'efc_iterations': iters, 'efc_ms_per_iteration': 1e3 * t_loop / iters,
+        'tikhonov_inverse_s': t_inv[1], 'tikhonov_first_call_s': t_inv[0], 'efc_iterations': iters, 'efc_ms_per_iteration': 1e3 * t_loop / iters,
         'dark_zone_ni_first_last': [ni[0], ni[-1]],
         'timing': 'host wall clock with a device synchronize on both sides',
         'cpu_baseline': {'jacobian_s_estimate': cpu_per_act * nact, 'cores': host_cores(), 'kind': 'port',
