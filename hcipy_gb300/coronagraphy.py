@@ -87,6 +87,8 @@ class LyotCoronagraph(OpticalElement):
         lead = tuple(t.shape[:-1])
         batch = int(np.prod(lead)) if lead else 1
         out = torch.empty(lead + (t.shape[-1],), dtype=torch.complex128 if split else t.dtype, device=t.device)
+        if batch == 0:
+            return out
         plan = ft._plan(t.dtype)
         lib = _lib.lib()
         nbytes = int(lib.hx_lyot_workspace_bytes(plan.handle, None, batch))

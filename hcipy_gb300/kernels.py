@@ -30,7 +30,7 @@ def apply_phase(e, s, scale):
     shape_e, shape_s = tuple(e.shape[:-1]), tuple(s.shape[:-1])
     be = int(np.prod(shape_e)) if shape_e else 1
     bs = int(np.prod(shape_s)) if shape_s else 1
-    batch = max(be, bs)
+    batch = max(be, bs) if be and bs else 0  # an empty batch on either side gives an empty result
     try:
         lead = tuple(torch.broadcast_shapes(shape_e, shape_s))  # keeps a batch of one given on either side
     except RuntimeError:
@@ -38,6 +38,8 @@ def apply_phase(e, s, scale):
     out_shape = (lead if int(np.prod(lead)) == batch else (shape_e if be >= bs else shape_s)) + (n,)
     e2, s2 = _batched(e, n), _batched(s, n)
     out = torch.empty(out_shape, dtype=e.dtype, device=e.device)
+    if out.numel() == 0:
+        return out
     rc = _lib.lib().hx_phase_apply(n, batch, be, bs, _lib.dptr(e2), _lib.dtype_code(e.dtype), _lib.dptr(s2),
                                    float(scale), _lib.dptr(out), _lib.stream_handle())
     _lib.check(rc, 'hx_phase_apply')
@@ -52,11 +54,13 @@ def apply_phase_grad(e, s, scale, g_out, need_e=True, need_s=True):
     shape_e, shape_s = tuple(e.shape[:-1]), tuple(s.shape[:-1])
     be = int(np.prod(shape_e)) if shape_e else 1
     bs = int(np.prod(shape_s)) if shape_s else 1
-    batch = max(be, bs)
+    batch = max(be, bs) if be and bs else 0  # an empty batch on either side gives an empty result
     e2, s2 = _batched(e, n), _batched(s, n)
     g2 = _batched(g_out.to(e.dtype), n)
     g_e = torch.empty(shape_e + (n,), dtype=e.dtype, device=e.device) if need_e else None
     g_s = torch.empty(shape_s + (n,), dtype=rdt, device=e.device) if need_s else None
+    if batch == 0 or n == 0:  # an empty batch contributes nothing to a shared input's gradient
+        return (None if g_e is None else g_e.zero_()), (None if g_s is None else g_s.zero_())
     rc = _lib.lib().hx_phase_apply_grad(n, batch, be, bs, _lib.dptr(e2), _lib.dtype_code(e.dtype), _lib.dptr(s2),
                                         float(scale), _lib.dptr(g2), None if g_s is None else _lib.dptr(g_s),
                                         None if g_e is None else _lib.dptr(g_e), _lib.stream_handle())
@@ -88,6 +92,8 @@ class SparseBasis(object):
         lead = tuple(coeffs.shape[:-1])
         c = _batched(coeffs.to(device=self.vals.device, dtype=self.dtype), nact)
         out = torch.empty(lead + (npix,), dtype=self.dtype, device=self.vals.device)
+        if out.numel() == 0:
+            return out
         rc = _lib.lib().hx_influence_apply(npix, nact, _lib.dptr(self.row_ptr), _lib.dptr(self.col_idx),
                                            _lib.dptr(self.vals), _lib.dtype_code(self.dtype), c.shape[0],
                                            _lib.dptr(c), _lib.dptr(out), _lib.stream_handle())
@@ -100,6 +106,8 @@ class SparseBasis(object):
         lead = tuple(g.shape[:-1])
         g2 = _batched(g.to(device=self.vals.device, dtype=self.dtype), npix)
         out = torch.empty(lead + (nact,), dtype=self.dtype, device=self.vals.device)
+        if out.numel() == 0:
+            return out
         rc = _lib.lib().hx_influence_apply_transpose(npix, nact, _lib.dptr(self.col_ptr), _lib.dptr(self.row_idx),
                                                      _lib.dptr(self.vals_csc), _lib.dtype_code(self.dtype),
                                                      g2.shape[0], _lib.dptr(g2), _lib.dptr(out),
