@@ -9,7 +9,8 @@
 // a0 b2 + a1 b1 + a2 b0 | a1 b2 + a2 b1) into four FP32 accumulators in TMEM;
 // the dropped level (a2 b2) weighs at most 2^-36, so ~29 bits of each operand
 // survive.  The level-0 products are integers of magnitude <= 2^12, so their
-// FP32 sum is exact up to 4096 terms (K' = 2K <= 4096); the other levels carry
+// FP32 sum is exact up to 4096 terms: a CTA sums at most K' = 4096, and a
+// longer K' is split across CTAs (see split K below); the other levels carry
 // 2^-11, 2^-22 and 2^-33 of the weight, so their FP32 rounding sits far below
 // 2^-29.  This removes the FP32 accumulation error of the plain path, which
 // dominates a coronagraph's dark hole (its normalized-intensity error is
@@ -64,7 +65,9 @@ constexpr int A_PLANE_BYTES = BM * BK * 2;
 constexpr int A_STAGE_BYTES = NSLICE * A_PLANE_BYTES;
 constexpr int NUM_THREADS = 320;  // TMA warp, MMA warp, 8 epilogue warps
 constexpr uint64_t WAIT_LIMIT = 2000000000ull;  // 2 s per wait
-constexpr int MAX_KPITCH = 4096;                // exact level-0 sums need K' <= 4096
+constexpr int MAX_SPLIT_K = 4096;               // exact level-0 sums need at most 4096 K' per CTA
+constexpr int MAX_SPLIT_KTILES = MAX_SPLIT_K / BK;
+constexpr int MAX_GRID_POINTS = 8192;           // points per axis of a split plan
 constexpr int EXTRA_BYTES = 1024 + 1664;        // alignment slack, barriers, flags, per-row tables
 
 // Tile of BN output columns: four level accumulators of BN TMEM columns each, so BN = 128 takes all
@@ -1021,12 +1024,15 @@ void forced_tiles(int* bn, int* ks) {
     *ks = forced_split;
 }
 
+// A CTA sums at most MAX_SPLIT_KTILES K-steps (its level-0 FP32 sum stays exact), so a longer K is always split
+// across CTAs, whose float-float partials the last CTA of the tile adds.
 TileChoice make_choice(long long m_tiles, int N, int grid_z, int ktiles, int bn, int ksplit) {
     TileChoice c;
     c.bn = bn;
     c.n_tiles = (int)ceil_div(N, bn);
     c.tiles = m_tiles * c.n_tiles * grid_z;
-    c.ksplit = std::max(1, std::min(ksplit, std::max(1, ktiles / 4)));
+    const int min_split = (int)ceil_div(ktiles, MAX_SPLIT_KTILES);
+    c.ksplit = std::max(min_split, std::max(1, std::min(ksplit, std::max(1, ktiles / 4))));
     return c;
 }
 
@@ -1042,7 +1048,7 @@ std::vector<TileChoice> tile_candidates(long long m_tiles, int N, int grid_z, in
         const TileChoice c1 = make_choice(m_tiles, N, grid_z, ktiles, bn, 1);
         v.push_back(c1);
         const TileChoice c2 = make_choice(m_tiles, N, grid_z, ktiles, bn, fill_split(c1.tiles, sms));
-        if (c2.ksplit > 1) v.push_back(c2);
+        if (c2.ksplit > c1.ksplit) v.push_back(c2);
     }
     return v;
 }
@@ -1456,8 +1462,8 @@ int split_mft_create(int nx, int ny, int nu, int nv, const double* x, const doub
                      const double* v, const double* wx, const double* wy, const double* wu, const double* wv,
                      cudaStream_t st, SplitMftPlan** out) {
     *out = nullptr;
-    if (2 * round_up(std::max(std::max(nx, ny), std::max(nu, nv)), 32) > MAX_KPITCH) {
-        set_error("the split tensor-core MFT takes grids of at most %d points per axis", MAX_KPITCH / 2);
+    if (std::max(std::max(nx, ny), std::max(nu, nv)) > MAX_GRID_POINTS) {
+        set_error("the split tensor-core MFT takes grids of at most %d points per axis", MAX_GRID_POINTS);
         return HX_ERR_UNSUPPORTED;
     }
     SplitMftPlan* p = new SplitMftPlan();

@@ -174,3 +174,30 @@ def test_split_throughput_schedule_all_directions():
     assert mft._plan(torch.complex64).status() == 0
     with pytest.raises(ValueError):
         mft.schedule = 'fastest'
+
+
+def test_split_beyond_one_cta_exact_range():
+    """A CTA's level-0 sum is exact up to K' = 4096, so a 2080-point axis (K' = 4160) is always split across
+    CTAs (float-float partials): forward and backward against the float64 oracle at the split tolerance.  Grids
+    beyond 8192 points per axis are refused loudly (HX_ERR_UNSUPPORTED) before anything is allocated."""
+    pupil = hg.make_pupil_grid(2080, 1)
+    focal = hg.make_focal_grid(2, 6)
+    uv = focal.scaled(2 * np.pi)
+    mft = hg.MatrixFourierTransform(pupil, uv, precision='split')
+    rng = np.random.default_rng(12)
+    e = (rng.standard_normal(pupil.size) + 1j * rng.standard_normal(pupil.size)).astype(np.complex64)
+    x, y = pupil.separated_coords
+    u, v = uv.separated_coords
+    w_in = float(np.asarray(pupil.weights).ravel()[0])
+    fwd = mft.forward(hg.Field(torch.from_numpy(e).cuda(), pupil)).data.cpu().numpy()
+    ref = ofourier.mft_forward(e.astype(np.complex128), x, y, u, v, w_in)
+    assert rel_err(fwd, ref) < 2e-8, rel_err(fwd, ref)
+    f = (rng.standard_normal(uv.size) + 1j * rng.standard_normal(uv.size)).astype(np.complex64)
+    w_out = float(np.asarray(uv.weights).ravel()[0])
+    back = mft.backward(hg.Field(torch.from_numpy(f).cuda(), uv)).data.cpu().numpy()
+    ref_b = ofourier.mft_backward(f.astype(np.complex128), x, y, u, v, w_out)
+    assert rel_err(back, ref_b) < 2e-8, rel_err(back, ref_b)
+    big = hg.make_pupil_grid(8200, 1)
+    mft_big = hg.MatrixFourierTransform(big, uv, precision='split')
+    with pytest.raises(hg.HXError, match='at most 8192 points per axis'):
+        mft_big.forward(hg.Field(torch.ones(big.size, dtype=torch.complex64, device='cuda'), big))
