@@ -56,11 +56,11 @@ extern "C" {
 
 /* Arithmetic of the MFT GEMMs. */
 #define HX_PREC_FP32 0  /* FP32 CUDA-core complex GEMM (HX_C64) or FP64 (HX_C128) */
-#define HX_PREC_SPLIT 1 /* split-operand tensor-core GEMM on tcgen05 */
+#define HX_PREC_SPLIT 1 /* split-operand tensor-core GEMM on tcgen05 (grids up to 8192 points per axis) */
 
 /* Tile policy of a plan's GEMMs (no counterpart in the reference). */
 #define HX_SCHEDULE_LATENCY 0    /* fill the GPU with this transform alone (splits K for small shapes) */
-#define HX_SCHEDULE_THROUGHPUT 1 /* other transforms run beside it: least SM time, no K split */
+#define HX_SCHEDULE_THROUGHPUT 1 /* other transforms run beside it: least SM time, K split only past K' = 4096 */
 
 /* Message of the last failure on this thread ("" if none). */
 HX_API const char* hx_last_error(void);
@@ -172,7 +172,8 @@ HX_API int hx_mft_plan_status(const hx_mft_plan* plan, int reset);
 
 /* Tile policy of the plan's GEMMs, HX_SCHEDULE_LATENCY (default) or HX_SCHEDULE_THROUGHPUT, for plans whose
  * transforms run concurrently with others (several streams, or parallel branches of a CUDA graph): small
- * transforms then take the tile with the least SM time instead of splitting K to fill the GPU alone, and the
+ * transforms then take the tile with the least SM time instead of splitting K to fill the GPU alone (a split
+ * tensor-core GEMM still splits a contraction longer than 4096 real terms, to keep its sums exact), and the
  * autotuner's measurements are ranked by duration x occupied SMs; FP32/FP64 plans keep their widest CUDA-core
  * tile instead of narrowing it to occupy the GPU. */
 HX_API int hx_mft_plan_set_schedule(hx_mft_plan* plan, int schedule);
