@@ -242,7 +242,7 @@ def run_grad(args, dev):
         dm.actuators = a
         e = dm.forward(hg.Wavefront(hg.Field(e0, pupil), 1.0))
         img = prop.forward(lyot.forward(e)).electric_field.data
-        loss = ((img.real**2 + img.imag**2) * roi).sum()
+        loss = hg.intensity_sum(img, roi).sum()  # compensated dark-hole sums, fused, with their own backward
         loss.backward()
         return loss, a.grad
 

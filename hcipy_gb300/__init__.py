@@ -21,6 +21,7 @@ from .atmosphere import (AtmosphericLayer, InfiniteAtmosphericLayer, MultiLayerA
                          Cn_squared_from_fried_parameter, fried_parameter_from_Cn_squared, subpixel_shift)
 from .broadband import BroadbandImager, diffraction_scaled_focal_grids
 from .efc import SVD, inverse_tikhonov, inverse_truncated, inverse_truncated_modal, poke_jacobian, efc_step, run_efc
+from .metrics import intensity_sum, mean_intensity_in_roi
 from .io import (read_fits, write_fits, read_grid, write_grid, read_field, write_field, read_mode_basis,
                  write_mode_basis)
 from ._lib import HXError, launch_count, autotune
@@ -43,5 +44,5 @@ __all__ = [
     'BroadbandImager', 'diffraction_scaled_focal_grids', 'autotune',
     'SVD', 'inverse_tikhonov', 'inverse_truncated', 'inverse_truncated_modal', 'poke_jacobian', 'efc_step',
     'run_efc', 'read_fits', 'write_fits', 'read_grid', 'write_grid', 'read_field', 'write_field',
-    'read_mode_basis', 'write_mode_basis',
+    'read_mode_basis', 'write_mode_basis', 'intensity_sum', 'mean_intensity_in_roi',
 ]

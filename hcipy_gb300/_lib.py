@@ -57,6 +57,9 @@ SIGNATURES = {
     'hx_autotune_entries': (c_int, []),
     'hx_autotune_entry': (c_int, [c_int, P(c_ll), P(c_int), P(c_int), P(c_int), P(ctypes.c_float)]),
     'hx_autotune_clear': (c_int, []),
+    'hx_intensity_sums_workspace_bytes': (c_size_t, [c_ll, c_int]),
+    'hx_intensity_sums': (c_int, [c_void_p, c_int, c_ll, c_int, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    'hx_intensity_sums_grad': (c_int, [c_void_p, c_int, c_ll, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     'hx_influence_apply': (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p,
                                    c_void_p]),
     'hx_influence_apply_transpose': (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p,

@@ -150,3 +150,22 @@ class LyotFunction(torch.autograd.Function):
             res = ft._run(v, ft.output_grid, ft.input_grid, _lib.HX_ADJOINT, _conj(a_fwd),
                           epilogue=_lib.HX_EPI_BABINET, src=u).data
         return res.to(ctx.in_dtype), None, None
+
+
+class _IntensitySumFunction(torch.autograd.Function):
+    """Weighted intensity sums per field; the backward pass is one kernel, 2 g w E."""
+
+    @staticmethod
+    def forward(ctx, e, w):
+        ctx.save_for_backward(e)
+        ctx.w = w
+        return kernels.intensity_sums(e, w)
+
+    @staticmethod
+    def backward(ctx, g):
+        e, = ctx.saved_tensors
+        return kernels.intensity_sums_grad(e, ctx.w, g), None
+
+
+def intensity_sum_apply(e, w):
+    return _IntensitySumFunction.apply(e, w)

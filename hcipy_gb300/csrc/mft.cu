@@ -348,4 +348,27 @@ int hx_autotune_clear(void) {
     return HX_OK;
 }
 
+size_t hx_intensity_sums_workspace_bytes(long long n, int batch) { return hx::intensity_sums_workspace_bytes(n, batch); }
+
+int hx_intensity_sums(const void* field, int dtype, long long n, int batch, const float* weights, double* sums,
+                      void* workspace, size_t workspace_bytes, void* stream) {
+    HX_CHECK_ARG(n > 0 && batch > 0, "hx_intensity_sums: sizes must be positive");
+    HX_CHECK_ARG(field && sums, "hx_intensity_sums: NULL pointer");
+    HX_CHECK_ARG(dtype == HX_C64 || dtype == HX_C128, "hx_intensity_sums: dtype must be HX_C64 or HX_C128");
+    const size_t need = hx::intensity_sums_workspace_bytes(n, batch);
+    HX_CHECK_ARG(workspace != nullptr && workspace_bytes >= need, "hx_intensity_sums: workspace of %zu bytes needed",
+                 need);
+    if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
+    return hx::intensity_sums(field, dtype, n, batch, weights, sums, workspace, (cudaStream_t)stream);
+}
+
+int hx_intensity_sums_grad(const void* field, int dtype, long long n, int batch, const float* weights,
+                           const double* grad, void* out, void* stream) {
+    HX_CHECK_ARG(n > 0 && batch > 0, "hx_intensity_sums_grad: sizes must be positive");
+    HX_CHECK_ARG(field && grad && out, "hx_intensity_sums_grad: NULL pointer");
+    HX_CHECK_ARG(dtype == HX_C64 || dtype == HX_C128, "hx_intensity_sums_grad: dtype must be HX_C64 or HX_C128");
+    if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
+    return hx::intensity_sums_grad(field, dtype, n, batch, weights, grad, out, (cudaStream_t)stream);
+}
+
 }  // extern "C"

@@ -1658,4 +1658,125 @@ void split_mft_destroy(SplitMftPlan* p) {
     delete p;
 }
 
+// ---- weighted intensity sums (the dark-hole contrast) -------------------------------------------------
+//
+// sums[b] = sum_p w[p] |E_b[p]|^2 with float-float products and a compensated (float-float) accumulation on the
+// FP32 pipe: per-chunk partials in a fixed reduction order, then one warp per field adds its chunks in order,
+// so the result does not depend on scheduling.  Its gradient (torch's convention for a real loss of complex
+// fields) is 2 g_b w[p] E_b[p].
+
+namespace {
+
+constexpr int INT_THREADS = 256;
+constexpr int INT_CHUNK = INT_THREADS * 32;  // pixels per CTA of the partial pass
+
+__device__ __forceinline__ ff warp_sum_ff(ff v) {
+    for (int o = 16; o > 0; o >>= 1)
+        v = ff_add(v, ff{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)});
+    return v;
+}
+
+template <int SRC>
+__global__ void __launch_bounds__(INT_THREADS) intensity_partial_kernel(FieldIO f, long long n,
+                                                                        const float* __restrict__ w,
+                                                                        float2* partial) {
+    const int b = blockIdx.y;
+    const long long p0 = (long long)blockIdx.x * INT_CHUNK;
+    const long long p1 = min(n, p0 + INT_CHUNK);
+    ff acc = {0.0f, 0.0f};
+    for (long long p = p0 + threadIdx.x; p < p1; p += INT_THREADS) {
+        const cff v = load_fmt<SRC>(f, (long long)b * n + p);
+        ff s = ff_add(ff_mul(v.re, v.re), ff_mul(v.im, v.im));
+        if (w) s = ff_mulf(s, __ldg(&w[p]));
+        acc = ff_add(acc, s);
+    }
+    __shared__ float2 red[INT_THREADS / 32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    acc = warp_sum_ff(acc);
+    if (lane == 0) red[warp] = make_float2(acc.hi, acc.lo);
+    __syncthreads();
+    if (warp == 0) {
+        acc = lane < INT_THREADS / 32 ? ff{red[lane].x, red[lane].y} : ff{0.0f, 0.0f};
+        acc = warp_sum_ff(acc);
+        if (lane == 0) partial[(long long)b * gridDim.x + blockIdx.x] = make_float2(acc.hi, acc.lo);
+    }
+}
+
+__global__ void intensity_final_kernel(const float2* __restrict__ partial, int nchunks, int batch,
+                                       double* sums) {
+    const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (b >= batch) return;
+    ff acc = {0.0f, 0.0f};
+    for (int c = lane; c < nchunks; c += 32) {
+        const float2 q = partial[(long long)b * nchunks + c];
+        acc = ff_add(acc, ff{q.x, q.y});
+    }
+    acc = warp_sum_ff(acc);
+    if (lane == 0) sums[b] = ff_to_double(acc);
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(INT_THREADS) intensity_grad_kernel(FieldIO f, long long n,
+                                                                     const float* __restrict__ w,
+                                                                     const double* __restrict__ g, FieldIO out) {
+    const int b = blockIdx.y;
+    __shared__ ff s_scale;
+    if (threadIdx.x == 0) {
+        const ff gb = double_to_ff(g[b]);
+        s_scale = {2.0f * gb.hi, 2.0f * gb.lo};  // exact doubling
+    }
+    __syncthreads();
+    const ff scale = s_scale;
+    for (long long p = (long long)blockIdx.x * INT_THREADS + threadIdx.x; p < n;
+         p += (long long)gridDim.x * INT_THREADS) {
+        const long long i = (long long)b * n + p;
+        const cff v = load_fmt<FMT>(f, i);
+        const ff c = w ? ff_mulf(scale, __ldg(&w[p])) : scale;
+        store_fmt<FMT>(out, i, cff{ff_mul(v.re, c), ff_mul(v.im, c)});
+    }
+}
+
+}  // namespace
+
+size_t intensity_sums_workspace_bytes(long long n, int batch) {
+    if (n <= 0 || batch <= 0) return 0;
+    return sizeof(float2) * (size_t)batch * ceil_div(n, INT_CHUNK);
+}
+
+int intensity_sums(const void* field, int dtype, long long n, int batch, const float* w, double* sums, void* ws,
+                   cudaStream_t st) {
+    const unsigned nchunks = ceil_div(n, INT_CHUNK);
+    if (batch > 65535) {
+        set_error("hx_intensity_sums: at most 65535 fields per call");
+        return HX_ERR_UNSUPPORTED;
+    }
+    float2* partial = (float2*)ws;
+    const dim3 grid(nchunks, (unsigned)batch);
+    if (dtype == HX_C128)
+        intensity_partial_kernel<FMT_C128><<<grid, INT_THREADS, 0, st>>>(input_field(field, dtype), n, w, partial);
+    else
+        intensity_partial_kernel<FMT_C64><<<grid, INT_THREADS, 0, st>>>(input_field(field, dtype), n, w, partial);
+    HX_TRY(launch_status("intensity_partial_kernel"));
+    intensity_final_kernel<<<ceil_div(batch, 8), 256, 0, st>>>(partial, (int)nchunks, batch, sums);
+    return launch_status("intensity_final_kernel");
+}
+
+int intensity_sums_grad(const void* field, int dtype, long long n, int batch, const float* w, const double* g,
+                        void* out, cudaStream_t st) {
+    if (batch > 65535) {
+        set_error("hx_intensity_sums_grad: at most 65535 fields per call");
+        return HX_ERR_UNSUPPORTED;
+    }
+    const unsigned bx = std::min<unsigned>(ceil_div(n, INT_THREADS), 4096u);
+    const dim3 grid(bx, (unsigned)batch);
+    if (dtype == HX_C128)
+        intensity_grad_kernel<FMT_C128><<<grid, INT_THREADS, 0, st>>>(input_field(field, dtype), n, w, g,
+                                                                     output_field(out, dtype));
+    else
+        intensity_grad_kernel<FMT_C64><<<grid, INT_THREADS, 0, st>>>(input_field(field, dtype), n, w, g,
+                                                                    output_field(out, dtype));
+    return launch_status("intensity_grad_kernel");
+}
+
 }  // namespace hx

@@ -35,5 +35,12 @@ int split_autotune_entries();
 // Entry i: shape {m_tiles, N, grid_z, ktiles}, n candidates with their tile width, K split and time (<= 8).
 int split_autotune_entry(int i, long long* shape, int* n, int* bn, int* ksplit, float* ms);
 void split_autotune_clear();
+// Weighted intensity sums sum_p w[p] |E_b[p]|^2 per field (w may be NULL) in compensated float-float
+// arithmetic, and their gradient 2 g_b w E_b; fields are complex64 or complex128.
+size_t intensity_sums_workspace_bytes(long long n, int batch);
+int intensity_sums(const void* field, int dtype, long long n, int batch, const float* w, double* sums, void* ws,
+                   cudaStream_t stream);
+int intensity_sums_grad(const void* field, int dtype, long long n, int batch, const float* w, const double* g,
+                        void* out, cudaStream_t stream);
 
 }  // namespace hx

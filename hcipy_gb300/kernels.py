@@ -114,3 +114,57 @@ class SparseBasis(object):
                                                      _lib.stream_handle())
         _lib.check(rc, 'hx_influence_apply_transpose')
         return out
+
+
+def _weights(w, n, device):
+    if w is None:
+        return None
+    w = w.data if hasattr(w, 'grid') and hasattr(w, 'data') else w
+    w = torch.as_tensor(np.asarray(w) if not isinstance(w, torch.Tensor) else w)
+    w = w.to(device=device, dtype=torch.float32).reshape(-1).contiguous()
+    if w.numel() != n:
+        raise ValueError('weights have %d points, the field %d' % (w.numel(), n))
+    return w
+
+
+def intensity_sums(e, w=None):
+    """sum_p w[p] |e[..., p]|^2 per field in compensated float-float arithmetic, as a float64 tensor of e's batch
+    shape (w: a real weight or region mask per point, or None)."""
+    if e.dtype not in _REAL:
+        raise TypeError('intensity sums take complex64 or complex128 fields, not %s' % e.dtype)
+    n = e.shape[-1]
+    lead = tuple(e.shape[:-1])
+    batch = int(np.prod(lead)) if lead else 1
+    out = torch.zeros(lead, dtype=torch.float64, device=e.device)
+    if batch == 0 or n == 0:
+        return out
+    e2 = _batched(e, n)
+    wt = _weights(w, n, e.device)
+    lib = _lib.lib()
+    nbytes = int(lib.hx_intensity_sums_workspace_bytes(n, batch))
+    ws = _lib.workspace(nbytes, e.device)
+    rc = lib.hx_intensity_sums(_lib.dptr(e2), _lib.dtype_code(e.dtype), n, batch,
+                               None if wt is None else _lib.dptr(wt), _lib.dptr(out), _lib.dptr(ws), nbytes,
+                               _lib.stream_handle())
+    _lib.check(rc, 'hx_intensity_sums')
+    return out
+
+
+def intensity_sums_grad(e, w, g):
+    """Gradient of ``intensity_sums`` in torch's convention: 2 g[b] w e_b, in e's dtype and shape."""
+    n = e.shape[-1]
+    lead = tuple(e.shape[:-1])
+    batch = int(np.prod(lead)) if lead else 1
+    out = torch.empty(lead + (n,), dtype=e.dtype, device=e.device)
+    if batch == 0 or n == 0:
+        return out
+    e2 = _batched(e, n)
+    wt = _weights(w, n, e.device)
+    g2 = g.to(device=e.device, dtype=torch.float64).reshape(-1).contiguous()
+    if g2.numel() != batch:
+        raise ValueError('expected %d upstream gradients, got %d' % (batch, g2.numel()))
+    rc = _lib.lib().hx_intensity_sums_grad(_lib.dptr(e2), _lib.dtype_code(e.dtype), n, batch,
+                                           None if wt is None else _lib.dptr(wt), _lib.dptr(g2), _lib.dptr(out),
+                                           _lib.stream_handle())
+    _lib.check(rc, 'hx_intensity_sums_grad')
+    return out

@@ -165,6 +165,18 @@ HX_API int hx_lyot_execute(const hx_mft_plan* fpm_plan, const hx_mft_plan* img_p
                     void* lyot_out, int lyot_dtype, void* image_out, int image_dtype,
                     void* workspace, size_t workspace_bytes, void* stream);
 
+/* Dark-hole contrast sums (no single counterpart in the reference, which forms intensities with numexpr,
+ * wavefront.py:113-143, and sums them in numpy): sums[b] = sum_p w[p] |E_b[p]|^2 for batch fields of n
+ * points (complex64 or complex128), w a float32 weight or region mask per point (NULL: all ones), in
+ * compensated float-float arithmetic with a fixed reduction order (deterministic); the workspace holds the
+ * per-chunk partials. */
+HX_API size_t hx_intensity_sums_workspace_bytes(long long n, int batch);
+HX_API int hx_intensity_sums(const void* field, int dtype, long long n, int batch, const float* weights,
+                             double* sums, void* workspace, size_t workspace_bytes, void* stream);
+/* Its gradient in torch's convention for a real loss of complex fields: out_b = 2 grad[b] w E_b (field dtype). */
+HX_API int hx_intensity_sums_grad(const void* field, int dtype, long long n, int batch, const float* weights,
+                                  const double* grad, void* out, void* stream);
+
 /* Status of the plan's bounded device-side waits since the last reset: HX_OK, or
  * HX_ERR_TIMEOUT when a wait of the tensor-core GEMM gave up (its CTA then
  * returned without writing).  Synchronizes with the device; reset != 0 clears it. */
