@@ -112,3 +112,22 @@ def test_formats_and_errors(tmp_path):
         hio.write_grid(CartesianGrid(SeparatedCoords([np.arange(3.0), np.arange(2.0)])), str(tmp_path / 'g.fits'))
     hio.write_grid(g, str(tmp_path / 'g.dat'), fmt='npz')
     assert hio.read_grid(str(tmp_path / 'g.dat'), fmt='npz').coords.key() == g.coords.key()
+
+
+def test_fits_long_headers_and_scaled_data(tmp_path):
+    """Headers longer than one 2880-byte block, long free-format float values, and BSCALE/BZERO scaling of
+    integer data (FITS 4.0, section 5.2.5) on reading."""
+    data = np.arange(12, dtype=np.int16).reshape(3, 4)
+    cards = [hio._card('KEY%d' % i, float(-1.2345678901234567e-05 * (i + 1))) for i in range(60)]
+    cards += [hio._card('NOTE', "it's a test"), hio._card('BSCALE', 0.5), hio._card('BZERO', 10.0)]
+    raw = hio._image_hdu(data, True, cards)
+    f = str(tmp_path / 'scaled.fits')
+    with open(f, 'wb') as fh:
+        fh.write(raw)
+    hdus = hio._read_hdus(open(f, 'rb').read())
+    header, got = hdus[0]
+    assert len(hdus) == 1
+    assert header['NOTE'] == "it's a test"
+    np.testing.assert_allclose(header['KEY59'], -1.2345678901234567e-05 * 60, rtol=1e-15)
+    np.testing.assert_array_equal(got, data * 0.5 + 10.0)
+    assert (len(raw) - 2880) % 2880 == 0 and len(raw) > 2 * 2880  # the header took two blocks
