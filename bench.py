@@ -902,12 +902,16 @@ def run_ours(args, rank, world, dist):
     # -- end to end through the public API with host buffers ------------------------------------------
     # Every step uploads its pupil field from pinned host memory and reads its image back.  The copies run on
     # their own streams, double-buffered, so step i+1's upload and step i-1's download overlap step i's
-    # transforms (as a streaming user would run them); the timed region spans all three streams.
+    # transforms (as a streaming user would run them); the timed region spans all three streams.  Unless
+    # --no-graph, the chain runs as two hcipy_gb300.CapturedCall graphs of the public API, one per input
+    # buffer, alternating: each upload lands in its graph's input, and a graph replays only after the download
+    # of its previous image.
     e_host = torch.from_numpy(w['E'].astype(np.complex64)).pin_memory()
     img_host = [torch.empty(focal.size, dtype=img.dtype).pin_memory() for _ in range(2)]  # complex128 (split)
     e2e_steps = max(10, min(args.steps, 100))
     h2d, d2h = torch.cuda.Stream(), torch.cuda.Stream()
-    d_in = [torch.empty_like(e_dev) for _ in range(2)]
+    e2e_graphs = None if args.no_graph else [hg.CapturedCall(step, e_dev) for _ in range(2)]
+    d_in = [g.static_in[0] for g in e2e_graphs] if e2e_graphs else [torch.empty_like(e_dev) for _ in range(2)]
     in_ready = [torch.cuda.Event() for _ in range(2)]
     in_free = [torch.cuda.Event() for _ in range(2)]
     out_done = [torch.cuda.Event() for _ in range(2)]
@@ -922,12 +926,18 @@ def run_ours(args, rank, world, dist):
                 d_in[b].copy_(e_host, non_blocking=True)
                 in_ready[b].record(h2d)
             stream.wait_event(in_ready[b])
-            res = step(d_in[b])
+            if e2e_graphs:
+                if used[b]:
+                    stream.wait_event(out_done[b])  # the graph's output buffer is free again
+                res = e2e_graphs[b](d_in[b])
+            else:
+                res = step(d_in[b])
             in_free[b].record(stream)
             used[b] = True
             d2h.wait_stream(stream)
             with torch.cuda.stream(d2h):
-                res.record_stream(d2h)
+                if not e2e_graphs:
+                    res.record_stream(d2h)
                 img_host[b].copy_(res, non_blocking=True)
                 out_done[b].record(d2h)
         stream.wait_stream(d2h)
@@ -1012,7 +1022,10 @@ def run_ours(args, rank, world, dist):
                      'algorithmic': '%d complex MACs x 8 FLOP per propagation' % cmacs, 'peak_note': peak_note,
                      'tensor_flop_per_algorithmic_flop': 8 if args.precision == 'split' else None},
         'e2e': {'value': e2e_value, 'unit': UNIT, 'h2d_bytes_per_step': int(e_host.numel() * 8),
-                'd2h_bytes_per_step': int(img_host.numel() * img_host.element_size())},
+                'd2h_bytes_per_step': int(img_host.numel() * img_host.element_size()),
+                'launch': ('two alternating hcipy_gb300.CapturedCall graphs of the chain' if e2e_graphs
+                           else 'Python launches of the chain'),
+                'e2e_image_equals_device_image': bool(np.array_equal(img_host.numpy(), img.cpu().numpy()))},
         'gpu_launches': int(gpu_launches),
         'clocks': clocks,
         'accuracy': {'ni_err_max': ni_max, 'ni_err_mean': ni_mean, 'dark_hole_mean_ni': ni_level,
