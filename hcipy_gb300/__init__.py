@@ -18,7 +18,8 @@ from .coronagraphy import LyotCoronagraph, MultiScaleCoronagraph, VortexCoronagr
 from .deformable_mirror import (ModeBasis, DeformableMirror, make_actuator_positions,
                                 make_gaussian_influence_functions, find_illuminated_actuators)
 from .atmosphere import (AtmosphericLayer, InfiniteAtmosphericLayer, MultiLayerAtmosphere,
-                         Cn_squared_from_fried_parameter, fried_parameter_from_Cn_squared, subpixel_shift)
+                         Cn_squared_from_fried_parameter, fried_parameter_from_Cn_squared, subpixel_shift,
+                         power_spectral_density_von_karman, SpectralNoiseFactoryMultiscale)
 from .broadband import BroadbandImager, diffraction_scaled_focal_grids
 from .efc import SVD, inverse_tikhonov, inverse_truncated, inverse_truncated_modal, poke_jacobian, efc_step, run_efc
 from .metrics import intensity_sum, mean_intensity_in_roi
@@ -41,6 +42,7 @@ __all__ = [
     'ModeBasis', 'DeformableMirror', 'make_actuator_positions', 'make_gaussian_influence_functions',
     'find_illuminated_actuators', 'AtmosphericLayer', 'InfiniteAtmosphericLayer', 'MultiLayerAtmosphere',
     'Cn_squared_from_fried_parameter', 'fried_parameter_from_Cn_squared', 'subpixel_shift',
+    'power_spectral_density_von_karman', 'SpectralNoiseFactoryMultiscale',
     'BroadbandImager', 'diffraction_scaled_focal_grids', 'autotune',
     'SVD', 'inverse_tikhonov', 'inverse_truncated', 'inverse_truncated_modal', 'poke_jacobian', 'efc_step',
     'run_efc', 'read_fits', 'write_fits', 'read_grid', 'write_grid', 'read_field', 'write_field',

@@ -15,9 +15,11 @@ SVD) runs on the host in float64 as in the reference; every frame runs on the GP
   (``hx_atmosphere_shift``);
 * ``forward``/``backward`` multiply by exp(+-i screen / lambda) in one kernel (``hx_phase_apply``).
 
-The initial screen is this package's own: a von Karman FFT screen of twice the extent, cropped (the reference
-draws it with its multi-scale spectral-noise generator, hcipy/util/spectral_noise.py:203-320, so a seeded layer
-here starts from a different but statistically equivalent screen).  ``initial_screen`` sets it explicitly.
+The initial screen is the reference's: multi-scale spectral noise at oversampling 16
+(``SpectralNoiseFactoryMultiscale``, hcipy/util/spectral_noise.py:203-320), its random draws taken from the layer's
+generator in the reference's order after the stencil draws, and evaluated with this package's own padded FFT and
+matrix Fourier transform on the device in float64 (construction time only), so a layer seeded like the reference's
+starts from the reference's screen and extrudes the reference's rows.  ``initial_screen`` sets it explicitly.
 """
 import copy
 import math
@@ -69,6 +71,95 @@ def quintic_weights(shift):
     if shift >= 0:
         return np.array([0.0, b[0], b[1], b[2], b[3], b[4], b[5]])
     return np.array([b[5], b[4], b[3], b[2], b[1], b[0], 0.0])
+
+
+def power_spectral_density_von_karman(r0, L0):  # noqa: N803
+    """The von Karman phase PSD as a function of a grid of angular frequencies (atmospheric_model.py:376-399):
+    0.0229 ((u^2 + u0^2) / (2 pi)^2)^(-11/6) r0^(-5/3), u0 = 2 pi / L0, zero at the origin.  Returns float64
+    values on the host, one per grid point."""
+    def func(grid):
+        x, y = (np.asarray(c, np.float64) for c in grid.points_list())
+        u = np.hypot(x, y) + 1e-10
+        u0 = 2 * np.pi / L0
+        res = 0.0229 * ((u**2 + u0**2) / (2 * np.pi)**2)**(-11 / 6.) * r0**(-5 / 3)
+        res[u < 1e-9] = 0
+        return res
+    return func
+
+
+class SpectralNoiseFactoryMultiscale(object):
+    """Spectral noise from two Fourier transforms (hcipy/util/spectral_noise.py:203-264): the PSD's high
+    frequencies on the FFT grid of ``output_grid`` (padded FFT), the low ones on that grid scaled down by
+    ``oversampling`` (matrix Fourier transform), split at the largest frequency of the fine grid.  The amplitudes
+    are host float64 arrays; a realization lives on the device in complex128."""
+
+    def __init__(self, psd, output_grid, oversampling):
+        from .fft import FastFourierTransform
+        from .fourier import MatrixFourierTransform
+        self.psd = psd
+        self.output_grid = output_grid
+        self.oversampling = oversampling
+        self.fourier_1 = FastFourierTransform(output_grid)
+        self.input_grid_1 = self.fourier_1.output_grid
+        self.input_grid_2 = self.input_grid_1.scaled(1.0 / oversampling)
+        self.fourier_2 = MatrixFourierTransform(output_grid, self.input_grid_2)
+        boundary = np.abs(np.asarray(self.input_grid_2.points_list()[0], np.float64)).max()
+        r1 = np.hypot(*(np.asarray(c, np.float64) for c in self.input_grid_1.points_list()))
+        r2 = np.hypot(*(np.asarray(c, np.float64) for c in self.input_grid_2.points_list()))
+        nd = self.input_grid_1.ndim
+        w1 = float(np.asarray(self.input_grid_1.weights).ravel()[0])
+        w2 = float(np.asarray(self.input_grid_2.weights).ravel()[0])
+        # (2 pi)^ndim converts the PSD per Hertz to per radian
+        self.C_1 = np.sqrt(psd(self.input_grid_1) / w1 * (2 * np.pi)**nd)
+        self.C_1[r1 < boundary] = 0
+        self.C_2 = np.sqrt(psd(self.input_grid_2) / w2 * (2 * np.pi)**nd)
+        self.C_2[r2 >= boundary] = 0
+
+    def make_random(self, seed=None):
+        """One realization (spectral_noise.py:266-289): complex normal draws from ``numpy.random.default_rng(seed)``
+        in the reference's order, real then imaginary part of the fine grid, then of the coarse grid."""
+        rng = np.random.default_rng(seed)
+        n1, n2 = self.input_grid_1.size, self.input_grid_2.size
+        c1 = self.C_1 * (rng.standard_normal(n1) + 1j * rng.standard_normal(n1))
+        c2 = self.C_2 * (rng.standard_normal(n2) + 1j * rng.standard_normal(n2))
+        return SpectralNoiseMultiscale(self, c1, c2)
+
+
+class SpectralNoiseMultiscale(object):
+    """A realization of multi-scale spectral noise (spectral_noise.py:266-320) with its two spectra on the
+    device."""
+
+    def __init__(self, factory, C_1, C_2):  # noqa: N803
+        self.factory = factory
+        dev = torch.device('cuda')
+        self.C_1 = torch.as_tensor(np.asarray(C_1, np.complex128), device=dev)
+        self.C_2 = torch.as_tensor(np.asarray(C_2, np.complex128), device=dev)
+
+    def copy(self):
+        out = SpectralNoiseMultiscale.__new__(SpectralNoiseMultiscale)
+        out.factory, out.C_1, out.C_2 = self.factory, self.C_1.clone(), self.C_2.clone()
+        return out
+
+    def shift(self, shift):
+        """In-place shift by ``shift`` (grid units) as a phase ramp on both spectra (spectral_noise.py:291-307).
+        The reference forms the ramp as an outer sum over (x, y) flattened x-major and multiplies it onto the
+        y-major spectrum as it lies in memory; the same layout is kept so that shifted screens match."""
+        for name, grid in (('C_1', self.factory.input_grid_1), ('C_2', self.factory.input_grid_2)):
+            xs, ys = (np.asarray(c, np.float64) for c in grid.separated_coords)
+            ramp = np.exp(-1j * (shift[0] * xs[:, None] + shift[1] * ys[None, :]).ravel())
+            setattr(self, name, getattr(self, name) * torch.as_tensor(ramp, device=self.C_1.device))
+
+    def shifted(self, shift):
+        out = self.copy()
+        out.shift(shift)
+        return out
+
+    def __call__(self):
+        """The noise on the factory's output grid (spectral_noise.py:309-320), float64 on the device."""
+        f = self.factory
+        ps = f.fourier_1.backward(Field(self.C_1, f.input_grid_1)).data.real
+        ps = ps + f.fourier_2.backward(Field(self.C_2, f.input_grid_2)).data.real
+        return Field(ps.contiguous(), f.output_grid)
 
 
 def von_karman_screen(nx, ny, delta, Cn_squared, L0, rng, pad=2):  # noqa: N803
@@ -288,10 +379,10 @@ class InfiniteAtmosphericLayer(AtmosphericLayer):
         else:
             self.rng = copy.deepcopy(self._original_rng)
         if self._initial_screen is not None:
-            screen = self._initial_screen.reshape(self.ny, self.nx)
+            ring = torch.from_numpy(np.ascontiguousarray(self._initial_screen.reshape(self.ny, self.nx)))
         else:
-            screen = von_karman_screen(self.nx, self.ny, self._delta, self._Cn_squared, self._L0, self.rng)
-        ring = torch.from_numpy(np.ascontiguousarray(screen)).to(device='cuda', dtype=self.dtype)
+            ring = self._reference_initial_screen()
+        ring = ring.to(device='cuda', dtype=self.dtype).reshape(self.ny, self.nx)
         if getattr(self, '_ring', None) is not None and self._ring.shape == ring.shape:
             # in place: a captured CUDA graph that reads these buffers stays valid across resets
             self._ring.copy_(ring)
@@ -304,6 +395,14 @@ class InfiniteAtmosphericLayer(AtmosphericLayer):
         self._version += 1
         self.center = np.zeros(2)
         self._t = 0
+
+    def _reference_initial_screen(self):
+        """The reference's initial screen (infinite_atmospheric_layer.py:204-214): the phase at a wavelength of 1 m
+        of a finite layer with oversampling 16, i.e. multi-scale spectral noise with the von Karman PSD of this
+        layer's turbulence, drawn from the layer's generator (which then continues with the extrusion noise)."""
+        psd = power_spectral_density_von_karman(fried_parameter_from_Cn_squared(self._Cn_squared, 1), self._L0)
+        factory = SpectralNoiseFactoryMultiscale(psd, self.input_grid, 16)
+        return factory.make_random(self.rng)().data
 
     @property
     def Cn_squared(self):  # noqa: N802

@@ -16,7 +16,11 @@
 // host it is only a stand-in symbol -- so on its first call on each device this
 // entry point asks the runtime for the array's device address
 // (cudaGetSymbolAddress, with that device current) and caches it.  That first
-// call per device should therefore come before any stream capture.
+// call per device should therefore come before any stream capture.  The cache
+// is keyed on the device and its current CUDA context: after cudaDeviceReset
+// (or any teardown that gives the device a new primary context) the module is
+// loaded again at a new address, and the next call looks the address up again
+// instead of using a stale one.
 //
 // Every call uses the same array and it keeps the previous call's contents.
 // The MFT overwrites every scratch element it reads (the whole intermediate is
@@ -24,6 +28,8 @@
 // start at zero.  Two calls whose kernels overlap on the GPU (different
 // streams, or different host threads without ordering) race on the array.
 #include "hx_common.cuh"
+
+#include <cuda.h>
 
 #include <mutex>
 
@@ -33,7 +39,24 @@ __device__ __align__(256) unsigned char g_mft_scratch[HX_MFT_NOALLOC_SCRATCH_BYT
 
 constexpr int kMaxDevices = 64;
 void* g_scratch_ptr[kMaxDevices] = {};
+CUcontext g_scratch_ctx[kMaxDevices] = {};
 std::mutex g_scratch_mutex;
+
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+
+// cuCtxGetCurrent from the driver, looked up once through the runtime (the library does not link libcuda).
+CtxGetCurrent ctx_get_current() {
+    static CtxGetCurrent fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<CtxGetCurrent>(p);
+    });
+    return fn;
+}
 
 int scratch_for_current_device(void** out) {
     int dev = 0;
@@ -42,12 +65,25 @@ int scratch_for_current_device(void** out) {
         hx::set_error("hx_mft_execute_noalloc: device %d out of range", dev);
         return HX_ERR_UNSUPPORTED;
     }
+    CtxGetCurrent get = ctx_get_current();
+    CUcontext ctx = nullptr;
+    if (!get || get(&ctx) != CUDA_SUCCESS) {
+        hx::set_error("hx_mft_execute_noalloc: cuCtxGetCurrent is not available from the driver");
+        return HX_ERR_CUDA;
+    }
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (g_scratch_ptr[dev] == nullptr) {
+    if (g_scratch_ptr[dev] == nullptr || ctx == nullptr || g_scratch_ctx[dev] != ctx) {
+        // The lookup makes the device's primary context current if none was, so the context is read again after
+        // it: that is the context this call's kernels run in.
         void* p = nullptr;
         HX_TRY(hx::cuda_status(cudaGetSymbolAddress(&p, g_mft_scratch),
                                "hx_mft_execute_noalloc: cudaGetSymbolAddress(scratch)"));
+        if (get(&ctx) != CUDA_SUCCESS) {
+            hx::set_error("hx_mft_execute_noalloc: cuCtxGetCurrent failed");
+            return HX_ERR_CUDA;
+        }
         g_scratch_ptr[dev] = p;
+        g_scratch_ctx[dev] = ctx;
     }
     *out = g_scratch_ptr[dev];
     return HX_OK;

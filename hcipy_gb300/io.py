@@ -11,7 +11,9 @@ Formats, picked from the file name as the reference does (``_guess_file_format``
   data raise ``TypeError`` (the reference's astropy path rejects them too); use ``npz``.
 * ``npz``: numpy archive with the values and the grid's description (regular, separated or unstructured
   coordinates and weights); complex data welcome.
-* ``pickle``: Python pickles of this package's objects, with the device tensors moved to host memory.
+* ``pickle``: Python pickles of this package's objects, with the device tensors moved to host memory.  Pickles
+  that the reference wrote (its fields, old- and new-style, and its Cartesian grids with regular, separated or
+  unstructured coordinates) read back too, into this package's objects, without the reference installed.
 * ``asdf``: not built (the asdf package is not part of this build): ``NotImplementedError``.
 
 Data read back land on the device as the other operators expect.
@@ -289,6 +291,106 @@ def _grid_from_arrays(d, prefix='grid_'):
     return CartesianGrid(coords, w)
 
 
+# ---- pickles written by the reference ---------------------------------------------------------------------
+#
+# The reference pickles its Field either as an ndarray subclass (hcipy/field/field.py:113-135, 175-211: the
+# ndarray state plus the grid) or as a wrapper whose state is {'data', 'grid'} (:512-541), its CartesianGrid with
+# the default instance dict {'coords', '_weights'} (hcipy/field/grid.py:31), and its coordinates with small state
+# dicts (hcipy/field/coordinates.py:264-277, 420-433, 623-641).  The unpickler below maps those classes onto
+# stand-ins that keep the state, and the stand-ins are converted to this package's grids and fields.
+
+class _RefState(object):
+    """Keeps the pickled state of one reference object."""
+
+    def __init__(self, *args):
+        self.state = None
+
+    def __setstate__(self, state):
+        self.state = state
+
+
+class _RefOldField(_RefState):
+    pass
+
+
+class _RefNewField(_RefState):
+    pass
+
+
+class _RefGrid(_RefState):
+    pass
+
+
+class _RefRegular(_RefState):
+    pass
+
+
+class _RefSeparated(_RefState):
+    pass
+
+
+class _RefUnstructured(_RefState):
+    pass
+
+
+def _ref_field_reconstruct(subtype, baseclass, baseshape, basetype):
+    return subtype()
+
+
+_REF_CLASSES = {
+    ('hcipy.field.field', '_field_reconstruct'): _ref_field_reconstruct,
+    ('hcipy.field.field', 'OldStyleField'): _RefOldField,
+    ('hcipy.field.field', 'NewStyleField'): _RefNewField,
+    ('hcipy.field.field', 'Field'): _RefNewField,
+    ('hcipy.field.cartesian_grid', 'CartesianGrid'): _RefGrid,
+    ('hcipy.field.coordinates', 'RegularCoords'): _RefRegular,
+    ('hcipy.field.coordinates', 'SeparatedCoords'): _RefSeparated,
+    ('hcipy.field.coordinates', 'UnstructuredCoords'): _RefUnstructured,
+}
+
+
+class _Unpickler(pickle.Unpickler):
+    def find_class(self, module, name):
+        if module.startswith('hcipy.') or module == 'hcipy':
+            cls = _REF_CLASSES.get((module, name))
+            if cls is None:
+                raise pickle.UnpicklingError('%s.%s: not a reference field or grid class this reader knows'
+                                             % (module, name))
+            return cls
+        return super().find_class(module, name)
+
+
+def _from_ref(obj):
+    """Reference stand-ins -> this package's objects (anything else passes through)."""
+    if isinstance(obj, _RefOldField):
+        _, shape, dtype, fortran, raw, grid = obj.state
+        arr = np.ndarray.__new__(np.ndarray, (0,), 'b')
+        arr.__setstate__((shape, dtype, fortran, raw))
+        return Field(np.ascontiguousarray(arr), _from_ref(grid))
+    if isinstance(obj, _RefNewField):
+        return Field(np.ascontiguousarray(np.asarray(obj.state['data'])), _from_ref(obj.state['grid']))
+    if isinstance(obj, _RefGrid):
+        w = obj.state.get('_weights')
+        if w is not None:
+            w = np.asarray(w)
+            w = float(w) if w.ndim == 0 else w
+        return CartesianGrid(_from_ref(obj.state['coords']), w)
+    if isinstance(obj, _RefRegular):
+        st = obj.state
+        return RegularCoords(np.asarray(st['delta'], np.float64), np.asarray(st['dims'], np.int64),
+                             np.asarray(st['zero'], np.float64))
+    if isinstance(obj, _RefSeparated):
+        return SeparatedCoords([np.asarray(c, np.float64) for c in obj.state['separated_coords']])
+    if isinstance(obj, _RefUnstructured):
+        return UnstructuredCoords([np.asarray(c, np.float64) for c in obj.state['coords']])
+    return obj
+
+
+def _load_pickle(filename):
+    with open(filename, 'rb') as f:
+        return _from_ref(_Unpickler(f).load())
+
+
 def _wcs_cards(grid):
     if grid is None or not grid.is_regular:
         return []
@@ -336,8 +438,7 @@ def read_grid(filename, fmt=None):
     """A grid from a file (io.py:134-174)."""
     fmt = _format(filename, fmt)
     if fmt == 'pickle':
-        with open(filename, 'rb') as f:
-            return pickle.load(f)
+        return _load_pickle(filename)
     if fmt == 'npz':
         with np.load(filename) as d:
             return _grid_from_arrays(dict(d))
@@ -382,8 +483,7 @@ def read_field(filename, fmt=None):
     """A Field from a file (io.py:217-266), on the device."""
     fmt = _format(filename, fmt)
     if fmt == 'pickle':
-        with open(filename, 'rb') as f:
-            return pickle.load(f)
+        return _load_pickle(filename)
     if fmt == 'npz':
         with np.load(filename) as d:
             d = dict(d)
@@ -437,8 +537,7 @@ def read_mode_basis(filename, fmt=None):
     from .deformable_mirror import ModeBasis
     fmt = _format(filename, fmt)
     if fmt == 'pickle':
-        with open(filename, 'rb') as f:
-            return pickle.load(f)
+        return _load_pickle(filename)
     if fmt == 'npz':
         with np.load(filename) as d:
             d = dict(d)

@@ -231,8 +231,12 @@ class PhaseApodizer(OpticalElement):
     def _apply(self, wavefront, sign):
         from .kernels import apply_phase
         e = wavefront.electric_field
-        return Wavefront(Field(apply_phase(e.data, as_tensor(self._phase, e.data.device), sign), e.grid),
-                         wavefront.wavelength)
+        if np.isscalar(self._phase) or np.ndim(self._phase) == 0:  # a uniform phase, as the reference allows
+            phase = torch.full((e.data.shape[-1],), float(np.asarray(self._phase)), dtype=torch.float64,
+                               device=e.data.device)
+        else:
+            phase = as_tensor(self._phase, e.data.device)
+        return Wavefront(Field(apply_phase(e.data, phase, sign), e.grid), wavefront.wavelength)
 
     def forward(self, wavefront):
         return self._apply(wavefront, 1.0)

@@ -209,7 +209,10 @@ HX_API int hx_autotune_clear(void);
  * a static device array of HX_MFT_NOALLOC_SCRATCH_BYTES compiled into the library
  * (one per GPU that loads it, held until exit) instead of a caller workspace.
  * The call allocates nothing.  Its first call on a device looks up the array's
- * device address, so make that first call before any stream capture.  A batch
+ * device address, so make that first call before any stream capture; the address
+ * is looked up again when the device's context changes (after cudaDeviceReset,
+ * the first call again does the lookup).  Split tensor-core plans run through it
+ * too while their scratch fits.  A batch
  * whose scratch need (hx_mft_workspace_bytes) exceeds the array is rejected with
  * HX_ERR_INVALID.  All calls share the array: calls that overlap on the GPU race. */
 #define HX_MFT_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)

@@ -100,3 +100,47 @@ def von_karman_covariance(r, r0, l0):
 def cn2_noise_std(cn2):
     """Standard deviation of the extrusion noise, infinite_atmospheric_layer.py:238."""
     return math.sqrt(cn2)
+
+
+def von_karman_psd(grid, r0, l0):
+    """hcipy/atmosphere/atmospheric_model.py:376-399 on a regular grid's points (angular frequency)."""
+    x, y = grid.coords()
+    u = np.hypot(x, y) + 1e-10
+    u0 = 2 * np.pi / l0
+    res = 0.0229 * ((u**2 + u0**2) / (2 * np.pi)**2)**(-11 / 6.) * r0**(-5 / 3)
+    res[u < 1e-9] = 0
+    return res
+
+
+def multiscale_spectral_noise(grid, r0, l0, oversampling, rng, shift=None):
+    """One realization of SpectralNoiseFactoryMultiscale (hcipy/util/spectral_noise.py:203-320) with the von
+    Karman PSD, evaluated on ``grid``: the high frequencies on the FFT grid of ``grid``, the low ones on that grid
+    scaled down by ``oversampling`` through a matrix Fourier transform; draws from ``rng`` in the reference's
+    order (real then imaginary part of the FFT part, then of the MFT part)."""
+    from .fourier import FFTPlan, mft_backward
+    fft = FFTPlan(grid)
+    g1 = fft.output_grid
+    g2 = g1.scaled(1.0 / oversampling)
+    x2, y2 = g2.coords()
+    boundary = np.abs(x2).max()
+    x1, y1 = g1.coords()
+    c1 = np.sqrt(von_karman_psd(g1, r0, l0) / g1.weights * (2 * np.pi)**2)
+    c1[np.hypot(x1, y1) < boundary] = 0
+    c2 = np.sqrt(von_karman_psd(g2, r0, l0) / g2.weights * (2 * np.pi)**2)
+    c2[np.hypot(x2, y2) >= boundary] = 0
+    n1, n2 = g1.size, g2.size
+    c1 = c1 * (rng.standard_normal(n1) + 1j * rng.standard_normal(n1))
+    c2 = c2 * (rng.standard_normal(n2) + 1j * rng.standard_normal(n2))
+    if shift is not None:
+        # SpectralNoiseMultiscale.shift (:291-307): the ramp is the outer sum of shift[0] x and shift[1] y laid out
+        # x-major (np.ix_ then ravel), multiplied onto the y-major noise as it lies in memory
+        c1 = c1 * np.exp(-1j * _ix_sum(shift, g1.separated_coords))
+        c2 = c2 * np.exp(-1j * _ix_sum(shift, g2.separated_coords))
+    gx, gy = grid.separated_coords
+    ux, uy = g2.separated_coords
+    return fft.backward(c1).real + mft_backward(c2, gx, gy, ux, uy, g2.weights).real
+
+
+def _ix_sum(shift, axes):
+    """sum(np.ix_(*[shift[i] * axes[i]])) flattened in C order (spectral_noise.py:300-305)."""
+    return (shift[0] * axes[0][:, None] + shift[1] * axes[1][None, :]).ravel()

@@ -7,7 +7,11 @@ for the plotting / FITS packages that the diffraction path never calls).
 
 Usage (from the repository root, with the reference checked out read-only)::
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py REFERENCE_SOURCE_TREE [case ...]
+
+REFERENCE_SOURCE_TREE is the directory that holds the reference's ``hcipy``
+package (required).  With case names (the ``make_<case>`` functions below,
+e.g. ``pickle_case``) only those cases are regenerated.
 
 Every case is small and seeded; the outputs are written as compressed ``.npz``
 files next to this script.  Nothing in the test suite runs this script: the
@@ -440,29 +444,75 @@ def make_efc_case(hp, out):
     }
 
 
+def make_pickle_case(hp, out):
+    """Fields and grids pickled by the reference's own writers (hcipy/util/io.py:204-215, 262-266, 296-320): a
+    complex field on a regular grid, a real tensor field on a separated grid and an unstructured grid with
+    weights, each as the bytes of the file the reference wrote, with the values and grids they hold."""
+    import pickle
+    import tempfile
+    rng = np.random.default_rng(21)
+    reg = hp.make_pupil_grid([12, 10], [1.2, 1.0])
+    f_reg = hp.Field(rng.standard_normal(reg.size) + 1j * rng.standard_normal(reg.size), reg)
+    sep = hp.CartesianGrid(hp.SeparatedCoords([np.sort(rng.uniform(-1, 1, 7)), np.sort(rng.uniform(-2, 2, 5))]))
+    f_sep = hp.Field(rng.standard_normal((3, sep.size)), sep)
+    pts = rng.standard_normal((2, 9))
+    uns = hp.CartesianGrid(hp.UnstructuredCoords(pts), rng.uniform(0.5, 1.5, 9))
+    rec = {'reg_values': np.asarray(f_reg), 'reg_delta': np.asarray(reg.delta, np.float64),
+           'reg_dims': np.asarray(reg.dims, np.int64), 'reg_zero': np.asarray(reg.zero, np.float64),
+           'sep_values': np.asarray(f_sep), 'sep_x': np.asarray(sep.separated_coords[0]),
+           'sep_y': np.asarray(sep.separated_coords[1]), 'uns_points': pts,
+           'uns_weights': np.asarray(uns.weights, np.float64)}
+    with tempfile.TemporaryDirectory() as d:
+        for name, obj, writer in [('reg', f_reg, hp.write_field), ('sep', f_sep, hp.write_field),
+                                  ('uns', uns, hp.write_grid)]:
+            path = os.path.join(d, name + '.pkl')
+            writer(obj, path, fmt='pickle')
+            with open(path, 'rb') as f:
+                rec[name + '_pickle'] = np.frombuffer(f.read(), np.uint8)
+            with open(path, 'rb') as f:
+                pickle.load(f)  # the reference reads its own file back
+    out['io_pickle'] = rec
+
+
+def make_spectral_noise_case(hp, out):
+    """Multi-scale spectral noise (hcipy/util/spectral_noise.py:203-320) with the von Karman PSD
+    (hcipy/atmosphere/atmospheric_model.py:376-399) on a rectangular grid: the screen of one seeded realization,
+    and the same realization shifted."""
+    grid = hp.make_pupil_grid([40, 32], [2.0, 1.6])
+    r0, L0 = 0.15, 12.0  # noqa: N806
+    psd = hp.power_spectral_density_von_karman(r0, L0)
+    factory = hp.SpectralNoiseFactoryMultiscale(psd, grid, 4)
+    noise = factory.make_random(9)
+    shift = np.array([0.13, -0.07])
+    out['spectral_noise'] = {
+        'screen': np.asarray(noise()), 'shifted': np.asarray(noise.shifted(shift)()), 'shift': shift,
+        'r0': np.float64(r0), 'L0': np.float64(L0), 'oversampling': np.int64(4), 'seed': np.int64(9),
+        **grid_record('grid', grid),
+    }
+
+
 def save(out):
     for name, rec in out.items():
         np.savez_compressed(os.path.join(HERE, name + '.npz'), **rec)
         print('wrote', name, sum(np.asarray(v).nbytes for v in rec.values()), 'bytes')
 
 
+CASES = ['mft_cases', 'fraunhofer_cfg1', 'fft_cases', 'czt_cases', 'asp_cases', 'fresnel_cases', 'vortex_cases',
+         'pyramid_case', 'lyot_case', 'subpixel_cases', 'atmosphere_case', 'dm_case', 'efc_case', 'pickle_case',
+         'spectral_noise_case']
+
+
 def main():
-    ref_path = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
-    hp = import_reference(ref_path)
+    if len(sys.argv) < 2:
+        sys.exit('usage: make_golden.py REFERENCE_SOURCE_TREE [case ...]  (cases: %s)' % ' '.join(CASES))
+    hp = import_reference(sys.argv[1])
+    chosen = sys.argv[2:] or CASES
+    unknown = [c for c in chosen if c not in CASES]
+    if unknown:
+        sys.exit('unknown case(s): %s' % ' '.join(unknown))
     out = {}
-    make_mft_cases(hp, out)
-    make_fraunhofer_cfg1(hp, out)
-    make_fft_cases(hp, out)
-    make_czt_cases(hp, out)
-    make_asp_cases(hp, out)
-    make_fresnel_cases(hp, out)
-    make_vortex_cases(hp, out)
-    make_pyramid_case(hp, out)
-    make_lyot_case(hp, out)
-    make_subpixel_cases(hp, out)
-    make_atmosphere_case(hp, out)
-    make_dm_case(hp, out)
-    make_efc_case(hp, out)
+    for case in chosen:
+        globals()['make_' + case](hp, out)
     save(out)
 
 

@@ -232,3 +232,41 @@ def test_multilayer_scintillation_matches_oracle_chain():
     atm.scintillation = False
     assert rel_err(atm.forward(hg.Wavefront(hg.Field(e, grid), wl)).electric_field.numpy(),
                    e * np.exp(1j * sum(screens) / wl)) < 1e-12
+
+
+def test_spectral_noise_matches_reference():
+    """Multi-scale spectral noise (hcipy/util/spectral_noise.py:203-320) on the device, float64: the reference's
+    seeded realization on a rectangular grid and its shifted evaluation, within 1e-10."""
+    g = load_golden('spectral_noise')
+    grid = _grid(g, 'grid')
+    psd = hg.power_spectral_density_von_karman(float(g['r0']), float(g['L0']))
+    factory = hg.SpectralNoiseFactoryMultiscale(psd, grid, int(g['oversampling']))
+    noise = factory.make_random(int(g['seed']))
+    screen = noise().numpy()
+    assert screen.dtype == np.float64
+    assert rel_err(screen, g['screen']) < 1e-10
+    assert rel_err(noise.shifted(g['shift'])().numpy(), g['shifted']) < 1e-10
+    assert rel_err(noise().numpy(), g['screen']) < 1e-10  # shifted() leaves the realization itself alone
+
+
+def test_seeded_layer_starts_from_the_reference_screen_and_stream():
+    """A layer seeded like the reference's starts from the reference's initial screen (1e-10), and its own
+    generator then yields the reference's extrusion noise, so with the reference's A/B matrices the layer
+    evolves into the reference's screens without any injected noise (1e-10)."""
+    import copy
+    g = load_golden('atmosphere')
+    grid = _grid(g, 'pupil')
+    layer = hg.InfiniteAtmosphericLayer(grid, float(g['cn2']), L0=25, velocity=tuple(g['velocity']),
+                                        use_interpolation=True, seed=5)
+    assert rel_err(layer.achromatic_screen.numpy(), g['screen0']) < 1e-10
+    draw = copy.deepcopy(layer.rng).normal(0, np.sqrt(float(g['cn2'])), size=g['noise_0'].shape[1])
+    assert np.array_equal(draw, g['noise_0'][0])
+    _use_reference_matrices(layer, g)
+    t = 0.0
+    for i in range(3):
+        t += float(g['dt_%d' % i])
+        layer.t = t
+        assert rel_err(layer.achromatic_screen.numpy(), g['screen_%d' % i]) < 1e-10, i
+        assert rel_err(layer.phase_for(1.0).numpy(), g['shifted_%d' % i]) < 1e-10, i
+    layer.reset()
+    assert rel_err(layer.achromatic_screen.numpy(), g['screen0']) < 1e-10

@@ -131,3 +131,25 @@ def test_fits_long_headers_and_scaled_data(tmp_path):
     np.testing.assert_allclose(header['KEY59'], -1.2345678901234567e-05 * 60, rtol=1e-15)
     np.testing.assert_array_equal(got, data * 0.5 + 10.0)
     assert (len(raw) - 2880) % 2880 == 0 and len(raw) > 2 * 2880  # the header took two blocks
+
+
+def test_reads_a_grid_the_reference_pickled(tmp_path):
+    """An unstructured grid with weights, pickled by the reference's write_grid (hcipy/util/io.py:204-215), reads
+    back into this package's grid without the reference installed."""
+    from conftest import load_golden
+    g = load_golden('io_pickle')
+    f = tmp_path / 'grid.pkl'
+    f.write_bytes(g['uns_pickle'].tobytes())
+    grid = hio.read_grid(str(f))
+    assert isinstance(grid, CartesianGrid) and grid.is_unstructured
+    np.testing.assert_array_equal(np.asarray(grid.points_list()), g['uns_points'])
+    np.testing.assert_array_equal(np.asarray(grid.weights), g['uns_weights'])
+
+
+def test_reference_pickles_name_only_known_classes(tmp_path):
+    """A pickle that names another class of the reference is refused instead of importing anything."""
+    import pickle
+    f = tmp_path / 'other.pkl'
+    f.write_bytes(b'chcipy.optics\nWavefront\n.')  # protocol 0: GLOBAL hcipy.optics.Wavefront, STOP
+    with pytest.raises(pickle.UnpicklingError, match='not a reference field or grid class'):
+        hio.read_grid(str(f))

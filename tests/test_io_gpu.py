@@ -75,3 +75,27 @@ def test_mode_basis_round_trips(tmp_path):
     dm_a.actuators = act
     dm_b.actuators = act
     assert torch.equal(dm_a.surface.data, dm_b.surface.data)
+
+
+def test_reads_fields_the_reference_pickled(tmp_path):
+    """Fields pickled by the reference's write_field (hcipy/util/io.py:262-266, 316-318): a complex field on a
+    regular grid and a real tensor field on a separated grid come back on the device, values bit for bit."""
+    from conftest import load_golden
+    g = load_golden('io_pickle')
+    f = tmp_path / 'reg.pkl'
+    f.write_bytes(g['reg_pickle'].tobytes())
+    field = hio.read_field(str(f))
+    assert isinstance(field, hg.Field) and field.data.is_cuda
+    np.testing.assert_array_equal(field.numpy(), g['reg_values'])
+    assert field.grid.is_regular
+    np.testing.assert_array_equal(np.asarray(field.grid.delta), g['reg_delta'])
+    np.testing.assert_array_equal(np.asarray(field.grid.dims), g['reg_dims'])
+    np.testing.assert_array_equal(np.asarray(field.grid.zero), g['reg_zero'])
+    f = tmp_path / 'sep.pkl'
+    f.write_bytes(g['sep_pickle'].tobytes())
+    field = hio.read_field(str(f))
+    assert field.shape == g['sep_values'].shape
+    np.testing.assert_array_equal(field.numpy(), g['sep_values'])
+    assert field.grid.is_separated and not field.grid.is_regular
+    np.testing.assert_array_equal(np.asarray(field.grid.separated_coords[0]), g['sep_x'])
+    np.testing.assert_array_equal(np.asarray(field.grid.separated_coords[1]), g['sep_y'])

@@ -200,3 +200,34 @@ def test_efc_oracle():
     for k in range(1, len(g['actuators'])):
         act = efc.efc_step(em, field(act, g['aberration']), dz, act, g['gain'])
         assert rel_err(act, g['actuators'][k]) < 1e-9
+
+
+def test_spectral_noise_oracle():
+    """Multi-scale spectral noise with the von Karman PSD (hcipy/util/spectral_noise.py:203-320): the seeded
+    realization and its shifted evaluation, as the reference drew them."""
+    g = load_golden('spectral_noise')
+    grid = grid_from(g, 'grid')
+    rng = np.random.default_rng(int(g['seed']))
+    s = atmosphere.multiscale_spectral_noise(grid, float(g['r0']), float(g['L0']), int(g['oversampling']), rng)
+    assert rel_err(s, g['screen']) < 1e-12
+    rng = np.random.default_rng(int(g['seed']))
+    s = atmosphere.multiscale_spectral_noise(grid, float(g['r0']), float(g['L0']), int(g['oversampling']), rng,
+                                             shift=g['shift'])
+    assert rel_err(s, g['shifted']) < 1e-12
+
+
+def test_infinite_layer_initial_screen_oracle():
+    """A seeded infinite layer's initial screen is multi-scale spectral noise at oversampling 16 drawn from the
+    layer's generator after its stencil draws (infinite_atmospheric_layer.py:111-140, 204-214), and the first
+    extrusion's noise continues that generator."""
+    g = load_golden('atmosphere')
+    grid = grid_from(g, 'pupil')
+    nx, ny = (int(d) for d in g['pupil_dims'])
+    rng = np.random.default_rng(5)
+    rng.geometric(0.5, nx)
+    rng.geometric(0.5, ny)
+    r0 = (0.423 * float(g['cn2']) * (2 * np.pi)**2)**(-3. / 5)  # Fried parameter at a wavelength of 1 m
+    screen = atmosphere.multiscale_spectral_noise(grid, r0, 25.0, 16, rng)
+    assert rel_err(screen, g['screen0']) < 1e-12
+    noise = rng.normal(0, np.sqrt(float(g['cn2'])), size=g['noise_0'].shape[1])
+    assert np.array_equal(noise, g['noise_0'][0])
