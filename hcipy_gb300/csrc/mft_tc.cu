@@ -24,9 +24,20 @@
 // of an MFT, and between the MFTs of a coronagraph, as float-float planes
 // (hi and lo of Re and Im); slicing reads them with FP32 operations only.
 //
+// Where the embedding lives.  When A is a plan constant (a phase matrix) the
+// embedding above is used (EMB = 0): A' holds 64-row blocks of Cr rows then Ci
+// rows and B' is the field, [Br; Bi] per column.  When A is the per-call field
+// (EMB = 1) the embedding moves to the constant B instead, so that the field is
+// sliced once as [Ar | Ai] (M x 2K) and never duplicated:
+//     B' = [[Br, Bi], [-Bi, Br]] (2K x 2N),  C = [Cr | Ci],
+// stored as B' rows (one per output column, K' = 2K long) in blocks of 8 complex
+// columns: the 8 Cr rows [Br | -Bi] then the 8 Ci rows [Bi | Br].  A tile is then
+// 128 complex rows x BN/2 complex columns, and TMEM lane = complex row.
+//
 // Kernel.  One CTA computes 64 complex rows x BN columns of C (BN = 64 or 128):
 // a 128-row tile of A' (the 64 Cr rows then their 64 Ci rows) times a BN-row
-// tile of B'.  warp 0 issues TMA loads (one 3-D box per operand per stage:
+// tile of B' (EMB = 0; with EMB = 1, 128 complex rows x BN/2 complex columns).
+// warp 0 issues TMA loads (one 3-D box per operand per stage:
 // three slice planes of 64 K-elements, 128-byte swizzle), warp 1 issues
 // tcgen05.mma (8 slice products x 4 K16 steps per stage) into four TMEM
 // accumulators of 128 lanes x BN columns, warps 2-9 read TMEM, combine and
@@ -68,7 +79,7 @@ constexpr uint64_t WAIT_LIMIT = 2000000000ull;  // 2 s per wait
 constexpr int MAX_SPLIT_K = 4096;               // exact level-0 sums need at most 4096 K' per CTA
 constexpr int MAX_SPLIT_KTILES = MAX_SPLIT_K / BK;
 constexpr int MAX_GRID_POINTS = 8192;           // points per axis of a split plan
-constexpr int EXTRA_BYTES = 1024 + 1664;        // alignment slack, barriers, flags, per-row tables
+constexpr int EXTRA_BYTES = 1024 + 3712;        // alignment slack, barriers, flags, per-row tables
 
 // Tile of BN output columns: four level accumulators of BN TMEM columns each, so BN = 128 takes all
 // 512 columns of the SM.  Stage count fills the shared memory.
@@ -286,6 +297,7 @@ struct __align__(64) GemmArgs {
     int epi;
     const float2* mask;
     FieldIO src;           // Babinet source, same indexing as the output
+    int emb;               // 1: the embedding is on B (A = [Ar | Ai]), see the file comment
     int rows_per_field;    // mask index = (m % rows_per_field) * N + n
     unsigned int* colmax;  // max(|Re|, |Im|) of the output as float bits, per (field, column)
     long long colmax_z;
@@ -310,11 +322,14 @@ __device__ __forceinline__ ff combine_levels(float v0, float v1, float v2, float
     return two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(v2 * 0x1p-34f, v3 * 0x1p-45f)));
 }
 
-// OUT: format of the result; SRC: format of the Babinet source (FMT_NONE for other epilogues).
-template <int BN, int OUT, int SRC>
+// OUT: format of the result; SRC: format of the Babinet source (FMT_NONE for other epilogues); EMB: where the
+// complex embedding lives (0: on A, 1: on B).
+template <int BN, int OUT, int SRC, int EMB>
 __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid_constant__ GemmArgs g) {
     using T = Tile<BN>;
     constexpr int STAGES = T::STAGES;
+    constexpr int TM = EMB ? 128 : 64;     // complex rows of a tile
+    constexpr int TN = EMB ? BN / 2 : BN;  // complex columns of a tile
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     const uint32_t raw_addr = ptx::smem_addr(smem_raw);
     uint8_t* smem = smem_raw + ((1024 - (raw_addr & 1023)) & 1023);
@@ -324,10 +339,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(extra + 64);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(extra + 68);
     volatile int* last_flag = reinterpret_cast<volatile int*>(extra + 72);
-    float* s_rscale = reinterpret_cast<float*>(extra + 128);               // per tile row (64): row scale
-    int* s_field = reinterpret_cast<int*>(extra + 384);                    // m / colmax_rows_per_field
-    long long* s_rowoff = reinterpret_cast<long long*>(extra + 640);       // output offset of the row
-    long long* s_maskoff = reinterpret_cast<long long*>(extra + 1152);     // mask offset of the row
+    float* s_rscale = reinterpret_cast<float*>(extra + 128);               // per tile row (TM): row scale
+    int* s_field = reinterpret_cast<int*>(extra + 640);                    // m / colmax_rows_per_field
+    long long* s_rowoff = reinterpret_cast<long long*>(extra + 1152);      // output offset of the row
+    long long* s_maskoff = reinterpret_cast<long long*>(extra + 2176);     // mask offset of the row
+    unsigned int* s_rowmax = reinterpret_cast<unsigned int*>(extra + 3200);  // EMB: row maxima of the tile
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -350,14 +366,15 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
         *last_flag = 0;
         ptx::fence_mbar_init();
     }
-    if (threadIdx.x >= 64 && threadIdx.x < 128) {
+    if (threadIdx.x >= 64 && threadIdx.x < 64 + TM) {
         const int r = threadIdx.x - 64;
-        const int m = m_tile * 64 + r;
+        const int m = m_tile * TM + r;
         const bool ok = m < g.M;
         s_rscale[r] = ok ? g.row_scale[z * g.row_scale_z + m] : 0.0f;
         s_field[r] = (ok && g.colmax_rows_per_field > 0) ? m / g.colmax_rows_per_field : 0;
         s_rowoff[r] = z * g.out_z + (long long)m * g.ldo;
         s_maskoff[r] = ok ? (long long)(m % g.rows_per_field) * g.N : 0;
+        if (EMB) s_rowmax[r] = 0u;
     }
     if (warp == 1) {
         ptx::tmem_alloc(ptx::smem_addr(tmem_slot), T::TMEM_COLS);
@@ -547,20 +564,25 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
             const bool imag_alpha = g.alpha[0] == 0.0f && g.alpha[1] == 0.0f;  // e.g. Fraunhofer's 1/(i f lambda)
             const bool unit_alpha = real_alpha && g.alpha[0] == 1.0f && g.alpha[1] == 0.0f;
             const float2* mask = (g.epi == HX_EPI_MUL || g.epi == HX_EPI_BABINET) ? g.mask : nullptr;
-            // Each thread keeps one column; a warp covers 32 consecutive columns of one row.
-            const int nl = et % BN;
-            const int n = n_tile * BN + nl;
+            // Each thread keeps one complex column; a warp covers consecutive columns of one row.
+            const int nl = et % TN;
+            const int n = n_tile * TN + nl;
             const bool nok = n < g.N;
             const float csc = nok ? g.col_scale[z * g.col_scale_z + n] : 0.0f;
-            constexpr int RSTEP = EPI / BN;       // rows per iteration
-            constexpr int ITER = 64 / RSTEP;
+            // staged position of the real and imaginary parts: EMB = 0, rows ml and 64 + ml of column nl;
+            // EMB = 1, row ml, columns of the 8-column Cr / Ci blocks
+            const int c_re = EMB ? (nl >> 3) * 16 + (nl & 7) : nl;
+            const int c_im = EMB ? c_re + 8 : nl;
+            constexpr int R_IM = EMB ? 0 : 64;
+            constexpr int RSTEP = EPI / TN;       // rows per iteration
+            constexpr int ITER = TM / RSTEP;
             constexpr int U = 4;                  // rows per batch: loads issued before any store
-            static_assert(64 % (RSTEP * U) == 0, "rows of a tile per batch");
-            // With BN not dividing the epilogue threads (BN = 112) the last EPI - RSTEP * BN threads have no
-            // column; they skip the loop so that no row beyond the tile's 64 is touched.
-            const bool has_col = et < RSTEP * BN;
-            const int r0 = et / BN;
-            const int mlim = g.M - m_tile * 64;   // valid rows of this tile
+            static_assert(TM % (RSTEP * U) == 0, "rows of a tile per batch");
+            // With TN not dividing the epilogue threads (BN = 112) the last EPI - RSTEP * TN threads have no
+            // column; they skip the loop so that no row beyond the tile's TM is touched.
+            const bool has_col = et < RSTEP * TN;
+            const int r0 = et / TN;
+            const int mlim = g.M - m_tile * TM;   // valid rows of this tile
             int cfield = -1;
             float cmax = 0.0f;
 #pragma unroll 1
@@ -584,8 +606,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
                     float mag = 0.0f;
                     if (nok && ml < mlim) {
                         const float sc = s_rscale[ml] * csc;  // product of powers of two: exact
-                        cff v = {ff{st_hi[ml * T::PITCH + nl] * sc, st_lo[ml * T::PITCH + nl] * sc},
-                                 ff{st_hi[(64 + ml) * T::PITCH + nl] * sc, st_lo[(64 + ml) * T::PITCH + nl] * sc}};
+                        cff v = {ff{st_hi[ml * T::PITCH + c_re] * sc, st_lo[ml * T::PITCH + c_re] * sc},
+                                 ff{st_hi[(R_IM + ml) * T::PITCH + c_im] * sc,
+                                    st_lo[(R_IM + ml) * T::PITCH + c_im] * sc}};
                         if (!unit_alpha)
                             v = real_alpha   ? cff{ff_mul(v.re, alpha.re), ff_mul(v.im, alpha.re)}
                                 : imag_alpha ? cff{ff_neg(ff_mul(v.im, alpha.im)), ff_mul(v.re, alpha.im)}
@@ -607,18 +630,28 @@ __global__ void __launch_bounds__(NUM_THREADS, 1) split_gemm_kernel(const __grid
                             cmax = fmaxf(cmax, mag);
                         }
                     }
-                    if (g.rowmax) s_mag[ml * T::PITCH + nl] = mag;
+                    if (g.rowmax) {
+                        if (EMB) {
+                            if (mag > 0.0f) atomicMax(&s_rowmax[ml], __float_as_uint(mag));
+                        } else {
+                            s_mag[ml * T::PITCH + nl] = mag;
+                        }
+                    }
                 }
             }
             if (g.colmax && cfield >= 0 && cmax > 0.0f)
                 atomicMax(&g.colmax[z * g.colmax_z + cfield * g.colmax_field_stride + n], __float_as_uint(cmax));
         }
         ptx::named_barrier(1, EPI);
-        if (run && g.rowmax && et < 64 && et < g.M - m_tile * 64) {
+        if (run && g.rowmax && et < TM && et < g.M - m_tile * TM) {
             float mx = 0.0f;
-            const int nmax = min(BN, g.N - n_tile * BN);
-            for (int c = 0; c < nmax; ++c) mx = fmaxf(mx, s_mag[et * T::PITCH + c]);
-            if (mx > 0.0f) atomicMax(&g.rowmax[z * g.rowmax_z + m_tile * 64 + et], __float_as_uint(mx));
+            if (EMB) {
+                mx = __uint_as_float(s_rowmax[et]);
+            } else {
+                const int nmax = min(BN, g.N - n_tile * BN);
+                for (int c = 0; c < nmax; ++c) mx = fmaxf(mx, s_mag[et * T::PITCH + c]);
+            }
+            if (mx > 0.0f) atomicMax(&g.rowmax[z * g.rowmax_z + m_tile * TM + et], __float_as_uint(mx));
         }
     }
     ptx::tc_fence_before();
@@ -653,7 +686,9 @@ __device__ __forceinline__ void slice3(ff x, float inv, __half& h0, __half& h1, 
     h2 = __float2half_rn(a2);
 }
 
-// One CTA per complex row m of X (M x K, row stride ld): writes the Cr and Ci rows of A'.
+// One CTA per complex row m of X (M x K, row stride ld): writes the Cr and Ci rows of A' (EMB = 0), or the one
+// row [Re | Im] of A (EMB = 1).
+template <int EMB>
 __global__ void slice_rows_kernel(FieldIO src, long long ld, int K, int Kp, const unsigned int* rowmax,
                                   __half* planes, long long plane_stride, int kpitch, float* scale_out) {
     const int m = blockIdx.x;
@@ -688,7 +723,7 @@ __global__ void slice_rows_kernel(FieldIO src, long long ld, int K, int Kp, cons
     }
     __syncthreads();
     const float inv = 1.0f / s_scale;
-    const long long r_cr = (long long)(m / 64) * 128 + (m % 64);
+    const long long r_cr = EMB ? (long long)m : (long long)(m / 64) * 128 + (m % 64);
     const long long r_ci = r_cr + 64;
     // Four consecutive K-elements per thread: 8-byte stores into each plane (Kp and kpitch are multiples of 32).
     for (int k0 = 4 * threadIdx.x; k0 < Kp; k0 += 4 * blockDim.x) {
@@ -713,6 +748,11 @@ __global__ void slice_rows_kernel(FieldIO src, long long ld, int K, int Kp, cons
             __half2 ni01 = __hneg2(im01), ni23 = __hneg2(im23);
             *reinterpret_cast<uint2*>(pl + r_cr * kpitch + k0) =
                 make_uint2(*reinterpret_cast<uint32_t*>(&re01), *reinterpret_cast<uint32_t*>(&re23));
+            if (EMB) {
+                *reinterpret_cast<uint2*>(pl + r_cr * kpitch + Kp + k0) =
+                    make_uint2(*reinterpret_cast<uint32_t*>(&im01), *reinterpret_cast<uint32_t*>(&im23));
+                continue;
+            }
             *reinterpret_cast<uint2*>(pl + r_cr * kpitch + Kp + k0) =
                 make_uint2(*reinterpret_cast<uint32_t*>(&ni01), *reinterpret_cast<uint32_t*>(&ni23));
             *reinterpret_cast<uint2*>(pl + r_ci * kpitch + k0) =
@@ -740,9 +780,12 @@ __global__ void colmax_kernel(FieldIO src, int K, int N, long long field_stride,
 }
 
 // Per-field K x N matrix Y -> B' rows (z*n_rows_per_field + n): [slices of Re Y[:, n] | slices of Im Y[:, n]].
+// emb (plan-time phase matrices that carry the embedding, see the file comment): two rows per column n, in
+// blocks of 8 columns, row (n/8)*16 + n%8 = [Re | -Im] and row (n/8)*16 + 8 + n%8 = [Im | Re].
 __global__ void slice_cols_kernel(FieldIO src, int K, int N, int Kp, long long field_stride,
                                   const unsigned int* colmax, long long colmax_stride, __half* planes,
-                                  long long plane_stride, int kpitch, int n_rows_per_field, float* scale_out) {
+                                  long long plane_stride, int kpitch, int n_rows_per_field, float* scale_out,
+                                  int emb) {
     __shared__ ff tr[32][33], ti[32][33];
     __shared__ float sc[32];
     const int n0 = blockIdx.x * 32, k0 = blockIdx.y * 32, z = blockIdx.z;
@@ -770,6 +813,18 @@ __global__ void slice_cols_kernel(FieldIO src, int K, int N, int Kp, long long f
         slice3(ti[tx][r], inv, i0, i1, i2);
         const __half rs[3] = {r0, r1, r2};
         const __half is[3] = {i0, i1, i2};
+        if (emb) {
+            const long long row = (long long)z * n_rows_per_field + (n >> 3) * 16 + (n & 7);
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+                __half* pl = planes + p * plane_stride;
+                pl[row * kpitch + k] = rs[p];
+                pl[row * kpitch + Kp + k] = __hneg(is[p]);
+                pl[(row + 8) * kpitch + k] = is[p];
+                pl[(row + 8) * kpitch + Kp + k] = rs[p];
+            }
+            continue;
+        }
         const long long row = (long long)z * n_rows_per_field + n;
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
@@ -959,10 +1014,14 @@ FieldIO carve_ff(Carver& c, long long n) {
 }
 
 int launch_slice_rows(const FieldIO& src, long long ld, long long M, int K, const unsigned int* rowmax,
-                      SliceMat& s, cudaStream_t st) {
+                      SliceMat& s, cudaStream_t st, bool emb = false) {
     if (M > 2147483647LL) return HX_ERR_UNSUPPORTED;
-    slice_rows_kernel<<<(unsigned)M, 256, 0, st>>>(src, ld, K, s.Kp, rowmax, s.planes, s.plane_stride(), s.kpitch,
-                                                   s.scale);
+    if (emb)
+        slice_rows_kernel<1><<<(unsigned)M, 256, 0, st>>>(src, ld, K, s.Kp, rowmax, s.planes, s.plane_stride(),
+                                                          s.kpitch, s.scale);
+    else
+        slice_rows_kernel<0><<<(unsigned)M, 256, 0, st>>>(src, ld, K, s.Kp, rowmax, s.planes, s.plane_stride(),
+                                                          s.kpitch, s.scale);
     return launch_status("slice_rows_kernel");
 }
 
@@ -975,10 +1034,11 @@ int launch_colmax(const FieldIO& src, int K, int N, int fields, long long field_
 
 int launch_slice_cols(const FieldIO& src, int K, int N, int fields, long long field_stride,
                       const unsigned int* colmax, long long colmax_stride, SliceMat& s, int n_rows_per_field,
-                      cudaStream_t st) {
+                      cudaStream_t st, bool emb = false) {
     dim3 grid(ceil_div(N, 32), ceil_div(s.Kp, 32), fields);
     slice_cols_kernel<<<grid, dim3(32, 8), 0, st>>>(src, K, N, s.Kp, field_stride, colmax, colmax_stride, s.planes,
-                                                    s.plane_stride(), s.kpitch, n_rows_per_field, s.scale);
+                                                    s.plane_stride(), s.kpitch, n_rows_per_field, s.scale,
+                                                    emb ? 1 : 0);
     return launch_status("slice_cols_kernel");
 }
 
@@ -1079,9 +1139,10 @@ TileChoice choose_tile(long long m_tiles, int N, int grid_z, int ktiles, int sch
 
 struct GemmShape {
     long long m_tiles;
-    int N, grid_z, ktiles, sms, dev;
+    int N, grid_z, ktiles, sms, dev, emb;
     bool operator<(const GemmShape& o) const {
-        return std::tie(m_tiles, N, grid_z, ktiles, sms, dev) < std::tie(o.m_tiles, o.N, o.grid_z, o.ktiles, o.sms, o.dev);
+        return std::tie(m_tiles, N, grid_z, ktiles, sms, dev, emb) <
+               std::tie(o.m_tiles, o.N, o.grid_z, o.ktiles, o.sms, o.dev, o.emb);
     }
 };
 
@@ -1113,25 +1174,29 @@ std::atomic<int> g_autotune{0};
 std::mutex g_tune_mu;
 std::map<GemmShape, TunedEntry> g_tuned;
 
-template <int BN, int OUT, int SRC> int launch_tile(const GemmArgs& g, dim3 grid, cudaStream_t st) {
+template <int BN, int OUT, int SRC, int EMB> int launch_tile(const GemmArgs& g, dim3 grid, cudaStream_t st) {
     static bool configured[64];
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64 || !configured[dev]) {
-        HX_TRY(cuda_status(cudaFuncSetAttribute(split_gemm_kernel<BN, OUT, SRC>,
+        HX_TRY(cuda_status(cudaFuncSetAttribute(split_gemm_kernel<BN, OUT, SRC, EMB>,
                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, Tile<BN>::SMEM_BYTES),
                            "cudaFuncSetAttribute(split_gemm_kernel)"));
         if (dev >= 0 && dev < 64) configured[dev] = true;
     }
-    split_gemm_kernel<BN, OUT, SRC><<<grid, NUM_THREADS, Tile<BN>::SMEM_BYTES, st>>>(g);
+    split_gemm_kernel<BN, OUT, SRC, EMB><<<grid, NUM_THREADS, Tile<BN>::SMEM_BYTES, st>>>(g);
     return launch_status("split_gemm_kernel");
+}
+
+template <int BN, int OUT, int SRC> int launch_emb(const GemmArgs& g, dim3 grid, cudaStream_t st) {
+    return g.emb ? launch_tile<BN, OUT, SRC, 1>(g, grid, st) : launch_tile<BN, OUT, SRC, 0>(g, grid, st);
 }
 
 template <int BN, int OUT> int launch_src(const GemmArgs& g, dim3 grid, int src, cudaStream_t st) {
     switch (src) {
-        case FMT_NONE: return launch_tile<BN, OUT, FMT_NONE>(g, grid, st);
-        case FMT_C64: return launch_tile<BN, OUT, FMT_C64>(g, grid, st);
-        case FMT_C128: return launch_tile<BN, OUT, FMT_C128>(g, grid, st);
+        case FMT_NONE: return launch_emb<BN, OUT, FMT_NONE>(g, grid, st);
+        case FMT_C64: return launch_emb<BN, OUT, FMT_C64>(g, grid, st);
+        case FMT_C128: return launch_emb<BN, OUT, FMT_C128>(g, grid, st);
         default:
             set_error("internal: unsupported Babinet source format");
             return HX_ERR_INVALID;
@@ -1149,7 +1214,7 @@ template <int BN> int launch_out(const GemmArgs& g, dim3 grid, int out, int src,
 // One launch with a given tile choice.  partial / counters: split-K workspace (unused when c.ksplit == 1).
 int launch_choice(GemmArgs& g, const SliceMat& A, const SliceMat& B, const TileChoice& c, int grid_z,
                   float* partial, unsigned int* counters, double cmacs, bool traced, cudaStream_t st) {
-    const long long m_tiles = A.rows / BM;
+    const long long m_tiles = ceil_div(A.rows, BM);
     if (m_tiles > 65535 || grid_z > 65535 || (long long)c.n_tiles * c.ksplit > 2147483647LL) {
         set_error("split GEMM grid too large");
         return HX_ERR_UNSUPPORTED;
@@ -1230,7 +1295,9 @@ int launch_gemm(GemmArgs& g, const SliceMat& A, const SliceMat& B, TileChoice c,
     if (g_autotune.load(std::memory_order_relaxed) && !fbn && !fks) {
         int dev = 0;
         cudaGetDevice(&dev);
-        const GemmShape key{A.rows / BM, g.N, grid_z, A.kpitch / BK, sm_count(), dev};
+        // with the embedding on B, a complex column is two B' rows
+        const GemmShape key{ceil_div(A.rows, BM), g.emb ? 2 * g.N : g.N, grid_z, A.kpitch / BK, sm_count(), dev,
+                            g.emb};
         bool found = false;
         {
             std::lock_guard<std::mutex> lock(g_tune_mu);
@@ -1276,9 +1343,10 @@ struct SplitMftPlan {
 
 namespace {
 
-// Slice a phase matrix (rows x cols, evaluated on the device) as an A (row) or B (column) operand.
+// Slice a phase matrix (rows x cols, evaluated on the device) as an A (row) or B (column) operand; emb: a B operand
+// that carries the complex embedding (two rows per column, see the file comment).
 int slice_phase(int rows, int cols, const double* a, const double* b, double sign, const double* wr,
-                const double* wc, bool as_rows, SliceMat& out, cudaStream_t st) {
+                const double* wc, bool as_rows, SliceMat& out, cudaStream_t st, bool emb = false) {
     void* tmp = nullptr;
     const long long n = (long long)rows * cols;
     Carver count(nullptr);
@@ -1298,7 +1366,7 @@ int slice_phase(int rows, int cols, const double* a, const double* b, double sig
             } else {
                 rc = cuda_status(cudaMemsetAsync(mx, 0, sizeof(unsigned int) * round_up(cols, 64), st), "memset");
                 if (rc == HX_OK) rc = launch_colmax(f, rows, cols, 1, 0, mx, 0, st);
-                if (rc == HX_OK) rc = launch_slice_cols(f, rows, cols, 1, 0, mx, 0, out, 0, st);
+                if (rc == HX_OK) rc = launch_slice_cols(f, rows, cols, 1, 0, mx, 0, out, 0, st, emb);
             }
         }
     }
@@ -1320,6 +1388,9 @@ struct Ws {
     unsigned int* counters = nullptr;
 };
 
+// The GEMMs whose A operand is the per-call field (the forward transform's first, the backward transform's
+// second) carry the embedding on their constant B operand: the field is sliced once as [Re | Im] rows, and the
+// tile logic counts two B' rows per complex output column.
 void carve_ws(Carver& c, const SplitMftPlan* p, int direction, int batch, Ws& w) {
     long long g1_rows, g2_rows;
     int g1_n, g1_z, g1_kt, g2_n, g2_z, g2_kt;
@@ -1327,28 +1398,28 @@ void carve_ws(Carver& c, const SplitMftPlan* p, int direction, int batch, Ws& w)
     const long long nu64 = round_up(p->nu, 64);
     const long long b_rows = round_up(batch * nu64, 128);
     if (direction == HX_FORWARD) {
-        carve_slices(c, w.s1, 2 * round_up(rows, 64), p->nx, rows);
+        carve_slices(c, w.s1, round_up(rows, BM), p->nx, rows);  // rows past the field: discarded tile rows
         w.t = carve_ff(c, rows * p->nu);
         w.t_max = (unsigned int*)c.take(sizeof(unsigned int) * batch * nu64);
         carve_slices(c, w.s2, b_rows, p->ny, b_rows);
-        g1_rows = w.s1.rows, g1_n = p->nu, g1_z = 1, g1_kt = w.s1.kpitch / BK;
+        g1_rows = w.s1.rows, g1_n = 2 * p->nu, g1_z = 1, g1_kt = w.s1.kpitch / BK;
         g2_rows = p->m1f.rows, g2_n = p->nu, g2_z = batch, g2_kt = p->m1f.kpitch / BK;
     } else {
         w.in_max = (unsigned int*)c.take(sizeof(unsigned int) * batch * nu64);
         carve_slices(c, w.s1, b_rows, p->nv, b_rows);
         w.t = carve_ff(c, rows * p->nu);
         w.t_max = (unsigned int*)c.take(sizeof(unsigned int) * rows);
-        carve_slices(c, w.s2, 2 * round_up(rows, 64), p->nu, rows);
+        carve_slices(c, w.s2, round_up(rows, BM), p->nu, rows);
         g1_rows = p->m1b.rows, g1_n = p->nu, g1_z = batch, g1_kt = p->m1b.kpitch / BK;
-        g2_rows = w.s2.rows, g2_n = p->nx, g2_z = 1, g2_kt = w.s2.kpitch / BK;
+        g2_rows = w.s2.rows, g2_n = 2 * p->nx, g2_z = 1, g2_kt = w.s2.kpitch / BK;
     }
-    w.c1 = choose_tile(g1_rows / BM, g1_n, g1_z, g1_kt, p->schedule);
-    w.c2 = choose_tile(g2_rows / BM, g2_n, g2_z, g2_kt, p->schedule);
+    w.c1 = choose_tile(ceil_div(g1_rows, BM), g1_n, g1_z, g1_kt, p->schedule);
+    w.c2 = choose_tile(ceil_div(g2_rows, BM), g2_n, g2_z, g2_kt, p->schedule);
     // split-K workspace for every candidate tile of both GEMMs, so the layout does not depend on the choice
     size_t part = 0;
     long long tiles = 0;
     for (const TileChoice* t : {&w.c1, &w.c2}) {
-        const long long m_tiles = t == &w.c1 ? g1_rows / BM : g2_rows / BM;
+        const long long m_tiles = t == &w.c1 ? ceil_div(g1_rows, BM) : ceil_div(g2_rows, BM);
         for (const TileChoice& cand : tile_candidates(m_tiles, t == &w.c1 ? g1_n : g2_n, t == &w.c1 ? g1_z : g2_z,
                                                       t == &w.c1 ? g1_kt : g2_kt)) {
             part = std::max(part, cand.partial_floats());
@@ -1375,9 +1446,11 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
     carve_ws(c, p, direction, batch, w);
     if (direction == HX_FORWARD) {
         HX_TRY(cuda_status(cudaMemsetAsync(w.t_max, 0, sizeof(unsigned int) * batch * nu64, st), "memset"));
-        // G1: T = E . M2f, stacked over the batch; column maxima of T per field for the next slicing.
-        HX_TRY(launch_slice_rows(in, nx, rows, nx, in_max, w.s1, st));
+        // G1: T = E . M2f, stacked over the batch (embedding on M2f); column maxima of T per field for the next
+        // slicing.
+        HX_TRY(launch_slice_rows(in, nx, rows, nx, in_max, w.s1, st, true));
         GemmArgs g1 = base_args(p->status);
+        g1.emb = 1;
         g1.M = (int)rows;
         g1.N = nu;
         g1.row_scale = w.s1.scale;
@@ -1435,9 +1508,10 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
     g1.rowmax = w.t_max;
     g1.rowmax_z = ny;
     HX_TRY(launch_gemm(g1, m1, w.s1, w.c1, batch, w.partial, w.counters, (double)ny * nu * nv * batch, p->schedule, st));
-    // G2: out = alpha T . M2, stacked over the batch, with the fused epilogue.
-    HX_TRY(launch_slice_rows(w.t, nu, rows, nu, w.t_max, w.s2, st));
+    // G2: out = alpha T . M2, stacked over the batch (embedding on M2), with the fused epilogue.
+    HX_TRY(launch_slice_rows(w.t, nu, rows, nu, w.t_max, w.s2, st, true));
     GemmArgs g2 = base_args(p->status);
+    g2.emb = 1;
     g2.M = (int)rows;
     g2.N = nx;
     g2.row_scale = w.s2.scale;
@@ -1469,14 +1543,17 @@ int split_mft_create(int nx, int ny, int nu, int nv, const double* x, const doub
     SplitMftPlan* p = new SplitMftPlan();
     p->nx = nx; p->ny = ny; p->nu = nu; p->nv = nv;
     const bool own_adj = wx || wy || wu || wv;
+    // m2f, m2b, m2a are the B operands of GEMMs whose A is the field: they carry the embedding (two rows per
+    // column, blocks of 8 columns); the padding rows are zero, and rows past them read as zeros through the TMA
+    // bounds.
     auto layout = [&](Carver& c) {
-        carve_slices(c, p->m2f, round_up(nu, 128), nx, round_up(nu, 64));
+        carve_slices(c, p->m2f, round_up(2LL * nu, 128), nx, round_up(nu, 64));
         carve_slices(c, p->m1f, 2 * round_up(nv, 64), ny, nv);
         carve_slices(c, p->m1b, 2 * round_up(ny, 64), nv, ny);
-        carve_slices(c, p->m2b, round_up(nx, 128), nu, round_up(nx, 64));
+        carve_slices(c, p->m2b, round_up(2LL * nx, 128), nu, round_up(nx, 64));
         if (own_adj) {
             carve_slices(c, p->m1a, 2 * round_up(ny, 64), nv, ny);
-            carve_slices(c, p->m2a, round_up(nx, 128), nu, round_up(nx, 64));
+            carve_slices(c, p->m2a, round_up(2LL * nx, 128), nu, round_up(nx, 64));
         }
         p->status = (int*)c.take(sizeof(int));
     };
@@ -1492,14 +1569,14 @@ int split_mft_create(int nx, int ny, int nu, int nv, const double* x, const doub
             p->m2a = p->m2b;
         }
         // forward: M2f[x,u] = wx exp(-i x u) as B (K = x rows, N = u); M1f[v,y] = exp(-i v y) wy as A
-        rc = slice_phase(nx, nu, x, u, -1.0, wx, nullptr, false, p->m2f, st);
+        rc = slice_phase(nx, nu, x, u, -1.0, wx, nullptr, false, p->m2f, st, true);
         if (rc == HX_OK) rc = slice_phase(nv, ny, v, y, -1.0, nullptr, wy, true, p->m1f, st);
         // backward: M1b[y,v] = exp(+i y v) wv as A; M2b[u,x] = wu exp(+i u x) as B
         if (rc == HX_OK) rc = slice_phase(ny, nv, y, v, +1.0, nullptr, wv, true, p->m1b, st);
-        if (rc == HX_OK) rc = slice_phase(nu, nx, u, x, +1.0, wu, nullptr, false, p->m2b, st);
+        if (rc == HX_OK) rc = slice_phase(nu, nx, u, x, +1.0, wu, nullptr, false, p->m2b, st, true);
         if (rc == HX_OK && own_adj) {
             rc = slice_phase(ny, nv, y, v, +1.0, wy, nullptr, true, p->m1a, st);
-            if (rc == HX_OK) rc = slice_phase(nu, nx, u, x, +1.0, nullptr, wx, false, p->m2a, st);
+            if (rc == HX_OK) rc = slice_phase(nu, nx, u, x, +1.0, nullptr, wx, false, p->m2a, st, true);
         }
     }
     if (rc != HX_OK) {
