@@ -10,6 +10,7 @@
 //                         evaluate_supersampled (hcipy/field/util.py:655-692)
 #include "hx_common.cuh"
 #include "fft_line.cuh"
+#include "fft_pow2.cuh"
 
 #include <algorithm>
 #include <complex>
@@ -129,8 +130,68 @@ int run_line_m(const LineArgs<T>& a, int threads, size_t smem, int sign, bool co
                     : launch_line<T, 1, false, MIXED>(a, threads, smem, batch, s);
 }
 
+// Threads per CTA of the register-resident power-of-two kernel: 512.  HX_FFT_P2_THREADS (256 or 512) and
+// HX_FFT_P2_THREADS_LF (256, 512 or 1024, strided lines) override it (tuning).
+int p2_threads(bool lf) {
+    static int v[2] = {0, 0};
+    if (!v[lf]) {
+        const char* e = getenv(lf ? "HX_FFT_P2_THREADS_LF" : "HX_FFT_P2_THREADS");
+        const int x = e ? atoi(e) : 0;
+        v[lf] = (x == 256 || x == 512 || (x == 1024 && lf)) ? x : 512;
+    }
+    return v[lf];
+}
+
+template <int N, int SIGN, bool LF>
+int launch_p2(const LineArgs<float>& a0, int batch, cudaStream_t stream) {
+    using P = Pow2Shape<N>;
+    LineArgs<float> a = a0;
+    const int lpc = std::max(1, std::min(p2_threads(LF) / P::T, a.nlines));
+    a.lines_per_cta = lpc;
+    const size_t smem = sizeof(float2) * (size_t)lpc * P::PITCH;
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(fft_pow2_kernel<N, SIGN, LF>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        configured = true;
+    }
+    dim3 grid((a.nlines + lpc - 1) / lpc, batch);
+    if (grid.y > 65535u) {
+        set_error("FFT batch too large (%d)", batch);
+        return HX_ERR_UNSUPPORTED;
+    }
+    TraceScope trace(HX_TRACE_FFT, (double)a.nlines * (a.in_count + a.out_count) * batch * sizeof(float2), stream);
+    fft_pow2_kernel<N, SIGN, LF><<<grid, lpc * P::T, smem, stream>>>(a);
+    return launch_status("fft_pow2_kernel");
+}
+
+template <int N>
+int run_p2_n(const LineArgs<float>& a, int sign, int batch, cudaStream_t s) {
+    const bool lf = a.in_es != 1;
+    if (sign < 0) return lf ? launch_p2<N, -1, true>(a, batch, s) : launch_p2<N, -1, false>(a, batch, s);
+    return lf ? launch_p2<N, 1, true>(a, batch, s) : launch_p2<N, 1, false>(a, batch, s);
+}
+
+// The register-resident kernel takes complex64 power-of-two lines of 256 to 4096 points without Bluestein chirps
+// or a spectrum multiply, whose input and output lines are both contiguous or both strided; -1 otherwise.
+int run_p2(const LineArgs<float>& a, int sign, bool conv, int batch, cudaStream_t s) {
+    if (conv || !a.tws || a.chirp_in || a.chirp_out || a.n_log != a.M || (a.in_es != 1) != (a.out_es != 1))
+        return -1;
+    switch (a.M) {
+        case 256: return run_p2_n<256>(a, sign, batch, s);
+        case 512: return run_p2_n<512>(a, sign, batch, s);
+        case 1024: return run_p2_n<1024>(a, sign, batch, s);
+        case 2048: return run_p2_n<2048>(a, sign, batch, s);
+        case 4096: return run_p2_n<4096>(a, sign, batch, s);
+        default: return -1;
+    }
+}
+
 template <typename T>
 int run_line(const LineArgs<T>& a, int threads, size_t smem, int sign, bool conv, int batch, cudaStream_t s) {
+    if constexpr (sizeof(T) == 4) {
+        const int rc = run_p2(a, sign, conv, batch, s);
+        if (rc != -1) return rc;
+    }
     bool mixed = false;
     unsigned long long code = a.radix_code;
     for (int i = 0; i < a.nstages; ++i, code >>= 5) {
@@ -244,9 +305,29 @@ struct AxisTables {
     bool bluestein = false;
     std::vector<int> radices;
     DevBuf tw;
+    DevBuf tws;  // stage twiddle tables of the register-resident kernel (complex64 power-of-two axes)
     DevBuf chirp_f, chirp_i;  // conj(b) for forward, b for inverse (length N)
     DevBuf spec_f, spec_i;    // FFT_M of the wrapped kernel / M
 };
+
+// Stage twiddle tables of an N-point power-of-two line for fft_pow2_kernel: exp(-2 pi i p k / (16 NS)) for
+// NS = 16, 256 and p = 1, 2, 4, 8, each row NS entries long (float64 arguments, rounded once).
+template <typename T>
+int make_stage_tables(DevBuf& dst, int N, cudaStream_t s) {
+    if (sizeof(T) != 4 || N < 256 || N > 4096 || (N & (N - 1)) != 0) return HX_OK;
+    std::vector<cd> v(kP2TwEntries, cd(1, 0));
+    for (int NS : {16, 256}) {
+        const int off = NS == 16 ? p2_tw_offset<16>() : p2_tw_offset<256>();
+        if (NS == 256 && N < 4096) continue;
+        const int pw[4] = {1, 2, 4, 8};
+        for (int row = 0; row < 4; ++row)
+            for (int k = 0; k < NS; ++k) {
+                const double ang = -2.0 * M_PI * (double)(pw[row] * k) / (16.0 * NS);
+                v[off + row * NS + k] = cd(std::cos(ang), std::sin(ang));
+            }
+    }
+    return upload_c<T>(dst, v, s);
+}
 
 template <typename T>
 int make_axis(AxisTables& ax, int N, cudaStream_t s) {
@@ -255,6 +336,7 @@ int make_axis(AxisTables& ax, int N, cudaStream_t s) {
     ax.radices = factor_radices(N, r16);
     if (!ax.radices.empty()) {
         ax.M = N;
+        HX_TRY(make_stage_tables<T>(ax.tws, N, s));
         return make_twiddles<T>(ax.tw, N, s);
     }
     ax.bluestein = true;
@@ -294,6 +376,7 @@ template <typename T>
 void axis_args(const AxisTables& ax, int sign, LineArgs<T>& a, bool* conv, int* launch_sign) {
     using Cx = typename cplx<T>::type;
     a.tw = (const Cx*)ax.tw.p;
+    a.tws = (const Cx*)ax.tws.p;
     a.n_log = ax.N;
     a.out_mod = ax.N;
     if (ax.bluestein) {
@@ -604,6 +687,7 @@ int filter_execute_t(const hx_filter_plan* p, int adjoint, int batch, const void
         size_t smem;
         HX_TRY(hx::launch_shape<T>(ax.M, ax.radices, ny, batch, 1, a, &thr, &smem));
         a.tw = (const Cx*)ax.tw.p;
+        a.tws = (const Cx*)ax.tws.p;
         a.n_log = Nx; a.nlines = ny;
         a.in = (const Cx*)in; a.in_ls = nx; a.in_es = 1; a.in_bs = in_sz;
         a.in_count = nx; a.in_offset = p->c[0]; a.load_add = 0;
@@ -637,6 +721,7 @@ int filter_execute_t(const hx_filter_plan* p, int adjoint, int batch, const void
         size_t smem;
         HX_TRY(hx::launch_shape<T>(ax.M, ax.radices, ny, batch, 1, a, &thr, &smem));
         a.tw = (const Cx*)ax.tw.p;
+        a.tws = (const Cx*)ax.tws.p;
         a.n_log = Nx; a.nlines = ny;
         a.in = (const Cx*)ws; a.in_ls = Nx; a.in_es = 1; a.in_bs = w_sz;
         a.in_count = Nx; a.in_offset = 0; a.load_add = 0;

@@ -58,6 +58,7 @@ struct LineArgs {
     const Cx* post;       // indexed [l*post_ls + kk*post_es], or null
     long long post_ls, post_es;
     Cx scale;
+    const Cx* tws;        // stage twiddle tables of the register-resident power-of-two kernel (fft_pow2.cuh)
 };
 
 template <typename Cx>
