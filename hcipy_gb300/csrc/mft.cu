@@ -86,6 +86,263 @@ void free_plan(hx_mft_plan* p) {
     delete p;
 }
 
+// ---- small transforms in one launch ------------------------------------------------------------------
+//
+// out[r, :] = alpha sum_q (A[r, :] . X[:, S_q]) . B[S_q, :] for a block of RPC output rows: A is R x K1, X one field
+// (K1 x K2), B K2 x C, out R x C, with the GEMM path's epilogues; forward A = M1f, X = E, B = M2f, backward A = M1b,
+// X = F, B = M2b.  The columns of X are cut into CS slices S_q and the CS CTAs of a thread-block cluster take one
+// slice each: CTA q forms w = A[rows] . X[:, S_q] and the partial image w . B[S_q, :], then the cluster adds the CS
+// partials of every output column in slice order through distributed shared memory, each CTA finishing C / CS of
+// the columns.  A CTA reads K1 x K2 / CS of the field and K2 / CS rows of B, so a transform whose two GEMMs would
+// occupy a few dozen SMs runs as one launch over ceil(R / RPC) x CS CTAs, and no intermediate leaves the cluster.
+// The products are associated by output rows (the same complex MACs as the two GEMMs); sums run in blocks of kBlk
+// terms added into the total, so FP32 rounding grows with sqrt(kBlk) + sqrt(K / kBlk) rather than sqrt(K).
+constexpr int kSmThreads = 256;
+constexpr int kSmRows = 4;     // output rows per cluster (RPC)
+constexpr int kSmSlices = 8;   // CTAs per cluster (CS)
+constexpr int kBlk = 16;       // terms per partial sum
+constexpr int kSmMaxBytes = 200 * 1024;
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+
+__device__ __forceinline__ unsigned cluster_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Shared-memory layout of the small-transform kernel (in elements of the complex type).
+struct SmLayout {
+    int xw, cw;                      // columns of X per slice, output columns per CTA
+    int a, x, b, w, part, total;     // offsets and total size
+    __host__ __device__ SmLayout(int K1, int K2, int C, int esize) {
+        xw = (K2 + kSmSlices - 1) / kSmSlices;
+        xw += xw & 1;  // even: 16-byte chunks of complex64
+        cw = (C + kSmSlices - 1) / kSmSlices;
+        a = 0;
+        x = a + kSmRows * K1;
+        b = x + K1 * xw;
+        w = b + xw * C;
+        part = w + 2 * kSmRows * xw;  // w holds two partial sums per element before they are added
+        total = part + kSmSlices * kSmRows * cw;
+        (void)esize;
+    }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kSmThreads) mft_small_kernel(int R, int K1, int K2, int C,
+                                                              typename hx::cplx<T>::type alpha,
+                                                              const typename hx::cplx<T>::type* __restrict__ A,
+                                                              const typename hx::cplx<T>::type* __restrict__ X,
+                                                              long long sX,
+                                                              const typename hx::cplx<T>::type* __restrict__ B,
+                                                              typename hx::cplx<T>::type* __restrict__ out,
+                                                              long long sO, hx::Epilogue<typename hx::cplx<T>::type> epi) {
+    using Cx = typename hx::cplx<T>::type;
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    Cx* sm = reinterpret_cast<Cx*>(sm_raw);
+    const SmLayout L(K1, K2, C, (int)sizeof(Cx));
+    const int q = (int)cluster_rank();
+    const int r0 = (blockIdx.x / kSmSlices) * kSmRows;
+    const int z = blockIdx.y;
+    const int x0 = q * L.xw;
+    const int xn = max(0, min(L.xw, K2 - x0));  // columns of this slice
+    const Cx zero = hx::make_c<T>(T(0), T(0));
+    Cx* a_s = sm + L.a;
+    Cx* x_s = sm + L.x;
+    Cx* b_s = sm + L.b;
+    Cx* w_s = sm + L.w;
+    Cx* part = sm + L.part;
+    // rows of A, the slice of X and the rows of B, by 16-byte asynchronous copies
+    constexpr int PER = 16 / (int)sizeof(Cx);  // complex elements per 16-byte chunk
+    const Cx* xf = X + sX * z;
+    {
+        // rows of A (rows past R read as zeros), 16-byte chunks: K1 * sizeof(Cx) is a multiple of 16
+        const int cpa = K1 / PER;
+        for (int c = threadIdx.x; c < kSmRows * cpa; c += kSmThreads) {
+            const int rr = c / cpa, j = c - rr * cpa;
+            if (r0 + rr < R) cp_async16(a_s + rr * K1 + j * PER, A + (long long)(r0 + rr) * K1 + j * PER);
+            else *reinterpret_cast<float4*>(a_s + rr * K1 + j * PER) = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        const int cpr = xn / PER;  // chunks per row of the X slice
+        for (int c = threadIdx.x; c < K1 * cpr; c += kSmThreads) {
+            const int y = c / cpr, j = c - y * cpr;
+            cp_async16(x_s + y * L.xw + j * PER, xf + (long long)y * K2 + x0 + j * PER);
+        }
+        const int bchunks = xn * C / PER;
+        for (int c = threadIdx.x; c < bchunks; c += kSmThreads) cp_async16(b_s + c * PER, B + (long long)x0 * C + c * PER);
+        asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+    }
+    __syncthreads();
+    // w[rr][xl] = sum_y A[r0 + rr][y] X[y][x0 + xl], two threads per element (the halves of y), added in order
+    const int nw = kSmRows * xn;
+    const int yh = (K1 / 2 + kBlk - 1) / kBlk * kBlk;  // first y of the second half
+    for (int i = threadIdx.x; i < 2 * nw; i += kSmThreads) {
+        const int h = i / nw, o = i - h * nw;
+        const int rr = o / xn, xl = o - rr * xn;
+        Cx acc = zero;
+        for (int y0 = h ? yh : 0; y0 < (h ? K1 : min(K1, yh)); y0 += kBlk) {
+            Cx blk = zero;
+            const int y1 = min(K1, y0 + kBlk);
+#pragma unroll 4
+            for (int y = y0; y < y1; ++y) {
+                const Cx av = a_s[rr * K1 + y], xv = x_s[y * L.xw + xl];
+                blk.x = fma(av.x, xv.x, blk.x);
+                blk.x = fma(-av.y, xv.y, blk.x);
+                blk.y = fma(av.x, xv.y, blk.y);
+                blk.y = fma(av.y, xv.x, blk.y);
+            }
+            acc.x += blk.x;
+            acc.y += blk.y;
+        }
+        w_s[h * kSmRows * L.xw + rr * L.xw + xl] = acc;
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < nw; o += kSmThreads) {
+        const int rr = o / xn, xl = o - rr * xn;
+        const Cx p1 = w_s[kSmRows * L.xw + rr * L.xw + xl];
+        w_s[rr * L.xw + xl].x += p1.x;
+        w_s[rr * L.xw + xl].y += p1.y;
+    }
+    __syncthreads();
+    // partial image p[rr][u] = sum_xl w[rr][xl] B[x0 + xl][u], sent to the CTA that finishes column u
+    cluster_barrier();  // every CTA of the cluster may now receive
+    for (int i = threadIdx.x; i < kSmRows * C; i += kSmThreads) {
+        const int rr = i / C, u = i - rr * C;
+        Cx acc = zero;
+        for (int j0 = 0; j0 < xn; j0 += kBlk) {
+            Cx blk = zero;
+            const int j1 = min(xn, j0 + kBlk);
+#pragma unroll 4
+            for (int j = j0; j < j1; ++j) {
+                const Cx wv = w_s[rr * L.xw + j], bv = b_s[j * C + u];
+                blk.x = fma(wv.x, bv.x, blk.x);
+                blk.x = fma(-wv.y, bv.y, blk.x);
+                blk.y = fma(wv.x, bv.y, blk.y);
+                blk.y = fma(wv.y, bv.x, blk.y);
+            }
+            acc.x += blk.x;
+            acc.y += blk.y;
+        }
+        const int owner = u / L.cw, ul = u - owner * L.cw;
+        Cx* dst = part + (q * kSmRows + rr) * L.cw + ul;
+        if (owner == q) {
+            *dst = acc;
+        } else {
+            unsigned raddr;
+            asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+                         : "=r"(raddr)
+                         : "r"((unsigned)__cvta_generic_to_shared(dst)), "r"((unsigned)owner));
+            if constexpr (sizeof(T) == 4)
+                asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(raddr), "f"(acc.x), "f"(acc.y) : "memory");
+            else
+                asm volatile("st.shared::cluster.v2.f64 [%0], {%1, %2};" ::"r"(raddr), "d"(acc.x), "d"(acc.y) : "memory");
+        }
+    }
+    cluster_barrier();  // every partial is in place
+    const long long obase = sO * z;
+    const int cn = max(0, min(L.cw, C - q * L.cw));
+    for (int i = threadIdx.x; i < kSmRows * cn; i += kSmThreads) {
+        const int rr = i / cn, ul = i - rr * cn;
+        const long long r = r0 + rr;
+        if (r >= R) continue;
+        Cx acc = zero;
+#pragma unroll
+        for (int sp = 0; sp < kSmSlices; ++sp) {
+            const Cx p = part[(sp * kSmRows + rr) * L.cw + ul];
+            acc.x += p.x;
+            acc.y += p.y;
+        }
+        const int u = q * L.cw + ul;
+        Cx v = hx::cmul(alpha, acc);
+        const long long frow = (r % epi.rows_per_field) * C;
+        if (epi.kind == hx::EPI_MUL) {
+            v = hx::cmul(v, epi.mask[frow + u]);
+        } else if (epi.kind == hx::EPI_BABINET) {
+            const Cx e = epi.src[obase + r * C + u];
+            v.x = e.x - v.x;
+            v.y = e.y - v.y;
+            if (epi.mask) v = hx::cmul(v, epi.mask[frow + u]);
+        }
+        out[obase + r * C + u] = v;
+    }
+}
+
+// Whether a transform takes the one-launch form: small enough that its two GEMMs would leave most SMs idle (at
+// most 512 points per axis, a few fields), with its slices of X and rows of B in shared memory, rows of whole
+// 16-byte chunks, and a cluster of kSmSlices such CTAs resident on this device.
+template <typename T>
+bool small_form_ok(int R, int K1, int K2, int C, int batch, const void* X, long long sX) {
+    using Cx = typename hx::cplx<T>::type;
+    static const bool allowed = [] {  // HX_MFT_SMALL=0 keeps every transform on the two GEMMs (comparisons)
+        const char* e = getenv("HX_MFT_SMALL");
+        return !(e && e[0] == '0');
+    }();
+    if (!allowed) return false;
+    if (R > 512 || C > 512 || K1 > 512 || K2 > 512 || batch > 8 || C < kSmSlices || K2 < 2 * kSmSlices) return false;
+    if (sizeof(Cx) == 8 && ((K1 | K2 | C) & 1)) return false;
+    if ((reinterpret_cast<uintptr_t>(X) & 15) != 0 || (sX * (long long)sizeof(Cx)) % 16 != 0) return false;
+    const SmLayout L(K1, K2, C, (int)sizeof(Cx));
+    if (sizeof(Cx) * (size_t)L.total > kSmMaxBytes) return false;
+    if (L.xw * (kSmSlices - 1) >= K2) return false;  // every slice holds columns
+    static int ok[64];  // per device: 0 unknown, 1 yes, 2 no
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    if (!ok[dev]) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(kSmSlices, 1, 1);
+        cfg.blockDim = dim3(kSmThreads);
+        cfg.dynamicSmemBytes = kSmMaxBytes;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = kSmSlices;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int n = 0;
+        const bool good = cudaFuncSetAttribute(mft_small_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               kSmMaxBytes) == cudaSuccess &&
+                          cudaOccupancyMaxActiveClusters(&n, mft_small_kernel<T>, &cfg) == cudaSuccess && n > 0;
+        cudaGetLastError();
+        ok[dev] = good ? 1 : 2;
+    }
+    return ok[dev] == 1;
+}
+
+template <typename T>
+int run_small(int R, int K1, int K2, int C, typename hx::cplx<T>::type alpha, const void* A, const void* X,
+              long long sX, const void* B, void* out, long long sO, int batch,
+              hx::Epilogue<typename hx::cplx<T>::type> epi, cudaStream_t stream) {
+    using Cx = typename hx::cplx<T>::type;
+    const SmLayout L(K1, K2, C, (int)sizeof(Cx));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(hx::ceil_div(R, kSmRows) * kSmSlices, batch, 1);
+    cfg.blockDim = dim3(kSmThreads);
+    cfg.dynamicSmemBytes = sizeof(Cx) * (size_t)L.total;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kSmSlices;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    hx::TraceScope trace(HX_TRACE_SIMT_GEMM, (double)batch * ((double)R * K1 * K2 + (double)R * K2 * C), stream);
+    HX_TRY(hx::cuda_status(cudaLaunchKernelEx(&cfg, mft_small_kernel<T>, R, K1, K2, C, alpha, (const Cx*)A,
+                                              (const Cx*)X, sX, (const Cx*)B, (Cx*)out, sO, epi),
+                           "mft_small_kernel"));
+    return hx::launch_status(sizeof(T) == 4 ? "mft_small_kernel<float>" : "mft_small_kernel<double>");
+}
+
 template <typename T>
 int execute_t(const hx_mft_plan* p, int direction, int batch, const void* in_, void* out_, double are, double aim,
               int epilogue, const void* mask, const void* src, void* ws_, cudaStream_t stream) {
@@ -101,6 +358,18 @@ int execute_t(const hx_mft_plan* p, int direction, int batch, const void* in_, v
     epi.kind = epilogue;
     epi.mask = (const Cx*)mask;
     epi.src = (const Cx*)src;
+    if (!tp) {
+        // small transforms: one launch (see mft_small_kernel)
+        const bool fwd = direction == HX_FORWARD;
+        const int R = fwd ? nv : ny, K1 = fwd ? ny : nv, K2 = fwd ? nx : nu, C = fwd ? nu : nx;
+        if (small_form_ok<T>(R, K1, K2, C, batch, in, (long long)K1 * K2)) {
+            const void* A = fwd ? p->m1f : direction == HX_BACKWARD ? p->m1b : p->m1a;
+            const void* B = fwd ? p->m2f : direction == HX_BACKWARD ? p->m2b : p->m2a;
+            epi.rows_per_field = R;
+            return run_small<T>(R, K1, K2, C, alpha, A, in, (long long)K1 * K2, B, out, (long long)R * C, batch, epi,
+                                stream);
+        }
+    }
     if (direction == HX_FORWARD) {
         // T (batch*ny x nu) = in (batch*ny x nx) . M2f (nx x nu)
         HX_TRY(hx::cgemm_nn<T>(batch * ny, nu, nx, one, in, nx, 0, (const Cx*)p->m2f, nu, 0, T1, nu, 0, 1, stream, {},
