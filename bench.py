@@ -341,6 +341,8 @@ def run_atmosphere(args, dev, peaks):
         layer.evolve_until((f + 1) * 1e-3)
     t_frame1.record()
     t_frame1.synchronize()
+    frame_ms = t_frame0.elapsed_time(t_frame1) / frames
+    multi = time_multilayer(dev, hbm)
     from oracle import atmosphere as oatm
     screen = layer.achromatic_screen.data.double().cpu().numpy()
     rng = np.random.default_rng(0)
@@ -356,7 +358,7 @@ def run_atmosphere(args, dev, peaks):
         'extrusion_frac_of_hbm': ab_bytes / (ext_us * 1e-6) / 1e9 / hbm,
         'extrusion_bytes': int(ab_bytes), 'shift_us': shift_us,
         'shift_GBps': 2 * 4 * pupil.size / (shift_us * 1e-6) / 1e9,
-        'frame_ms': t_frame0.elapsed_time(t_frame1) / frames,
+        'frame_ms': frame_ms, 'three_layers': multi,
         'frame': 'evolve_until for a 1 ms step: 3-4 extrusions (noise drawn on the host) and one shift, wall '
                  'time on the GPU including the host calls between launches',
         'kernel_timing': 'CUDA events around each extrusion / shift launch (hx_trace_enable)',
@@ -364,6 +366,77 @@ def run_atmosphere(args, dev, peaks):
         'cpu_baseline': 'oracle extrusion (the reference algorithm: float64 GEMV + screen copy in numpy), %d steps '
                         'on the host' % cpu_n,
         'peak_note': 'hbm_gbs of measured' if 'hbm_gbs' in peaks else 'fallback',
+    }
+
+
+def time_multilayer(dev, hbm):
+    """The broadband workload's three float32 1024^2 layers (r0 0.1/0.2/0.3 m, L0 25 m, winds 10/15/25 m/s):
+    one extrusion of every layer in one launch (hx_atmosphere_extrude_layers) and the shift of the three screens
+    with their sum in one pass (hx_atmosphere_shift_layers), CUDA events around each launch; then whole 1 ms
+    frames of MultiLayerAtmosphere.evolve_until (host plans and noise draws included)."""
+    import torch
+    import hcipy_gb300 as hg
+    from hcipy_gb300 import _lib, workloads
+    w = workloads.broadband_turbulence_workload()
+    pupil = w['pupil']
+    layers = [hg.InfiniteAtmosphericLayer(pupil, hg.Cn_squared_from_fried_parameter(lay['r0'], 500e-9), L0=w['L0'],
+                                          velocity=lay['velocity'], seed=lay['seed'], dtype=torch.float32)
+              for lay in w['layers']]
+    atm = hg.MultiLayerAtmosphere(layers)
+    noise = torch.randn(3, layers[0].B_horizontal.shape[1], device=dev)
+    lib, stream = _lib.lib(), _lib.stream_handle()
+
+    def extrude_all():
+        steps = (_lib.Extrusion * 3)(*[layer._extrusion('right', noise[i]) for i, layer in enumerate(layers)])
+        _lib.check(lib.hx_atmosphere_extrude_layers(steps, 3, _lib.HX_F32, stream), 'hx_atmosphere_extrude_layers')
+        for layer in layers:
+            layer._moved('right')
+
+    for _ in range(4):
+        extrude_all()
+    torch.cuda.synchronize()
+    n = 60
+    _lib.trace_read(_lib.HX_TRACE_ATMOSPHERE, reset=True)
+    _lib.trace_enable(True)
+    for _ in range(n):
+        extrude_all()
+    torch.cuda.synchronize()
+    _lib.trace_enable(False)
+    k, ms, _ = _lib.trace_read(_lib.HX_TRACE_ATMOSPHERE, reset=True)
+    ext_us = ms / max(k, 1) * 1e3
+    ab_bytes = 4.0 * sum(layer.A_horizontal.size + layer.B_horizontal.size for layer in layers)
+    t = 0.0
+    for _ in range(3):
+        t += w['frame_time']
+        atm.evolve_until(t)
+    torch.cuda.synchronize()
+    # the shift-and-sum pass alone: frames whose layers do not move (t unchanged) run only that launch
+    _lib.trace_enable(True)
+    for _ in range(n):
+        atm.evolve_until(t)
+    torch.cuda.synchronize()
+    _lib.trace_enable(False)
+    k, ms, _ = _lib.trace_read(_lib.HX_TRACE_ATMOSPHERE, reset=True)
+    shift_us = ms / max(k, 1) * 1e3
+    frames = 50
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = hg.launch_count()
+    ev0.record()
+    for _ in range(frames):
+        t += w['frame_time']
+        atm.evolve_until(t)
+    ev1.record()
+    ev1.synchronize()
+    return {
+        'extrusion_us': ext_us, 'extrusion_bytes': int(ab_bytes),
+        'extrusion_GBps': ab_bytes / (ext_us * 1e-6) / 1e9,
+        'extrusion_frac_of_hbm': ab_bytes / (ext_us * 1e-6) / 1e9 / hbm,
+        'extrusion': 'one step of each of the three layers in one launch (A 1024x3072 and B 1024x1024 float32 '
+                     'each)',
+        'shift_and_sum_us': shift_us,
+        'shift_and_sum_GBps': 4.0 * 7 * pupil.size / (shift_us * 1e-6) / 1e9,
+        'frame_ms': ev0.elapsed_time(ev1) / frames,
+        'launches_per_frame': (hg.launch_count() - launches0) / frames,
     }
 
 
@@ -550,6 +623,52 @@ def run_lyot_batched(args, dev, ref_img, peak_img):
     return out
 
 
+def time_efc_step(em, field, dz_dev, actuators, dev, steps=50):
+    """hx_efc_step alone (dark-zone gather, float64 EFC-matrix product in float-float, update), CUDA events on
+    the launching stream around each launch, L2 flushed between launches outside the events.  Algorithmic
+    bytes: the matrix once, the gathered field values, indices, commands in and out."""
+    import torch
+    from hcipy_gb300 import _lib
+    idx = torch.nonzero(dz_dev.reshape(-1)).reshape(-1).to(torch.int32).contiguous()
+    m = em.to(torch.float64).contiguous()
+    e = field.reshape(-1).contiguous()
+    a = actuators.to(torch.float64).contiguous()
+    out = torch.empty_like(a)
+    nact, n_dz = int(m.shape[0]), int(idx.numel())
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    lib = _lib.lib()
+
+    def launch():
+        _lib.check(lib.hx_efc_step(_lib.dptr(m), nact, n_dz, _lib.dptr(e), _lib.dtype_code(e.dtype), _lib.dptr(idx),
+                                   _lib.dptr(a), 0.5, _lib.dptr(out), _lib.stream_handle()), 'hx_efc_step')
+
+    for _ in range(3):
+        launch()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for i in range(steps):
+        flush.fill_(float(i))
+        ev[i][0].record(stream)
+        launch()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    us = 1e3 * sum(x.elapsed_time(y) for x, y in ev) / steps
+    nbytes = 8.0 * nact * 2 * n_dz + e.element_size() * n_dz + 4.0 * n_dz + 16.0 * nact
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        pass
+    hbm = peaks.get('hbm_gbs', 6800.0)
+    return {'matrix': [nact, 2 * n_dz], 'field_dtype': str(e.dtype).replace('torch.', ''), 'us_per_step': us,
+            'algorithmic_bytes': nbytes, 'achieved_gbs': nbytes / (us * 1e-6) / 1e9,
+            'frac_of_hbm': nbytes / (us * 1e-6) / 1e9 / hbm,
+            'peak_note': 'hbm_gbs of measured' if 'hbm_gbs' in peaks else 'fallback',
+            'timing': 'CUDA events around each launch, L2 flushed between launches outside the events'}
+
+
 def run_efc(args, dev):
     """Electric-field conjugation on the gradient workload's optics (512^2 pupil, 952-actuator DM, Lyot
     coronagraph, 256^2 image, dark zone = the 3-12 lambda/D half annulus): the poke Jacobian of every actuator
@@ -604,6 +723,7 @@ def run_efc(args, dev):
     torch.cuda.synchronize()
     t_loop = time.perf_counter() - t0
     ni = [float((f[dz_dev].abs()**2).mean()) / peak for f in fields]
+    step_leg = time_efc_step(em, fields[-1], dz_dev, hist[-1], dev)
     # host: the same pokes through the reference algorithm's port (complex128, matrices precomputed), a bounded
     # sample of actuators, extrapolated to all of them
     chain = optics.LyotChain(oracle_grid(pupil), oracle_grid(fpm_grid), oracle_grid(focal), w['fpm'], w['stop'])
@@ -624,6 +744,7 @@ def run_efc(args, dev):
         'jacobian_s': t_jac, 'propagations_per_s_in_jacobian': 2 * nact / t_jac,
         'tikhonov_inverse_s': t_inv[1], 'tikhonov_first_call_s': t_inv[0], 'efc_iterations': iters, 'efc_ms_per_iteration': 1e3 * t_loop / iters,
         'dark_zone_ni_first_last': [ni[0], ni[-1]],
+        'efc_step_kernel': step_leg,
         'timing': 'host wall clock with a device synchronize on both sides',
         'cpu_baseline': {'jacobian_s_estimate': cpu_per_act * nact, 'cores': host_cores(), 'kind': 'port',
                          'sample': '%d of %d actuators (2 pokes each) through the numpy port, complex128, '

@@ -57,6 +57,8 @@ SIGNATURES = {
     'hx_autotune_entries': (c_int, []),
     'hx_autotune_entry': (c_int, [c_int, P(c_ll), P(c_int), P(c_int), P(c_int), P(ctypes.c_float)]),
     'hx_autotune_clear': (c_int, []),
+    'hx_efc_step': (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_void_p, c_void_p, c_double, c_void_p,
+                            c_void_p]),
     'hx_intensity_sums_workspace_bytes': (c_size_t, [c_ll, c_int]),
     'hx_intensity_sums': (c_int, [c_void_p, c_int, c_ll, c_int, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     'hx_intensity_sums_grad': (c_int, [c_void_p, c_int, c_ll, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
@@ -64,13 +66,18 @@ SIGNATURES = {
                                    c_void_p]),
     'hx_influence_apply_transpose': (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p,
                                              c_void_p, c_void_p]),
+    'hx_influence_apply_transpose_blocked': (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_int,
+                                                     c_void_p, c_void_p, c_void_p]),
     'hx_phase_apply': (c_int, [c_ll, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_double, c_void_p, c_void_p]),
     'hx_phase_apply_grad': (c_int, [c_ll, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_double, c_void_p,
                                     c_void_p, c_void_p, c_void_p]),
     'hx_atmosphere_extrude': (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p,
-                                      c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
-    'hx_atmosphere_shift': (c_int, [c_void_p, c_int, c_int, c_int, c_int, P(c_double), P(c_double), c_void_p, c_int,
-                                    c_void_p]),
+                                      c_void_p, c_int, c_void_p, c_int, c_void_p]),
+    'hx_atmosphere_extrude_layers': (c_int, [c_void_p, c_int, c_int, c_void_p]),
+    'hx_atmosphere_shift': (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, P(c_double), P(c_double),
+                                    c_void_p, c_int, c_void_p]),
+    'hx_atmosphere_shift_layers': (c_int, [P(c_void_p), c_int, c_int, c_int, c_int, c_int, P(c_int), P(c_int),
+                                           P(c_double), P(c_double), P(c_void_p), c_void_p, c_int, c_void_p]),
     'hx_mft_plan_set_schedule': (c_int, [c_void_p, c_int]),
     'hx_atmosphere_combine': (c_int, [P(c_void_p), c_int, c_ll, c_void_p, c_int, c_void_p]),
     'hx_trace_read': (c_int, [c_int, P(c_ll), P(c_double), P(c_double), c_int]),
@@ -116,6 +123,13 @@ SIGNATURES = {
 }
 
 _lib = None
+
+
+class Extrusion(ctypes.Structure):
+    """``hx_extrusion``: one extrusion step of one layer (device pointers, ring sizes and offsets)."""
+    _fields_ = [('ring', c_void_p), ('stencil_idx', c_void_p), ('A', c_void_p), ('B', c_void_p),
+                ('noise', c_void_p), ('ny', c_int), ('nx', c_int), ('row0', c_int), ('col0', c_int),
+                ('where', c_int), ('nst', c_int), ('nb', c_int)]
 
 
 class HXError(RuntimeError):

@@ -6,13 +6,16 @@ von Karman covariances and autoregressive matrices A = C_xz C_zz^-1 and B from t
 (:142-202), and the same extrusion and time stepping (:216-364).  Plan-time work (covariances, Cholesky,
 SVD) runs on the host in float64 as in the reference; every frame runs on the GPU:
 
-* the screen is a ring buffer, so an extrusion moves an offset and writes one row or column
-  (``hx_atmosphere_extrude``: A . stencil + B . noise) instead of copying the screen;
+* the screen is a ring buffer with a spare row and column, so an extrusion moves an offset and writes one row
+  or column into the spare slice (``hx_atmosphere_extrude``: A . stencil + B . noise, the stencil gathered by
+  the same launch) instead of copying the screen; a ``MultiLayerAtmosphere`` frame extrudes step k of all its
+  layers in one launch (``hx_atmosphere_extrude_layers``);
 * the extrusion noise is drawn on the host from the layer's numpy Generator with the reference's call,
   ``rng.normal(0, sqrt(Cn^2), size=B.shape[1])``, one draw per step in the reference's order, so a layer seeded
   like the reference's extrudes the same rows;
 * the quintic sub-pixel shift (hcipy/_math/subpixel_shift.py) reads the ring and writes the shifted screen
-  (``hx_atmosphere_shift``);
+  (``hx_atmosphere_shift``); a ``MultiLayerAtmosphere`` frame shifts all its layers and sums their screens in
+  one pass (``hx_atmosphere_shift_layers``);
 * ``forward``/``backward`` multiply by exp(+-i screen / lambda) in one kernel (``hx_phase_apply``).
 
 The initial screen is the reference's: multi-scale spectral noise at oversampling 16
@@ -234,7 +237,7 @@ def subpixel_shift(img, row_shift, col_shift):
     tr = np.ascontiguousarray(quintic_weights(col_shift))
     tc = np.ascontiguousarray(quintic_weights(row_shift))
     P = _lib.ctypes.POINTER(_lib.ctypes.c_double)
-    rc = _lib.lib().hx_atmosphere_shift(_lib.dptr(t), int(ny), int(nx), 0, 0, tr.ctypes.data_as(P),
+    rc = _lib.lib().hx_atmosphere_shift(_lib.dptr(t), int(ny), int(nx), int(ny), int(nx), 0, 0, tr.ctypes.data_as(P),
                                         tc.ctypes.data_as(P), _lib.dptr(out), _lib.dtype_code(t.dtype),
                                         _lib.stream_handle())
     _lib.check(rc, 'hx_atmosphere_shift')
@@ -242,6 +245,42 @@ def subpixel_shift(img, row_shift, col_shift):
 
 
 # ---- layers ---------------------------------------------------------------------------------------------
+
+class _NoiseStage(object):
+    """Noise rows to the device without stalling the host: the rows go through one of two pinned host buffers
+    with an asynchronous copy on the current stream, so evolving a layer does not wait for the GPU work queued
+    before it (a copy from pageable memory would); a buffer is refilled only after the event recorded behind its
+    previous copy."""
+
+    def __init__(self, dtype):
+        self.dtype = dtype
+        self.slot = 1
+        self.host, self.event = [None, None], [None, None]
+        self.dev = None
+
+    def upload(self, draws):
+        """(len(draws), width) device tensor of the rows, zero-padded to the longest."""
+        width = max(x.size for x in draws)
+        need = len(draws) * width
+        self.slot = slot = (self.slot + 1) % 2
+        if self.event[slot] is not None:
+            self.event[slot].synchronize()
+        buf = self.host[slot]
+        if buf is None or buf.numel() < need:
+            buf = self.host[slot] = torch.empty(need, dtype=self.dtype, pin_memory=True)
+        if self.dev is None or self.dev.numel() < need:
+            self.dev = torch.empty(need, dtype=self.dtype, device='cuda')
+        host = buf[:need].numpy().reshape(len(draws), width)
+        host[...] = 0
+        for i, x in enumerate(draws):
+            host[i, :x.size] = x
+        dev = self.dev[:need]
+        dev.copy_(buf[:need], non_blocking=True)
+        if self.event[slot] is None:
+            self.event[slot] = torch.cuda.Event()
+        self.event[slot].record()
+        return dev.view(len(draws), width)
+
 
 class AtmosphericLayer(OpticalElement):
     """Base of the atmospheric layers (atmospheric_model.py:10-151): E exp(+-i phase_for(lambda))."""
@@ -379,17 +418,19 @@ class InfiniteAtmosphericLayer(AtmosphericLayer):
         else:
             self.rng = copy.deepcopy(self._original_rng)
         if self._initial_screen is not None:
-            ring = torch.from_numpy(np.ascontiguousarray(self._initial_screen.reshape(self.ny, self.nx)))
+            screen = torch.from_numpy(np.ascontiguousarray(self._initial_screen.reshape(self.ny, self.nx)))
         else:
-            ring = self._reference_initial_screen()
-        ring = ring.to(device='cuda', dtype=self.dtype).reshape(self.ny, self.nx)
-        if getattr(self, '_ring', None) is not None and self._ring.shape == ring.shape:
+            screen = self._reference_initial_screen()
+        screen = screen.to(device='cuda', dtype=self.dtype).reshape(self.ny, self.nx)
+        if getattr(self, '_ring', None) is not None and self._ring.shape == (self.ny + 1, self.nx + 1):
             # in place: a captured CUDA graph that reads these buffers stays valid across resets
-            self._ring.copy_(ring)
-            self._shifted.copy_(ring)
+            self._ring[:self.ny, :self.nx].copy_(screen)
+            self._shifted.copy_(screen)
         else:
-            self._ring = ring
-            self._shifted = ring.clone()
+            # the ring holds a spare row and column (outside the screen) that the next extrusion writes
+            self._ring = torch.zeros((self.ny + 1, self.nx + 1), dtype=self.dtype, device='cuda')
+            self._ring[:self.ny, :self.nx].copy_(screen)
+            self._shifted = screen.clone()
         self._row0 = 0
         self._col0 = 0
         self._version += 1
@@ -423,31 +464,45 @@ class InfiniteAtmosphericLayer(AtmosphericLayer):
             self._make_ab_matrices()
 
     # -- time stepping -------------------------------------------------------------------------------------
-    def _extrude(self, where, noise):
-        w = _WHERE[where]
+    def _step_matrices(self, where):
         d = self._dev
-        vertical = w <= 1
-        A, B, idx = (d['A_v'], d['B_v'], d['idx_v']) if vertical else (d['A_h'], d['B_h'], d['idx_h'])
-        rc = _lib.lib().hx_atmosphere_extrude(_lib.dptr(self._ring), self.ny, self.nx, self._row0, self._col0, w,
-                                              _lib.dptr(idx), int(idx.numel()), _lib.dptr(A), _lib.dptr(B),
-                                              int(B.shape[1]), _lib.dptr(noise), _lib.dtype_code(self.dtype),
-                                              _lib.dptr(self._work), _lib.stream_handle())
-        _lib.check(rc, 'hx_atmosphere_extrude')
-        self._version += 1
-        if w == 0:
-            self._row0 = (self._row0 - 1) % self.ny
-        elif w == 1:
-            self._row0 = (self._row0 + 1) % self.ny
-        elif w == 2:
-            self._col0 = (self._col0 - 1) % self.nx
-        else:
-            self._col0 = (self._col0 + 1) % self.nx
+        if _WHERE[where] <= 1:
+            return d['A_v'], d['B_v'], d['idx_v']
+        return d['A_h'], d['B_h'], d['idx_h']
 
-    def evolve_until(self, t):
-        """infinite_atmospheric_layer.py:305-364."""
-        if t is None:
-            self.reset()
-            return
+    def _extrusion(self, where, noise):
+        """The ``hx_extrusion`` record of one step from the current offsets."""
+        A, B, idx = self._step_matrices(where)
+        return _lib.Extrusion(_lib.dptr(self._ring), _lib.dptr(idx), _lib.dptr(A), _lib.dptr(B), _lib.dptr(noise),
+                              self.ny, self.nx, self._row0, self._col0, _WHERE[where], int(idx.numel()),
+                              int(B.shape[1]))
+
+    def _moved(self, where):
+        """The offsets after an extrusion (the spare slice becomes the new edge)."""
+        w = _WHERE[where]
+        if w == 0:
+            self._row0 = (self._row0 - 1) % (self.ny + 1)
+        elif w == 1:
+            self._row0 = (self._row0 + 1) % (self.ny + 1)
+        elif w == 2:
+            self._col0 = (self._col0 - 1) % (self.nx + 1)
+        else:
+            self._col0 = (self._col0 + 1) % (self.nx + 1)
+        self._version += 1
+
+    def _extrude(self, where, noise):
+        A, B, idx = self._step_matrices(where)
+        rc = _lib.lib().hx_atmosphere_extrude(_lib.dptr(self._ring), self.ny, self.nx, self._row0, self._col0,
+                                              _WHERE[where], _lib.dptr(idx), int(idx.numel()), _lib.dptr(A),
+                                              _lib.dptr(B), int(B.shape[1]), _lib.dptr(noise),
+                                              _lib.dtype_code(self.dtype), _lib.stream_handle())
+        _lib.check(rc, 'hx_atmosphere_extrude')
+        self._moved(where)
+
+    def _advance(self, t):
+        """The host part of ``evolve_until`` (infinite_atmospheric_layer.py:305-364): moves the layer's clock and
+        centre, draws the steps' noise from the generator in the reference's order and returns (steps, noise rows,
+        row taps, column taps) for the device."""
         if t < self._t:
             raise ValueError('Backwards temporal evolution is not allowed.')
         delta = self._delta
@@ -459,58 +514,43 @@ class InfiniteAtmosphericLayer(AtmosphericLayer):
         sub = self.center - new_center * delta
         plan = (['left' if steps[0] < 0 else 'right'] * abs(int(steps[0])) +
                 ['bottom' if steps[1] < 0 else 'top'] * abs(int(steps[1])))
-        if plan:
-            std = math.sqrt(self._Cn_squared)
-            draws = [self.rng.normal(0, std, size=(self.B_vertical if _WHERE[w] <= 1 else self.B_horizontal).shape[1])
-                     for w in plan]
-            noise = self._upload_noise(draws)
-            for i, w in enumerate(plan):
-                self._extrude(w, noise[i])
+        std = math.sqrt(self._Cn_squared)
+        draws = [self.rng.normal(0, std, size=(self.B_vertical if _WHERE[w] <= 1 else self.B_horizontal).shape[1])
+                 for w in plan]
         if self.use_interpolation:
             shift = sub / delta  # [x_px, y_px]
             taps_row = quintic_weights(shift[0])  # along x
             taps_col = quintic_weights(shift[1])  # along y
         else:
             taps_row = taps_col = np.array([0, 0, 0, 1.0, 0, 0, 0])
+        return plan, draws, taps_row, taps_col
+
+    def evolve_until(self, t):
+        """infinite_atmospheric_layer.py:305-364."""
+        if t is None:
+            self.reset()
+            return
+        plan, draws, taps_row, taps_col = self._advance(t)
+        if plan:
+            noise = self._upload_noise(draws)
+            for i, w in enumerate(plan):
+                self._extrude(w, noise[i])
         self._shift(taps_row, taps_col)
 
     def _upload_noise(self, draws):
-        """The step's noise rows on the device (len(draws) x width, zero-padded), without stalling the host.
-
-        The rows go through one of two pinned host buffers with an asynchronous copy on the current stream, so
-        evolving the layer does not wait for the GPU work queued before it (a copy from pageable memory would);
-        a buffer is refilled only after the event recorded behind its previous copy."""
-        width = max(x.size for x in draws)
-        need = len(draws) * width
-        self._noise_slot = slot = (getattr(self, '_noise_slot', 1) + 1) % 2
-        if not hasattr(self, '_noise_host'):
-            self._noise_host, self._noise_event = [None, None], [None, None]
-            self._noise_dev = None
-        if self._noise_event[slot] is not None:
-            self._noise_event[slot].synchronize()
-        buf = self._noise_host[slot]
-        if buf is None or buf.numel() < need:
-            buf = self._noise_host[slot] = torch.empty(need, dtype=self.dtype, pin_memory=True)
-        if self._noise_dev is None or self._noise_dev.numel() < need:
-            self._noise_dev = torch.empty(need, dtype=self.dtype, device='cuda')
-        host = buf[:need].numpy().reshape(len(draws), width)
-        host[...] = 0
-        for i, x in enumerate(draws):
-            host[i, :x.size] = x
-        dev = self._noise_dev[:need]
-        dev.copy_(buf[:need], non_blocking=True)
-        if self._noise_event[slot] is None:
-            self._noise_event[slot] = torch.cuda.Event()
-        self._noise_event[slot].record()
-        return dev.view(len(draws), width)
+        """The steps' noise rows on the device (len(draws) x width, zero-padded), without stalling the host."""
+        if getattr(self, '_noise', None) is None:
+            self._noise = _NoiseStage(self.dtype)
+        return self._noise.upload(draws)
 
     def _shift(self, taps_row, taps_col):
         tr = np.ascontiguousarray(taps_row, np.float64)
         tc = np.ascontiguousarray(taps_col, np.float64)
         P = _lib.ctypes.POINTER(_lib.ctypes.c_double)
-        rc = _lib.lib().hx_atmosphere_shift(_lib.dptr(self._ring), self.ny, self.nx, self._row0, self._col0,
-                                            tr.ctypes.data_as(P), tc.ctypes.data_as(P), _lib.dptr(self._shifted),
-                                            _lib.dtype_code(self.dtype), _lib.stream_handle())
+        rc = _lib.lib().hx_atmosphere_shift(_lib.dptr(self._ring), self.ny + 1, self.nx + 1, self.ny, self.nx,
+                                            self._row0, self._col0, tr.ctypes.data_as(P), tc.ctypes.data_as(P),
+                                            _lib.dptr(self._shifted), _lib.dtype_code(self.dtype),
+                                            _lib.stream_handle())
         _lib.check(rc, 'hx_atmosphere_shift')
         self._version += 1
 
@@ -521,9 +561,9 @@ class InfiniteAtmosphericLayer(AtmosphericLayer):
         taps = np.array([0, 0, 0, 1.0, 0, 0, 0])
         out = torch.empty_like(self._shifted)
         P = _lib.ctypes.POINTER(_lib.ctypes.c_double)
-        rc = _lib.lib().hx_atmosphere_shift(_lib.dptr(self._ring), self.ny, self.nx, self._row0, self._col0,
-                                            taps.ctypes.data_as(P), taps.ctypes.data_as(P), _lib.dptr(out),
-                                            _lib.dtype_code(self.dtype), _lib.stream_handle())
+        rc = _lib.lib().hx_atmosphere_shift(_lib.dptr(self._ring), self.ny + 1, self.nx + 1, self.ny, self.nx,
+                                            self._row0, self._col0, taps.ctypes.data_as(P), taps.ctypes.data_as(P),
+                                            _lib.dptr(out), _lib.dtype_code(self.dtype), _lib.stream_handle())
         _lib.check(rc, 'hx_atmosphere_shift')
         return Field(out.reshape(-1), self.input_grid)
 
@@ -580,10 +620,69 @@ class MultiLayerAtmosphere(OpticalElement):
         return elements
 
     def evolve_until(self, t):
-        for layer in self.layers:
-            layer.evolve_until(t)
+        """Every layer to time t (atmospheric_model.py:237-246).  When the layers are infinite layers of one grid
+        and screen dtype (up to 8), the frame runs as one batch: the host plans and noise draws of all layers
+        (each layer's generator in the reference's order), one upload of the noise, one extrusion launch per step
+        index (step k of every layer that moves k or more pixels), then one pass that shifts every layer's screen
+        and writes their sum."""
+        if t is not None and self._batchable():
+            self._evolve_batched(t)
+        else:
+            for layer in self.layers:
+                layer.evolve_until(t)
         self._t = t
         self.combined_screen()
+
+    def _batchable(self):
+        layers = self.layers
+        if not layers or len(layers) > 8:
+            return False
+        if any(type(layer).evolve_until is not InfiniteAtmosphericLayer.evolve_until for layer in layers):
+            return False
+        first = layers[0]
+        return all(layer.nx == first.nx and layer.ny == first.ny and layer.dtype == first.dtype for layer in layers)
+
+    def _evolve_batched(self, t):
+        layers = self.layers
+        first = layers[0]
+        plans = [layer._advance(t) for layer in layers]
+        draws = [d for p in plans for d in p[1]]
+        if draws:
+            if getattr(self, '_noise', None) is None or self._noise.dtype != first.dtype:
+                self._noise = _NoiseStage(first.dtype)
+            noise = self._noise.upload(draws)
+            row0 = np.cumsum([0] + [len(p[0]) for p in plans])
+            lib, dtc, stream = _lib.lib(), _lib.dtype_code(first.dtype), _lib.stream_handle()
+            for k in range(max(len(p[0]) for p in plans)):
+                todo = [(layer, p[0][k], noise[row0[i] + k]) for i, (layer, p) in enumerate(zip(layers, plans))
+                        if len(p[0]) > k]
+                steps = (_lib.Extrusion * len(todo))(*[layer._extrusion(w, x) for layer, w, x in todo])
+                _lib.check(lib.hx_atmosphere_extrude_layers(steps, len(todo), dtc, stream),
+                           'hx_atmosphere_extrude_layers')
+                for layer, w, _ in todo:
+                    layer._moved(w)
+        n = len(layers)
+        screens = [layer._shifted for layer in layers]
+        if (self._combined is None or self._combined.dtype != first.dtype or
+                self._combined.numel() != screens[0].numel()):
+            self._combined = torch.empty_like(screens[0].reshape(-1))
+        c = _lib.ctypes
+        rings = (c.c_void_p * n)(*[_lib.dptr(layer._ring) for layer in layers])
+        outs = (c.c_void_p * n)(*[_lib.dptr(x) for x in screens])
+        r0, _ = _lib.iarr([layer._row0 for layer in layers])
+        c0, _ = _lib.iarr([layer._col0 for layer in layers])
+        taps_row = np.ascontiguousarray(np.concatenate([p[2] for p in plans]), np.float64)
+        taps_col = np.ascontiguousarray(np.concatenate([p[3] for p in plans]), np.float64)
+        P = c.POINTER(c.c_double)
+        rc = _lib.lib().hx_atmosphere_shift_layers(rings, n, first.ny + 1, first.nx + 1, first.ny, first.nx,
+                                                   c.cast(r0, c.POINTER(c.c_int)), c.cast(c0, c.POINTER(c.c_int)),
+                                                   taps_row.ctypes.data_as(P), taps_col.ctypes.data_as(P), outs,
+                                                   _lib.dptr(self._combined), _lib.dtype_code(first.dtype),
+                                                   _lib.stream_handle())
+        _lib.check(rc, 'hx_atmosphere_shift_layers')
+        for layer in layers:
+            layer._version += 1
+        self._combined_key = tuple((id(layer), layer._version, s.data_ptr()) for layer, s in zip(layers, screens))
 
     def reset(self, make_independent_realization=False):
         for layer in self.layers:

@@ -1,147 +1,312 @@
 // Infinite atmospheric layer on the device (hcipy/atmosphere/infinite_atmospheric_layer.py:216-364).
 //
-// The achromatic screen (ny x nx) lives in a ring buffer: logical pixel (i, j) is stored at
-// ((i + row0) mod ny, (j + col0) mod nx).  An extrusion (:216-259) moves an offset by one and writes the new
-// row or column into the slot that the shift frees, instead of copying the whole screen as the reference
-// does.  The new slice is the autoregressive step  A . stencil + B . noise  (one warp per new pixel), with the
-// stencil gathered through the ring mapping and the flat reversal the reference applies for 'top'/'right'.
-// The quintic sub-pixel shift (hcipy/_math/subpixel_shift.py:7-343: 7-tap B-spline, clamp to edge, rows then
-// columns) reads the ring and writes the logical screen in one tiled pass.
+// The achromatic screen (ny x nx) lives in a ring buffer of (ny + 1) x (nx + 1) values: logical pixel (i, j) is
+// stored at ((i + row0) mod (ny + 1), (j + col0) mod (nx + 1)).  The ring's spare row and spare column lie outside
+// the logical screen; an extrusion (:216-259) moves an offset by one so that the spare slice becomes the new
+// edge row or column and the slice that falls off becomes the spare.  The new slice is the autoregressive step
+// A . stencil + B . noise; since it is written only into the spare slice, no stencil pixel of the same step is
+// overwritten and the stencil is gathered by the same launch that writes (the reference copies the whole
+// screen instead).  The extrusions of several layers (one step of each) run as one launch.  The quintic
+// sub-pixel shift (hcipy/_math/subpixel_shift.py:7-343: 7-tap B-spline, clamp to edge, rows then columns) reads
+// the rings and writes the layers' logical screens and their sum in one tiled pass.
+#include <type_traits>
+
 #include "hx_common.cuh"
+#include "tc_ptx.cuh"
 
 namespace {
 
-// Logical flat index of the (possibly flipped) 1-D view -> physical flat index of the ring.
+// ---- extrusion ---------------------------------------------------------------------------------------------
+// The new slice (nslice values) is A (nslice x nst) . stencil + B (nslice x nb) . noise.  A cluster of XS CTAs
+// computes XRC new pixels; CTA `rank` takes the rank-th eighth of the stencil columns and of the noise columns
+// (split-K): it gathers only its part of the stencil through the ring mapping into shared memory and streams its
+// column slice of the XRC rows of A and B (each warp XRC / 8 rows at once, 16-byte loads where the rows allow
+// them).  The XS partial sums of each pixel meet in the first CTA's shared memory (distributed shared memory) and
+// are added in rank order there, so the result is deterministic.  A and B stream from HBM once per step; the
+// stencil is gathered once per cluster.
+constexpr int XL_MAX = 8;       // extrusions per launch
+constexpr int XS = 8;           // CTAs per cluster (column slices)
+constexpr int XRC = 32;         // new pixels per cluster
+constexpr int XTHREADS = 256;
+constexpr int XRW = XRC / (XTHREADS / 32);  // rows per warp
+constexpr int XCHUNK = 2048;    // stencil values staged per pass
+
+template <typename T>
+struct Extrusion {
+    T* ring;
+    const long long* idx;
+    const T* A;
+    const T* B;
+    const T* noise;
+    int ny, nx, row0, col0, where, nst, nb, nslice, block0;
+};
+
+template <typename T>
+struct ExtrusionSet {
+    Extrusion<T> l[XL_MAX];
+    int count;
+};
+
+// Logical flat index k of the (possibly flipped) 1-D view -> physical index in the ring.
 __device__ __forceinline__ long long ring_index(long long k, int ny, int nx, int row0, int col0, bool flip) {
     const long long n = (long long)ny * nx;
     if (flip) k = n - 1 - k;
-    const int i = (int)(k / nx), j = (int)(k % nx);
-    const int pi = (i + row0) % ny, pj = (j + col0) % nx;
-    return (long long)pi * nx + pj;
+    const int i = (int)(k / nx), j = (int)(k - (long long)(k / nx) * nx);
+    int pi = i + row0, pj = j + col0;  // offsets are in [0, ny] / [0, nx]: one subtraction wraps them
+    if (pi > ny) pi -= ny + 1;
+    if (pj > nx) pj -= nx + 1;
+    return (long long)pi * (nx + 1) + pj;
 }
 
-// Stencil values of the screen before the step (the logical 1-D view, flipped for 'top'/'right').  A separate
-// launch from the update below: the new slice overwrites a ring slot that a far stencil pixel may occupy.
-template <typename T>
-__global__ void gather_stencil_kernel(const T* ring, int ny, int nx, int row0, int col0, bool flip,
-                                      const long long* stencil_idx, int nst, T* stencil) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < nst) stencil[k] = ring[ring_index(stencil_idx[k], ny, nx, row0, col0, flip)];
-}
-
-// new_slice[r] = sum_k A[r, k] stencil[k] + sum_k B[r, k] noise[k], written into the ring slot that the shift
-// frees.  where: 0 bottom, 1 top, 2 left, 3 right; row0/col0 are the offsets before the step.  A CTA of 256
-// threads computes 2 rows with 4 warps per row, each warp a quarter of the stencil and of the noise, with
-// 16-byte loads when the rows allow them: A and B stream from HBM once per step, so the kernel is sized for
-// many requests in flight (512 CTAs for a 1024-pixel slice) and starts loading at once (no staging).
-constexpr int EXT_ROWS = 2;      // rows per CTA
-constexpr int EXT_WARPS_ROW = 4; // warps per row
-
-template <typename T>
-__device__ __forceinline__ T dot_part(const T* __restrict__ w, const T* __restrict__ x, int n, int part, int lane) {
-    // Elements [part * n / 4, (part + 1) * n / 4) of w . x, lanes strided; x (the stencil or the noise, a few
-    // KB shared by every CTA) is read through L1/L2 like w.
-    const int k0 = (int)((long long)n * part / EXT_WARPS_ROW);
-    const int k1 = (int)((long long)n * (part + 1) / EXT_WARPS_ROW);
-    T acc = T(0);
-    if (sizeof(T) == 4 && ((k0 & 3) == 0) && ((reinterpret_cast<size_t>(w + k0) & 15) == 0) &&
-        ((reinterpret_cast<size_t>(x + k0) & 15) == 0)) {
-        const int n4 = (k1 - k0) >> 2;
-        const float4* w4 = reinterpret_cast<const float4*>(w + k0);
-        const float4* x4 = reinterpret_cast<const float4*>(x + k0);
-#pragma unroll 4
-        for (int q = lane; q < n4; q += 32) {
-            const float4 a = __ldg(&w4[q]);
-            const float4 b = __ldg(&x4[q]);
-            acc += (T)(a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w);
-        }
-        for (int k = k0 + 4 * n4 + lane; k < k1; k += 32) acc += w[k] * x[k];
-    } else {
-#pragma unroll 4
-        for (int k = k0 + lane; k < k1; k += 32) acc += __ldg(&w[k]) * __ldg(&x[k]);
-    }
-    return acc;
-}
-
-template <typename T>
-__global__ void extrude_kernel(T* ring, int ny, int nx, int row0, int col0, int where, const T* stencil, int nst,
-                               const T* A, const T* B, int nb, const T* noise, int nslice) {
-    __shared__ T part_sum[EXT_ROWS][EXT_WARPS_ROW];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int rl = warp / EXT_WARPS_ROW, part = warp % EXT_WARPS_ROW;
-    const int r = blockIdx.x * EXT_ROWS + rl;
-    T acc = T(0);
-    if (r < nslice) {
-        acc = dot_part(A + (long long)r * nst, stencil, nst, part, lane) +
-              dot_part(B + (long long)r * nb, noise, nb, part, lane);
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    }
-    if (lane == 0) part_sum[rl][part] = acc;
-    __syncthreads();
-    if (part != 0 || lane != 0 || r >= nslice) return;
-    acc = part_sum[rl][0] + part_sum[rl][1] + part_sum[rl][2] + part_sum[rl][3];
-    // Destination in logical coordinates after the shift: bottom -> row 0, top -> row ny-1 reversed,
-    // left -> column 0, right -> column nx-1 reversed.
-    int i, j;
-    if (where == 0) { i = 0; j = r; }
-    else if (where == 1) { i = ny - 1; j = nx - 1 - r; }
-    else if (where == 2) { i = r; j = 0; }
-    else { i = ny - 1 - r; j = nx - 1; }
-    // Offsets after the shift.
-    int nr = row0, nc = col0;
-    if (where == 0) nr = (row0 + ny - 1) % ny;
-    else if (where == 1) nr = (row0 + 1) % ny;
-    else if (where == 2) nc = (col0 + nx - 1) % nx;
-    else nc = (col0 + 1) % nx;
-    ring[(long long)((i + nr) % ny) * nx + (j + nc) % nx] = acc;
-}
-
-struct Taps {
-    double row[7];  // applied along x (within a row)
-    double col[7];  // applied along y (within a column)
+template <typename T> struct Vec16;
+template <> struct Vec16<float> {
+    using V = float4;
+    static constexpr int N = 4;
+    __device__ static float dot(const float4& a, const float4& b) { return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w; }
+};
+template <> struct Vec16<double> {
+    using V = double2;
+    static constexpr int N = 2;
+    __device__ static double dot(const double2& a, const double2& b) { return a.x * b.x + a.y * b.y; }
 };
 
-constexpr int TS = 32;       // output tile
-constexpr int HALO = 3;      // 7-tap kernel
+// acc[q] += sum_k w_q[k] x[k] over k in [0, len) for the XRW rows w_q = w + q * ld (rows q >= nr are skipped),
+// lanes strided; 16-byte loads when every row and x are aligned.
+template <typename T>
+__device__ __forceinline__ void dot_rows(T* acc, const T* __restrict__ w, long long ld, int nr,
+                                         const T* __restrict__ x, int len, int lane) {
+    using VT = Vec16<T>;
+    using V = typename VT::V;
+    const bool vec = ((reinterpret_cast<size_t>(w) | reinterpret_cast<size_t>(x) |
+                       (size_t)(ld * (long long)sizeof(T))) & 15) == 0;
+    int k0 = 0;
+    if (vec) {
+        const int nv = len / VT::N;
+        const V* xv = reinterpret_cast<const V*>(x);
+#pragma unroll 2
+        for (int q = lane; q < nv; q += 32) {
+            const V xx = xv[q];
+            V ww[XRW];
+#pragma unroll
+            for (int r = 0; r < XRW; ++r)
+                if (r < nr) ww[r] = __ldg(reinterpret_cast<const V*>(w + r * ld) + q);
+#pragma unroll
+            for (int r = 0; r < XRW; ++r)
+                if (r < nr) acc[r] += VT::dot(ww[r], xx);
+        }
+        k0 = VT::N * nv;
+    }
+    for (int k = k0 + lane; k < len; k += 32) {
+        const T xx = x[k];
+#pragma unroll
+        for (int r = 0; r < XRW; ++r)
+            if (r < nr) acc[r] += __ldg(&w[r * ld + k]) * xx;
+    }
+}
+
+// Bounds of column slice s (of n) of [0, len): multiples of 4 elements, so that every slice keeps the alignment
+// of the row it starts from.
+__device__ __forceinline__ int slice_bound(int len, int s, int n) {
+    return s >= n ? len : (int)(((long long)len * s / n) & ~3LL);
+}
+
+// 16-byte remote store of any 16 bytes (the bits travel unchanged).
+template <typename T>
+__device__ __forceinline__ void st_remote16(uint32_t addr, const T* v) {
+    const uint4 u = *reinterpret_cast<const uint4*>(v);
+    asm volatile("st.shared::cluster.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(u.x), "r"(u.y), "r"(u.z),
+                 "r"(u.w)
+                 : "memory");
+}
+
+// SPLIT: CTAs per cluster (XS, or 1 where clusters cannot be launched).  Six CTAs per SM for the float clusters
+// (40 registers): the three 1024^2 layers' 768 CTAs fit in one wave.
+template <typename T, int SPLIT>
+__global__ void __launch_bounds__(XTHREADS, (sizeof(T) == 4 && SPLIT > 1) ? 6 : 1)
+    extrude_layers_kernel(const __grid_constant__ ExtrusionSet<T> set) {
+    __shared__ __align__(16) T st[XCHUNK];
+    __shared__ __align__(16) T part[SPLIT][XRC];
+    int li = 0;
+    for (int q = 1; q < set.count; ++q)
+        if ((int)blockIdx.x >= set.l[q].block0) li = q;
+    const Extrusion<T>& L = set.l[li];
+    const int rank = SPLIT > 1 ? (int)((blockIdx.x - L.block0) % SPLIT) : 0;
+    const int r0 = (int)((blockIdx.x - L.block0) / SPLIT) * XRC;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rw = r0 + warp * XRW;                     // first row of this warp
+    const int nr = max(0, min(XRW, L.nslice - rw));     // rows of this warp inside the slice
+    const bool flip = L.where == 1 || L.where == 3;
+    T acc[XRW];
+#pragma unroll
+    for (int r = 0; r < XRW; ++r) acc[r] = T(0);
+    // B . noise over this CTA's noise columns (independent of the stencil: its loads go out first)
+    {
+        const int b0 = slice_bound(L.nb, rank, SPLIT), b1 = slice_bound(L.nb, rank + 1, SPLIT);
+        if (nr > 0 && b1 > b0) dot_rows(acc, L.B + (long long)rw * L.nb + b0, L.nb, nr, L.noise + b0, b1 - b0, lane);
+    }
+    // A . stencil over this CTA's stencil columns, gathered through the ring in chunks
+    const int s0 = slice_bound(L.nst, rank, SPLIT), s1 = slice_bound(L.nst, rank + 1, SPLIT);
+    for (int c0 = s0; c0 < s1; c0 += XCHUNK) {
+        const int clen = min(XCHUNK, s1 - c0);
+        if (c0 > s0) __syncthreads();  // the previous chunk is consumed
+        for (int k = threadIdx.x; k < clen; k += XTHREADS)
+            st[k] = L.ring[ring_index(__ldg(&L.idx[c0 + k]), L.ny, L.nx, L.row0, L.col0, flip)];
+        __syncthreads();
+        if (nr > 0) dot_rows(acc, L.A + (long long)rw * L.nst + c0, L.nst, nr, st, clen, lane);
+    }
+#pragma unroll
+    for (int r = 0; r < XRW; ++r)
+        for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+    if constexpr (SPLIT > 1) {
+        // every CTA of the cluster has started before the first remote store; the partial sums of this warp's
+        // XRW rows go to the first CTA as 16-byte stores
+        hx::ptx::cluster_sync();
+        static_assert((XRW * sizeof(T)) % 16 == 0, "whole 16-byte stores");
+        if (lane == 0) {
+            const uint32_t dst = hx::ptx::map_shared_rank(hx::ptx::smem_addr(&part[rank][warp * XRW]), 0);
+#pragma unroll
+            for (int c = 0; c < (int)(XRW * sizeof(T) / 16); ++c) st_remote16(dst + 16 * c, acc + c * (16 / sizeof(T)));
+        }
+        hx::ptx::cluster_sync();
+        if (rank != 0) return;
+    } else {
+        if (lane == 0) {
+#pragma unroll
+            for (int r = 0; r < XRW; ++r) part[0][warp * XRW + r] = acc[r];
+        }
+        __syncthreads();
+    }
+    const int rl = threadIdx.x;
+    const int r = r0 + rl;
+    if (rl >= XRC || r >= L.nslice) return;
+    T v = part[0][rl];
+#pragma unroll
+    for (int q = 1; q < SPLIT; ++q) v += part[q][rl];
+    // Destination in logical coordinates after the shift: bottom -> row 0, top -> row ny-1 reversed,
+    // left -> column 0, right -> column nx-1 reversed; with the offsets after the shift it lands in the slice
+    // that was the spare one.
+    const int ny = L.ny, nx = L.nx, w = L.where;
+    int i, j;
+    if (w == 0) { i = 0; j = r; }
+    else if (w == 1) { i = ny - 1; j = nx - 1 - r; }
+    else if (w == 2) { i = r; j = 0; }
+    else { i = ny - 1 - r; j = nx - 1; }
+    int nrow0 = L.row0, ncol0 = L.col0;
+    if (w == 0) nrow0 = nrow0 == 0 ? ny : nrow0 - 1;
+    else if (w == 1) nrow0 = nrow0 == ny ? 0 : nrow0 + 1;
+    else if (w == 2) ncol0 = ncol0 == 0 ? nx : ncol0 - 1;
+    else ncol0 = ncol0 == nx ? 0 : ncol0 + 1;
+    int pi = i + nrow0, pj = j + ncol0;
+    if (pi > ny) pi -= ny + 1;
+    if (pj > nx) pj -= nx + 1;
+    L.ring[(long long)pi * (nx + 1) + pj] = v;
+}
+
+template <typename T>
+bool extrude_clusters_ok() {
+    static int ok[64];  // per device: 0 unknown, 1 yes, 2 no
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    if (!ok[dev]) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(XS, 1, 1);
+        cfg.blockDim = dim3(XTHREADS);
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = XS;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int n = 0;
+        const bool good =
+            cudaOccupancyMaxActiveClusters(&n, extrude_layers_kernel<T, XS>, &cfg) == cudaSuccess && n > 0;
+        cudaGetLastError();
+        ok[dev] = good ? 1 : 2;
+    }
+    return ok[dev] == 1;
+}
+
+// ---- sub-pixel shift and the sum of the layers' screens ------------------------------------------------------
+// A 32 x 32 output tile per CTA of 32 x 8 threads: the 38 x 38 input tile (clamped to the logical screen,
+// wrapped through the ring) in shared memory, the row filter into a 38 x 32 tile, the column filter to the
+// output; thread (tx, ty) owns column tx of rows ty + 8 m.  Layers one after the other, their filtered tiles
+// summed in registers in layer order.
+constexpr int SL_MAX = 8;
+constexpr int TS = 32;
+constexpr int HALO = 3;
 constexpr int TIN = TS + 2 * HALO;
 
-// Separable 7-tap filter with clamp-to-edge of the logical screen read from the ring; out is logical.
 template <typename T>
-__global__ void ring_shift_kernel(const T* ring, int ny, int nx, int row0, int col0, Taps taps, T* out) {
-    __shared__ T in[TIN][TIN + 1];
-    __shared__ T mid[TIN][TS + 1];
-    __shared__ T wr[7], wc[7];  // taps in the working type, converted once
+struct ShiftSet {
+    const T* ring[SL_MAX];
+    T* out[SL_MAX];
+    int row0[SL_MAX], col0[SL_MAX];
+    T taps_row[SL_MAX][7];  // along x (within a row), rounded to T on the host
+    T taps_col[SL_MAX][7];  // along y (within a column)
+    T* sum;
+    int count, ring_ny, ring_nx, ny, nx;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) shift_layers_kernel(const __grid_constant__ ShiftSet<T> set) {
+    __shared__ T in[TIN][TIN];
+    __shared__ T mid[TIN][TS];
+    const int tx = threadIdx.x, ty = threadIdx.y;
     const int x0 = blockIdx.x * TS, y0 = blockIdx.y * TS;
-    if (threadIdx.y == 0 && threadIdx.x < 7) {
-        wr[threadIdx.x] = (T)taps.row[threadIdx.x];
-        wc[threadIdx.x] = (T)taps.col[threadIdx.x];
-    }
-    for (int t = threadIdx.y * blockDim.x + threadIdx.x; t < TIN * TIN; t += blockDim.x * blockDim.y) {
-        const int ly = t / TIN, lx = t % TIN;
-        const int gy = min(max(y0 + ly - HALO, 0), ny - 1);
-        const int gx = min(max(x0 + lx - HALO, 0), nx - 1);
-        int py = gy + row0, px = gx + col0;  // offsets are in [0, n): one subtraction wraps them
-        if (py >= ny) py -= ny;
-        if (px >= nx) px -= nx;
-        in[ly][lx] = ring[(long long)py * nx + px];
-    }
-    __syncthreads();
-    // rows: mid[ly][x] = sum_k in[ly][x + k] * row[k]
-    for (int t = threadIdx.y * blockDim.x + threadIdx.x; t < TIN * TS; t += blockDim.x * blockDim.y) {
-        const int ly = t / TS, x = t % TS;
-        T s = T(0);
+    const int ny = set.ny, nx = set.nx;
+    T total[4] = {T(0), T(0), T(0), T(0)};
+    for (int l = 0; l < set.count; ++l) {
+        const T* ring = set.ring[l];
+        const int row0 = set.row0[l], col0 = set.col0[l];
+        // columns of the input tile this thread loads: tx and tx + 32 (< TIN)
+        int px[2];
 #pragma unroll
-        for (int k = 0; k < 7; ++k) s += in[ly][x + k] * wr[k];
-        mid[ly][x] = s;
-    }
-    __syncthreads();
-    for (int t = threadIdx.y * blockDim.x + threadIdx.x; t < TS * TS; t += blockDim.x * blockDim.y) {
-        const int y = t / TS, x = t % TS;
-        if (y0 + y >= ny || x0 + x >= nx) continue;
-        T s = T(0);
+        for (int h = 0; h < 2; ++h) {
+            const int gx = min(max(x0 + tx + 32 * h - HALO, 0), nx - 1);
+            int p = gx + col0;
+            if (p >= set.ring_nx) p -= set.ring_nx;
+            px[h] = p;
+        }
+        for (int ly = ty; ly < TIN; ly += 8) {
+            const int gy = min(max(y0 + ly - HALO, 0), ny - 1);
+            int py = gy + row0;
+            if (py >= set.ring_ny) py -= set.ring_ny;
+            const T* rrow = ring + (long long)py * set.ring_nx;
+            in[ly][tx] = rrow[px[0]];
+            if (tx + 32 < TIN) in[ly][tx + 32] = rrow[px[1]];
+        }
+        T wr[7], wc[7];
 #pragma unroll
-        for (int k = 0; k < 7; ++k) s += mid[y + k][x] * wc[k];
-        out[(long long)(y0 + y) * nx + x0 + x] = s;
+        for (int k = 0; k < 7; ++k) {
+            wr[k] = set.taps_row[l][k];
+            wc[k] = set.taps_col[l][k];
+        }
+        __syncthreads();
+        for (int ly = ty; ly < TIN; ly += 8) {
+            T s = T(0);
+#pragma unroll
+            for (int k = 0; k < 7; ++k) s += in[ly][tx + k] * wr[k];
+            mid[ly][tx] = s;
+        }
+        __syncthreads();
+        T* out = set.out[l];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const int y = ty + 8 * m;
+            T s = T(0);
+#pragma unroll
+            for (int k = 0; k < 7; ++k) s += mid[y + k][tx] * wc[k];
+            total[m] = l == 0 ? s : total[m] + s;
+            if (out && y0 + y < ny && x0 + tx < nx) out[(long long)(y0 + y) * nx + x0 + tx] = s;
+        }
+    }
+    if (set.sum) {
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const int y = ty + 8 * m;
+            if (y0 + y < ny && x0 + tx < nx) set.sum[(long long)(y0 + y) * nx + x0 + tx] = total[m];
+        }
     }
 }
 
@@ -154,7 +319,7 @@ struct ScreenSet {
 };
 
 template <typename T>
-__global__ void combine_screens_kernel(ScreenSet<T> set, int count, long long n, T* out) {
+__global__ void combine_screens_kernel(const __grid_constant__ ScreenSet<T> set, int count, long long n, T* out) {
     const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 4;
     if (i >= n) return;
     if (i + 4 <= n) {
@@ -183,62 +348,146 @@ __global__ void combine_screens_kernel(ScreenSet<T> set, int count, long long n,
 
 extern "C" {
 
-int hx_atmosphere_extrude(void* ring, int ny, int nx, int row0, int col0, int where, const long long* stencil_idx,
-                          int nst, const void* A, const void* B, int nb, const void* noise, int dtype, void* work,
-                          void* stream) {
-    HX_CHECK_ARG(ring && stencil_idx && A && B && noise && work, "hx_atmosphere_extrude: NULL pointer");
-    HX_CHECK_ARG(ny > 0 && nx > 0 && nst > 0 && nb > 0, "hx_atmosphere_extrude: sizes must be positive");
-    HX_CHECK_ARG(where >= 0 && where <= 3, "hx_atmosphere_extrude: where must be 0..3 (bottom, top, left, right)");
-    HX_CHECK_ARG(row0 >= 0 && row0 < ny && col0 >= 0 && col0 < nx, "hx_atmosphere_extrude: ring offsets out of range");
-    HX_CHECK_ARG(dtype == HX_F32 || dtype == HX_F64, "hx_atmosphere_extrude: dtype must be HX_F32 or HX_F64");
-    const int nslice = (where <= 1) ? nx : ny;
+int hx_atmosphere_extrude_layers(const hx_extrusion* steps, int count, int dtype, void* stream) {
+    HX_CHECK_ARG(steps || count == 0, "hx_atmosphere_extrude_layers: NULL steps");
+    HX_CHECK_ARG(count >= 0 && count <= XL_MAX, "hx_atmosphere_extrude_layers: count must be 0..%d (got %d)", XL_MAX,
+                 count);
+    HX_CHECK_ARG(dtype == HX_F32 || dtype == HX_F64, "hx_atmosphere_extrude_layers: dtype must be HX_F32 or HX_F64");
+    for (int l = 0; l < count; ++l) {
+        const hx_extrusion& e = steps[l];
+        HX_CHECK_ARG(e.ring && e.stencil_idx && e.A && e.B && e.noise, "hx_atmosphere_extrude: NULL pointer (step %d)",
+                     l);
+        HX_CHECK_ARG(e.ny > 0 && e.nx > 0 && e.nst > 0 && e.nb > 0, "hx_atmosphere_extrude: sizes must be positive");
+        HX_CHECK_ARG(e.where >= 0 && e.where <= 3,
+                     "hx_atmosphere_extrude: where must be 0..3 (bottom, top, left, right)");
+        HX_CHECK_ARG(e.row0 >= 0 && e.row0 <= e.ny && e.col0 >= 0 && e.col0 <= e.nx,
+                     "hx_atmosphere_extrude: ring offsets out of range (row0 in [0, ny], col0 in [0, nx])");
+        for (int q = 0; q < l; ++q)
+            HX_CHECK_ARG(steps[q].ring != e.ring, "hx_atmosphere_extrude_layers: ring %d appears twice in one launch",
+                         l);
+    }
+    if (count == 0) return HX_OK;
     if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
     cudaStream_t st = (cudaStream_t)stream;
-    const bool flip = where == 1 || where == 3;
-    const int threads = 32 * EXT_ROWS * EXT_WARPS_ROW;
-    dim3 grid(hx::ceil_div(nslice, EXT_ROWS));
-    if (dtype == HX_F32) {
-        gather_stencil_kernel<float><<<hx::ceil_div(nst, 256), 256, 0, st>>>((const float*)ring, ny, nx, row0, col0,
-                                                                             flip, stencil_idx, nst, (float*)work);
-        HX_TRY(hx::launch_status("gather_stencil_kernel"));
-        hx::TraceScope trace(HX_TRACE_ATMOSPHERE, 4.0 * ((double)nslice * (nst + nb) + nst + nb), st);
-        extrude_kernel<float><<<grid, threads, 0, st>>>((float*)ring, ny, nx, row0, col0, where,
-                                                          (const float*)work, nst, (const float*)A, (const float*)B,
-                                                          nb, (const float*)noise, nslice);
-    } else {
-        gather_stencil_kernel<double><<<hx::ceil_div(nst, 256), 256, 0, st>>>((const double*)ring, ny, nx, row0,
-                                                                              col0, flip, stencil_idx, nst,
-                                                                              (double*)work);
-        HX_TRY(hx::launch_status("gather_stencil_kernel"));
-        hx::TraceScope trace(HX_TRACE_ATMOSPHERE, 8.0 * ((double)nslice * (nst + nb) + nst + nb), st);
-        extrude_kernel<double><<<grid, threads, 0, st>>>((double*)ring, ny, nx, row0, col0, where,
-                                                           (const double*)work, nst, (const double*)A,
-                                                           (const double*)B, nb, (const double*)noise, nslice);
-    }
-    return hx::launch_status("extrude_kernel");
+    const size_t esz = dtype == HX_F32 ? 4 : 8;
+    auto run = [&](auto* tag) -> int {
+        using T = std::remove_pointer_t<decltype(tag)>;
+        const bool cl = extrude_clusters_ok<T>();
+        const int split = cl ? XS : 1;
+        ExtrusionSet<T> set{};
+        double bytes = 0.0;
+        int b0 = 0;
+        for (int l = 0; l < count; ++l) {
+            const hx_extrusion& e = steps[l];
+            auto& d = set.l[l];
+            d.ring = (T*)e.ring;
+            d.idx = e.stencil_idx;
+            d.A = (const T*)e.A;
+            d.B = (const T*)e.B;
+            d.noise = (const T*)e.noise;
+            d.ny = e.ny;
+            d.nx = e.nx;
+            d.row0 = e.row0;
+            d.col0 = e.col0;
+            d.where = e.where;
+            d.nst = e.nst;
+            d.nb = e.nb;
+            d.nslice = e.where <= 1 ? e.nx : e.ny;
+            d.block0 = b0;
+            b0 += hx::ceil_div(d.nslice, XRC) * split;
+            bytes += (double)esz * ((double)d.nslice * (e.nst + e.nb) + d.nslice) + (esz + 8.0) * e.nst + esz * e.nb;
+        }
+        set.count = count;
+        hx::TraceScope trace(HX_TRACE_ATMOSPHERE, bytes, st);
+        if (cl) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3((unsigned)b0, 1, 1);
+            cfg.blockDim = dim3(XTHREADS);
+            cfg.stream = st;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = XS;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            HX_TRY(hx::cuda_status(cudaLaunchKernelEx(&cfg, extrude_layers_kernel<T, XS>, set),
+                                   "extrude_layers_kernel"));
+        } else {
+            extrude_layers_kernel<T, 1><<<(unsigned)b0, XTHREADS, 0, st>>>(set);
+        }
+        return hx::launch_status("extrude_layers_kernel");
+    };
+    return dtype == HX_F32 ? run((float*)nullptr) : run((double*)nullptr);
 }
 
-int hx_atmosphere_shift(const void* ring, int ny, int nx, int row0, int col0, const double* taps_row,
-                        const double* taps_col, void* out, int dtype, void* stream) {
-    HX_CHECK_ARG(ring && taps_row && taps_col && out, "hx_atmosphere_shift: NULL pointer");
-    HX_CHECK_ARG(ny > 0 && nx > 0, "hx_atmosphere_shift: sizes must be positive");
-    HX_CHECK_ARG(row0 >= 0 && row0 < ny && col0 >= 0 && col0 < nx, "hx_atmosphere_shift: ring offsets out of range");
+int hx_atmosphere_extrude(void* ring, int ny, int nx, int row0, int col0, int where, const long long* stencil_idx,
+                          int nst, const void* A, const void* B, int nb, const void* noise, int dtype, void* stream) {
+    hx_extrusion e{ring, stencil_idx, A, B, noise, ny, nx, row0, col0, where, nst, nb};
+    return hx_atmosphere_extrude_layers(&e, 1, dtype, stream);
+}
+
+int hx_atmosphere_shift_layers(const void* const* rings, int count, int ring_ny, int ring_nx, int ny, int nx,
+                               const int* row0, const int* col0, const double* taps_row, const double* taps_col,
+                               void* const* outs, void* sum, int dtype, void* stream) {
+    HX_CHECK_ARG(rings && row0 && col0 && taps_row && taps_col, "hx_atmosphere_shift: NULL pointer");
+    HX_CHECK_ARG(count >= 1 && count <= SL_MAX, "hx_atmosphere_shift_layers: count must be 1..%d (got %d)", SL_MAX,
+                 count);
+    HX_CHECK_ARG(ny > 0 && nx > 0 && ring_ny >= ny && ring_nx >= nx,
+                 "hx_atmosphere_shift: sizes must be positive and the ring at least ny x nx");
     HX_CHECK_ARG(dtype == HX_F32 || dtype == HX_F64, "hx_atmosphere_shift: dtype must be HX_F32 or HX_F64");
-    if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
-    Taps t;
-    for (int k = 0; k < 7; ++k) {
-        t.row[k] = taps_row[k];
-        t.col[k] = taps_col[k];
+    bool any_out = sum != nullptr;
+    for (int l = 0; l < count; ++l) {
+        HX_CHECK_ARG(rings[l], "hx_atmosphere_shift: NULL ring %d", l);
+        HX_CHECK_ARG(row0[l] >= 0 && row0[l] < ring_ny && col0[l] >= 0 && col0[l] < ring_nx,
+                     "hx_atmosphere_shift: ring offsets out of range");
+        any_out = any_out || (outs && outs[l]);
     }
+    HX_CHECK_ARG(any_out, "hx_atmosphere_shift_layers: no output");
+    if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
     dim3 grid(hx::ceil_div(nx, TS), hx::ceil_div(ny, TS));
     dim3 block(32, 8);
     cudaStream_t st = (cudaStream_t)stream;
-    hx::TraceScope trace(HX_TRACE_ATMOSPHERE, 2.0 * (dtype == HX_F32 ? 4 : 8) * (double)nx * ny, st);
-    if (dtype == HX_F32)
-        ring_shift_kernel<float><<<grid, block, 0, st>>>((const float*)ring, ny, nx, row0, col0, t, (float*)out);
-    else
-        ring_shift_kernel<double><<<grid, block, 0, st>>>((const double*)ring, ny, nx, row0, col0, t, (double*)out);
-    return hx::launch_status("ring_shift_kernel");
+    int nout = sum != nullptr;
+    for (int l = 0; l < count; ++l) nout += outs && outs[l];
+    hx::TraceScope trace(HX_TRACE_ATMOSPHERE, (double)(count + nout) * (dtype == HX_F32 ? 4 : 8) * nx * ny, st);
+    auto fill = [&](auto& set) {
+        using T = std::remove_pointer_t<decltype(set.sum)>;
+        for (int l = 0; l < count; ++l) {
+            set.ring[l] = (const T*)rings[l];
+            set.out[l] = outs ? (T*)outs[l] : nullptr;
+            set.row0[l] = row0[l];
+            set.col0[l] = col0[l];
+            for (int k = 0; k < 7; ++k) {  // float taps round to nearest, as a device conversion would
+                set.taps_row[l][k] = (T)taps_row[7 * l + k];
+                set.taps_col[l][k] = (T)taps_col[7 * l + k];
+            }
+        }
+        set.sum = (T*)sum;
+        set.count = count;
+        set.ring_ny = ring_ny;
+        set.ring_nx = ring_nx;
+        set.ny = ny;
+        set.nx = nx;
+    };
+    if (dtype == HX_F32) {
+        ShiftSet<float> set{};
+        fill(set);
+        shift_layers_kernel<float><<<grid, block, 0, st>>>(set);
+    } else {
+        ShiftSet<double> set{};
+        fill(set);
+        shift_layers_kernel<double><<<grid, block, 0, st>>>(set);
+    }
+    return hx::launch_status("shift_layers_kernel");
+}
+
+int hx_atmosphere_shift(const void* ring, int ring_ny, int ring_nx, int ny, int nx, int row0, int col0,
+                        const double* taps_row, const double* taps_col, void* out, int dtype, void* stream) {
+    HX_CHECK_ARG(ring && out, "hx_atmosphere_shift: NULL pointer");
+    void* outs[1] = {out};
+    return hx_atmosphere_shift_layers(&ring, 1, ring_ny, ring_nx, ny, nx, &row0, &col0, taps_row, taps_col, outs,
+                                      nullptr, dtype, stream);
 }
 
 int hx_atmosphere_combine(const void* const* screens, int count, long long n, void* out, int dtype, void* stream) {

@@ -11,7 +11,8 @@ device.
 import numpy as np
 import torch
 
-from .field import Field
+from . import _lib
+from .field import Field, as_tensor as _to_device
 
 _DEVICE = 'cuda'
 
@@ -196,17 +197,33 @@ def poke_jacobian(measure, dark_zone, num_modes, epsilon, num_amplitudes=2, batc
 
 
 def efc_step(efc_matrix, field, dark_zone, actuators, gain):
-    """One EFC update (the tutorial's loop body): x = [Re E_dz, Im E_dz], actuators - gain * (efc_matrix . x)."""
+    """One EFC update (the tutorial's loop body): x = [Re E_dz, Im E_dz], actuators - gain * (efc_matrix . x).
+
+    One launch of ``hx_efc_step`` (the dark-zone gather, the matrix product and the update, float-float
+    arithmetic); the EFC matrix (from ``inverse_tikhonov`` and friends, computed once per Jacobian) stays on the
+    device in float64."""
     dz = _mask(dark_zone)
     e = field.data if isinstance(field, Field) else field
     e = torch.as_tensor(e).reshape(-1)
     _check_pixels(e.numel(), int(dz.numel()))
-    e = e.to(_DEVICE).index_select(0, _dark_zone_index(dz)).to(torch.complex128)
-    x = torch.cat((e.real, e.imag))
+    e = _to_device(e)
+    if e.dtype not in (torch.complex64, torch.complex128):
+        e = e.to(torch.complex128)
+    e = e.contiguous()
+    idx = _dark_zone_index(dz).to(torch.int32).contiguous()
     m, _ = _device_matrix(efc_matrix)
+    m = m.to(torch.float64).contiguous()
+    if m.shape[1] != 2 * idx.numel():
+        raise ValueError('The EFC matrix has %d columns; the dark zone needs %d.' % (m.shape[1], 2 * idx.numel()))
     a = torch.as_tensor(actuators.data if isinstance(actuators, Field) else actuators)
-    a = a.to(device=_DEVICE, dtype=torch.float64)
-    return a - float(gain) * (m @ x)
+    a = a.to(device=_DEVICE, dtype=torch.float64).contiguous()
+    if a.numel() != m.shape[0]:
+        raise ValueError('%d actuators for an EFC matrix of %d rows.' % (a.numel(), m.shape[0]))
+    out = torch.empty_like(a)
+    rc = _lib.lib().hx_efc_step(_lib.dptr(m), int(m.shape[0]), int(idx.numel()), _lib.dptr(e), _lib.dtype_code(e.dtype),
+                                _lib.dptr(idx), _lib.dptr(a), float(gain), _lib.dptr(out), _lib.stream_handle())
+    _lib.check(rc, 'hx_efc_step')
+    return out
 
 
 def run_efc(measure, dark_zone, efc_matrix, actuators, iterations, gain=0.5):

@@ -85,6 +85,10 @@ class SparseBasis(object):
         self.col_ptr = torch.from_numpy(csc.indptr.astype(np.int32)).to(device)
         self.row_idx = torch.from_numpy(csc.indices.astype(np.int32)).to(device)
         self.vals_csc = torch.from_numpy(csc.data).to(device=device, dtype=dtype)
+        blk_ptr, blk_pix, blk_vals = _actuator_blocks(csc, BLOCK_ACTUATORS)
+        self.blk_ptr = torch.from_numpy(blk_ptr).to(device)
+        self.blk_pix = torch.from_numpy(blk_pix).to(device)
+        self.blk_vals = torch.from_numpy(blk_vals).to(device=device, dtype=dtype)
 
     def apply(self, coeffs):
         """surface[v, p] = sum_a M[p, a] coeffs[v, a] for coeffs of shape (..., nact)."""
@@ -108,12 +112,39 @@ class SparseBasis(object):
         out = torch.empty(lead + (nact,), dtype=self.dtype, device=self.vals.device)
         if out.numel() == 0:
             return out
-        rc = _lib.lib().hx_influence_apply_transpose(npix, nact, _lib.dptr(self.col_ptr), _lib.dptr(self.row_idx),
-                                                     _lib.dptr(self.vals_csc), _lib.dtype_code(self.dtype),
-                                                     g2.shape[0], _lib.dptr(g2), _lib.dptr(out),
-                                                     _lib.stream_handle())
-        _lib.check(rc, 'hx_influence_apply_transpose')
+        rc = _lib.lib().hx_influence_apply_transpose_blocked(npix, nact, _lib.dptr(self.blk_ptr),
+                                                             _lib.dptr(self.blk_pix), _lib.dptr(self.blk_vals),
+                                                             _lib.dtype_code(self.dtype), g2.shape[0], _lib.dptr(g2),
+                                                             _lib.dptr(out), _lib.stream_handle())
+        _lib.check(rc, 'hx_influence_apply_transpose_blocked')
         return out
+
+
+BLOCK_ACTUATORS = 4  # actuators per block of the blocked transpose (kBA in csrc/influence.cu)
+
+
+def _actuator_blocks(csc, block):
+    """Union pixel lists of blocks of ``block`` consecutive actuators, from the CSC form: (block pointers
+    (nblk + 1), pixel indices (sorted within a block), weights (n x block, zero where an actuator of the block does
+    not reach the pixel))."""
+    npix, nact = csc.shape
+    nblk = -(-nact // block)
+    ptr = np.zeros(nblk + 1, np.int32)
+    pix, vals = [], []
+    for b in range(nblk):
+        a0, a1 = b * block, min(nact, (b + 1) * block)
+        rows = csc.indices[csc.indptr[a0]:csc.indptr[a1]]
+        u = np.unique(rows)
+        w = np.zeros((u.size, block), csc.data.dtype)
+        for a in range(a0, a1):
+            r = csc.indices[csc.indptr[a]:csc.indptr[a + 1]]
+            w[np.searchsorted(u, r), a - a0] = csc.data[csc.indptr[a]:csc.indptr[a + 1]]
+        pix.append(u.astype(np.int32))
+        vals.append(w)
+        ptr[b + 1] = ptr[b] + u.size
+    pix = np.concatenate(pix) if pix else np.zeros(0, np.int32)
+    vals = np.concatenate(vals) if vals else np.zeros((0, block))
+    return ptr, pix, np.ascontiguousarray(vals).reshape(-1)
 
 
 def _weights(w, n, device):

@@ -330,6 +330,13 @@ HX_API int hx_influence_apply(int npix, int nact, const int* row_ptr, const int*
 HX_API int hx_influence_apply_transpose(int npix, int nact, const int* col_ptr, const int* row_idx,
                                         const void* vals, int dtype, int nvec, const void* g_surface,
                                         void* g_actuators, void* stream);
+/* The same transpose from blocks of 4 consecutive actuators: block b (actuators 4b .. 4b+3) lists the union of
+ * their pixels, blk_pix[blk_ptr[b] .. blk_ptr[b + 1]), with 4 weights per listed pixel in blk_vals (row-major,
+ * 16-byte aligned, zero where an actuator of the block does not reach the pixel), so a gradient value gathered
+ * once serves the block's actuators that overlap there. */
+HX_API int hx_influence_apply_transpose_blocked(int npix, int nact, const int* blk_ptr, const int* blk_pix,
+                                                const void* blk_vals, int dtype, int nvec, const void* g_surface,
+                                                void* g_actuators, void* stream);
 
 /* Phase screen: out[b, p] = e[b % batch_e, p] exp(i scale s[b % batch_s, p]) for b < batch (batch_e and
  * batch_s are 1 or batch).  e/out are HX_C64 or HX_C128 (dtype), s the matching real type.  Replaces the
@@ -345,28 +352,62 @@ HX_API int hx_phase_apply_grad(long long n, int batch, int batch_e, int batch_s,
 
 /* ------------------------------------------------------------------------
  * Infinite atmospheric layer (hcipy/atmosphere/infinite_atmospheric_layer.py:216-364).
- * The ny x nx achromatic screen is a ring buffer: logical pixel (i, j) is stored at
- * ((i + row0) % ny, (j + col0) % nx).  One extrusion (InfiniteAtmosphericLayer._extrude, :216-259):
+ * The ny x nx achromatic screen is a ring buffer of (ny + 1) x (nx + 1) values: logical pixel (i, j) is stored
+ * at ((i + row0) % (ny + 1), (j + col0) % (nx + 1)), row0 in [0, ny], col0 in [0, nx]; the spare row and
+ * column are outside the logical screen.  One extrusion (InfiniteAtmosphericLayer._extrude, :216-259):
  * where = 0 bottom, 1 top, 2 left, 3 right; stencil_idx (device, nst int64 in [0, ny*nx)) indexes the
  * logical flat screen (flipped for top/right as in the reference); A (nslice x nst), B (nslice x nb) and
- * noise (nb) are HX_F32 or HX_F64 device arrays; work holds nst values.  The caller passes the offsets
- * before the step and then moves them: bottom row0 -= 1, top row0 += 1, left col0 -= 1, right col0 += 1
- * (mod ny / nx).
+ * noise (nb) are HX_F32 or HX_F64 device arrays, nslice = nx for bottom/top and ny for left/right.  The new
+ * slice is written into the spare slice; the caller passes the offsets before the step and then moves them:
+ * bottom row0 -= 1, top row0 += 1, left col0 -= 1, right col0 += 1 (mod ny + 1 / nx + 1).
  * ------------------------------------------------------------------------ */
+typedef struct hx_extrusion {
+    void* ring;
+    const long long* stencil_idx;
+    const void* A;
+    const void* B;
+    const void* noise;
+    int ny, nx, row0, col0, where, nst, nb;
+} hx_extrusion;
 HX_API int hx_atmosphere_extrude(void* ring, int ny, int nx, int row0, int col0, int where,
                                  const long long* stencil_idx, int nst, const void* A, const void* B, int nb,
-                                 const void* noise, int dtype, void* work, void* stream);
-/* Sub-pixel shift of the logical screen into out (ny x nx): the separable 7-tap filter taps_row along x
- * then taps_col along y, clamp to edge (quintic weights of subpixel_shift, hcipy/_math/subpixel_shift.py:7-343;
- * taps are host arrays of 7 float64). */
-HX_API int hx_atmosphere_shift(const void* ring, int ny, int nx, int row0, int col0, const double* taps_row,
-                               const double* taps_col, void* out, int dtype, void* stream);
+                                 const void* noise, int dtype, void* stream);
+/* One extrusion of each of count (0..8) layers in one launch (the step k of every layer of a
+ * MultiLayerAtmosphere frame that moves k or more pixels, :216-259 per layer); steps is a host array, each ring
+ * at most once. */
+HX_API int hx_atmosphere_extrude_layers(const hx_extrusion* steps, int count, int dtype, void* stream);
+/* Sub-pixel shift of the logical ny x nx screen of a ring_ny x ring_nx ring (a plain image: ring_ny = ny,
+ * ring_nx = nx, offsets 0) into out (ny x nx): the separable 7-tap filter taps_row along x then taps_col along
+ * y, clamp to edge (quintic weights of subpixel_shift, hcipy/_math/subpixel_shift.py:7-343; taps are host
+ * arrays of 7 float64). */
+HX_API int hx_atmosphere_shift(const void* ring, int ring_ny, int ring_nx, int ny, int nx, int row0, int col0,
+                               const double* taps_row, const double* taps_col, void* out, int dtype, void* stream);
+/* The shifts of count (1..8) layers' rings in one pass (host arrays: rings, row0, col0, taps count x 7):
+ * layer l's screen into outs[l] (outs or an entry may be NULL) and the sum of the shifted screens, in layer
+ * order, into sum (may be NULL): the evolved screens of MultiLayerAtmosphere and the summed screen its
+ * forward applies (hcipy/atmosphere/atmospheric_model.py:264-280). */
+HX_API int hx_atmosphere_shift_layers(const void* const* rings, int count, int ring_ny, int ring_nx, int ny, int nx,
+                                      const int* row0, const int* col0, const double* taps_row,
+                                      const double* taps_col, void* const* outs, void* sum, int dtype,
+                                      void* stream);
 /* out (n) = the sum of count (1..8) screens of n HX_F32 or HX_F64 values; screens is a host array of device
  * pointers.  The phase of layers applied in sequence without propagation between them
  * (MultiLayerAtmosphere.forward with scintillation off, hcipy/atmosphere/atmospheric_model.py:264-280) is the
  * phase of this sum, so one phase application replaces one per layer. */
 HX_API int hx_atmosphere_combine(const void* const* screens, int count, long long n, void* out, int dtype,
                                  void* stream);
+
+/* ------------------------------------------------------------------------
+ * Electric-field conjugation: one step of the loop of the reference's EFC tutorial
+ * (doc/tutorial_notebooks/ElectricFieldConjugation, the update after the Tikhonov inverse of
+ * hcipy/util/matrix_inversion.py:71-100): x = [Re E[dz], Im E[dz]], actuators_out = actuators - gain M . x,
+ * with M the nact x 2 n_dz float64 EFC matrix (row-major), E the focal-plane field (HX_C64 or HX_C128),
+ * dz_index the n_dz dark-zone pixel indices (int32, device).  One launch (gather, product, update), float-float
+ * arithmetic with a fixed reduction order.  actuators_out may equal actuators.
+ * ------------------------------------------------------------------------ */
+HX_API int hx_efc_step(const double* efc_matrix, int nact, int n_dz, const void* field, int dtype,
+                       const int* dz_index, const double* actuators, double gain, double* actuators_out,
+                       void* stream);
 
 #ifdef __cplusplus
 }

@@ -76,7 +76,9 @@ def test_layer_extrudes_all_four_directions_like_the_oracle():
     _use_reference_matrices(layer, g)
     rng = np.random.default_rng(9)
     screen = g['screen0'].copy()
-    for where in ['right', 'top', 'left', 'bottom', 'top', 'right', 'right', 'bottom']:
+    # the ring has a spare row and column: runs of 30 steps wrap both offsets past the ends
+    for where in ['right', 'top', 'left', 'bottom', 'top', 'right', 'right', 'bottom'] + ['left'] * 30 + \
+            ['top'] * 30 + ['right'] * 3 + ['bottom'] * 31:
         vertical = where in ('top', 'bottom')
         a = g['A_vertical'] if vertical else g['A_horizontal']
         b = g['B_vertical'] if vertical else g['B_horizontal']
@@ -270,3 +272,50 @@ def test_seeded_layer_starts_from_the_reference_screen_and_stream():
         assert rel_err(layer.phase_for(1.0).numpy(), g['shifted_%d' % i]) < 1e-10, i
     layer.reset()
     assert rel_err(layer.achromatic_screen.numpy(), g['screen0']) < 1e-10
+
+
+@pytest.mark.parametrize('dtype', [torch.float64, torch.float32])
+def test_multilayer_batched_frames_equal_layer_by_layer(dtype):
+    """MultiLayerAtmosphere.evolve_until runs a frame as one extrusion launch per step index over all layers and
+    one shift-and-sum pass; the same layers evolved one by one (one extrusion launch per step, one shift each,
+    then the summed screen) must give the same screens and the same sum bit for bit, with layers that move 0, 1
+    or several pixels a frame, in all four directions, past the ends of the ring."""
+    grid = hg.make_pupil_grid(40, 2.0)
+    winds = ((10.0, 0.0), (-7.5, 13.0), (0.0, 0.0), (-31.0, -22.0))
+
+    def make():
+        return [hg.InfiniteAtmosphericLayer(grid, hg.Cn_squared_from_fried_parameter(0.15, 500e-9), L0=20,
+                                            velocity=v, seed=11 + i, dtype=dtype) for i, v in enumerate(winds)]
+    batched, single = make(), make()
+    atm = hg.MultiLayerAtmosphere(batched)
+    launches = []
+    t = 0.0
+    for frame in range(40):
+        t += 0.011
+        before = hg.launch_count()
+        atm.evolve_until(t)
+        mid = hg.launch_count()
+        for layer in single:
+            layer.evolve_until(t)
+        launches.append((mid - before, hg.launch_count() - mid))
+        for a, b in zip(batched, single):
+            assert a._row0 == b._row0 and a._col0 == b._col0
+            assert torch.equal(a._shifted, b._shifted), frame
+        expect = single[0]._shifted + single[1]._shifted + single[2]._shifted + single[3]._shifted
+        assert torch.equal(atm.combined_screen().reshape(expect.shape), expect), frame
+    # one launch per step of the fastest layer and one shift pass, against one launch per step and per layer
+    assert sum(b for b, _ in launches) < 0.7 * sum(s for _, s in launches), launches
+    assert all(np.array_equal(a.achromatic_screen.numpy(), b.achromatic_screen.numpy())
+               for a, b in zip(batched, single))
+
+
+def test_extrude_layers_rejects_a_ring_twice():
+    from hcipy_gb300 import _lib
+    grid = hg.make_pupil_grid(16, 1.0)
+    layer = hg.InfiniteAtmosphericLayer(grid, 1e-14, L0=20, seed=3)
+    noise = torch.zeros(64, dtype=torch.float64, device='cuda')
+    e = layer._extrusion('right', noise)
+    steps = (_lib.Extrusion * 2)(e, e)
+    rc = _lib.lib().hx_atmosphere_extrude_layers(steps, 2, _lib.HX_F64, _lib.stream_handle())
+    assert rc == _lib.HX_ERR_INVALID and b'twice' in _lib.lib().hx_last_error()
+    assert _lib.lib().hx_atmosphere_extrude_layers(steps, 0, _lib.HX_F64, _lib.stream_handle()) == _lib.HX_OK

@@ -258,3 +258,53 @@ def test_batch_of_one_keeps_its_dimension():
     dm.actuators = cmd[0]
     single = dm.forward(hg.Wavefront(hg.Field(e, pupil), 1.0)).electric_field.data
     assert single.shape == (pupil.size,) and torch.equal(single, out[0])
+
+
+@pytest.mark.parametrize('dtype,tol', [(torch.float64, 1e-12), (torch.float32, 2e-6)])
+def test_sparse_basis_staged_and_blocked_paths(dtype, tol):
+    """The surface kernel stages each CTA's actuator range of the commands in shared memory and the transpose
+    walks blocks of 4 actuators: against float64 dense products for 37 vectors (ragged against the 16 / 8
+    vectors a CTA takes), 1001 actuators (a ragged last block), a banded basis (staged) and one whose rows
+    reach across all actuators (too wide to stage: the global path).  The CSC transpose gives the same result,
+    and the surface is right for unsorted CSR columns at the C ABI."""
+    import scipy.sparse as sp
+    from hcipy_gb300 import _lib
+    from hcipy_gb300.kernels import SparseBasis
+    rng = np.random.default_rng(4)
+    npix, nact, nvec = 3000, 1001, 37
+    rows, cols = [], []
+    for p in range(npix):  # banded: pixel p touches actuators near p / 3
+        c = np.unique(np.clip(p // 3 + rng.integers(-20, 21, 12), 0, nact - 1))
+        rows += [p] * c.size
+        cols += list(c)
+    banded = sp.csr_matrix((rng.standard_normal(len(rows)), (rows, cols)), shape=(npix, nact))
+    wide = sp.random(npix, nact, density=0.02, random_state=5, format='csr')
+    for m in (banded, wide):
+        basis = SparseBasis(m, torch.device('cuda'), dtype)
+        a = rng.standard_normal((nvec, nact))
+        s = basis.apply(torch.from_numpy(a)).double().cpu().numpy()
+        ref = a @ m.T.toarray()
+        assert rel_err(s, ref) < tol
+        w = rng.standard_normal((nvec, npix))
+        gt = basis.apply_transpose(torch.from_numpy(w)).double().cpu().numpy()
+        assert rel_err(gt, w @ m.toarray()) < tol
+        g2 = torch.from_numpy(w).to('cuda', dtype)
+        out = torch.empty((nvec, nact), dtype=dtype, device='cuda')
+        rc = _lib.lib().hx_influence_apply_transpose(npix, nact, _lib.dptr(basis.col_ptr), _lib.dptr(basis.row_idx),
+                                                     _lib.dptr(basis.vals_csc), _lib.dtype_code(dtype), nvec,
+                                                     _lib.dptr(g2), _lib.dptr(out), _lib.stream_handle())
+        _lib.check(rc)
+        assert rel_err(out.double().cpu().numpy(), gt) < tol
+    # unsorted columns within each CSR row
+    m = banded.copy()
+    perm = np.concatenate([rng.permutation(np.arange(m.indptr[p], m.indptr[p + 1])) for p in range(npix)])
+    idx = torch.from_numpy(m.indices[perm].astype(np.int32)).cuda()
+    val = torch.from_numpy(m.data[perm]).to('cuda', dtype)
+    ptr = torch.from_numpy(m.indptr.astype(np.int32)).cuda()
+    a = rng.standard_normal((nvec, nact))
+    a_dev = torch.from_numpy(a).to('cuda', dtype)
+    out = torch.empty((nvec, npix), dtype=dtype, device='cuda')
+    _lib.check(_lib.lib().hx_influence_apply(npix, nact, _lib.dptr(ptr), _lib.dptr(idx), _lib.dptr(val),
+                                             _lib.dtype_code(dtype), nvec, _lib.dptr(a_dev), _lib.dptr(out),
+                                             _lib.stream_handle()))
+    assert rel_err(out.double().cpu().numpy(), a @ m.T.toarray()) < tol
