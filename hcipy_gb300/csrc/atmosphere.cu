@@ -139,13 +139,11 @@ __global__ void __launch_bounds__(XTHREADS, (sizeof(T) == 4 && SPLIT > 1) ? 6 : 
     T acc[XRW];
 #pragma unroll
     for (int r = 0; r < XRW; ++r) acc[r] = T(0);
-    // B . noise over this CTA's noise columns (independent of the stencil: its loads go out first)
-    {
-        const int b0 = slice_bound(L.nb, rank, SPLIT), b1 = slice_bound(L.nb, rank + 1, SPLIT);
-        if (nr > 0 && b1 > b0) dot_rows(acc, L.B + (long long)rw * L.nb + b0, L.nb, nr, L.noise + b0, b1 - b0, lane);
-    }
-    // A . stencil over this CTA's stencil columns, gathered through the ring in chunks
     const int s0 = slice_bound(L.nst, rank, SPLIT), s1 = slice_bound(L.nst, rank + 1, SPLIT);
+    const int b0 = slice_bound(L.nb, rank, SPLIT), b1 = slice_bound(L.nb, rank + 1, SPLIT);
+    // B . noise over this CTA's noise columns (independent of the stencil)
+    if (nr > 0 && b1 > b0) dot_rows(acc, L.B + (long long)rw * L.nb + b0, L.nb, nr, L.noise + b0, b1 - b0, lane);
+    // A . stencil over this CTA's stencil columns, gathered through the ring in chunks
     for (int c0 = s0; c0 < s1; c0 += XCHUNK) {
         const int clen = min(XCHUNK, s1 - c0);
         if (c0 > s0) __syncthreads();  // the previous chunk is consumed

@@ -124,6 +124,62 @@ __global__ void slice_rows_kernel(FieldIO src, long long ld, int K, int Kp, cons
     }
 }
 
+// slice_rows_kernel<1> for a row whose maximum is not known yet and that fits in registers (Kp <= 1024 G): the
+// CTA reads the row once into registers (G groups of four consecutive points per thread), takes its maximum and
+// slices from the registers, where slice_rows_kernel reads the row twice.  Same slices, same scales.
+template <int G>
+__global__ void __launch_bounds__(256) slice_rows_reg_kernel(FieldIO src, long long ld, int K, int Kp, __half* planes,
+                                                             long long plane_stride, int kpitch, float* scale_out) {
+    const long long m = blockIdx.x;
+    __shared__ float red[8];
+    __shared__ float s_scale;
+    cff v[G][4];
+    float mx = 0.0f;
+#pragma unroll
+    for (int gi = 0; gi < G; ++gi) {
+        const int k0 = 4 * ((int)threadIdx.x + gi * 256);
+        if (k0 + 4 <= K) {
+            load4_field(src, m * ld + k0, v[gi]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) v[gi][j] = k0 + j < K ? load_field(src, m * ld + k0 + j) : cff{};
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mx = fmaxf(mx, fmaxf(fabsf(v[gi][j].re.hi), fabsf(v[gi][j].im.hi)));
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < 8; ++i) mx = fmaxf(mx, red[i]);
+        s_scale = pow2_above(mx);
+        scale_out[m] = s_scale;
+    }
+    __syncthreads();
+    const float inv = 1.0f / s_scale;
+#pragma unroll
+    for (int gi = 0; gi < G; ++gi) {
+        const int k0 = 4 * ((int)threadIdx.x + gi * 256);
+        if (k0 >= Kp) continue;
+        __half rs[3][4], is[3][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            slice3(v[gi][j].re, inv, rs[0][j], rs[1][j], rs[2][j]);
+            slice3(v[gi][j].im, inv, is[0][j], is[1][j], is[2][j]);
+        }
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+            __half* pl = planes + p * plane_stride + m * kpitch;
+            __half2 re01 = __halves2half2(rs[p][0], rs[p][1]), re23 = __halves2half2(rs[p][2], rs[p][3]);
+            __half2 im01 = __halves2half2(is[p][0], is[p][1]), im23 = __halves2half2(is[p][2], is[p][3]);
+            *reinterpret_cast<uint2*>(pl + k0) =
+                make_uint2(*reinterpret_cast<uint32_t*>(&re01), *reinterpret_cast<uint32_t*>(&re23));
+            *reinterpret_cast<uint2*>(pl + Kp + k0) =
+                make_uint2(*reinterpret_cast<uint32_t*>(&im01), *reinterpret_cast<uint32_t*>(&im23));
+        }
+    }
+}
+
 // Column maxima max(|Re|, |Im|) of per-field K x N matrices (fields along grid z), as float bits.
 __global__ void colmax_kernel(FieldIO src, int K, int N, long long field_stride, unsigned int* colmax,
                               long long colmax_stride) {
@@ -280,6 +336,80 @@ __global__ void babinet_rows_kernel(FieldIO t, FieldIO src, const float2* __rest
     }
 }
 
+// The same row pass when the Lyot plane only feeds the image transform: the CTA keeps its row in registers (G
+// groups of four consecutive points per thread, Kp <= 1024 G), takes the row maximum, and writes the three fp16
+// slice planes of the row ([Re | Im], zero-padded to Kp) and its scale straight into the image transform's first
+// GEMM operand.  The slices are those slice_rows_kernel<1> makes from the float-float row with that maximum, so
+// the result is unchanged; the float-float Lyot plane is neither written nor read back.
+template <int SRC, int G>
+__global__ void __launch_bounds__(256) babinet_slice_rows_kernel(FieldIO t, FieldIO src, const float2* __restrict__ stop,
+                                                                 cff alpha, int ny, int nx, int Kp, __half* planes,
+                                                                 long long plane_stride, int kpitch, float* scale_out) {
+    const long long row = blockIdx.x;
+    const long long base = row * nx;
+    const float2* srow = stop ? stop + (row % ny) * nx : nullptr;
+    const bool real_alpha = alpha.im.hi == 0.0f && alpha.im.lo == 0.0f;
+    const bool imag_alpha = alpha.re.hi == 0.0f && alpha.re.lo == 0.0f;
+    __shared__ float red[8];
+    __shared__ float s_scale;
+    cff w[G][4];
+    float mx = 0.0f;
+#pragma unroll
+    for (int gi = 0; gi < G; ++gi) {
+        const int k0 = 4 * ((int)threadIdx.x + gi * 256);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int c = k0 + j;
+            cff x = {};
+            if (c < nx) {
+                const cff v = load_fmt<FMT_FF>(t, base + c);
+                const cff e = load_fmt<SRC>(src, base + c);
+                x = real_alpha   ? cff{ff_mul(v.re, alpha.re), ff_mul(v.im, alpha.re)}
+                    : imag_alpha ? cff{ff_neg(ff_mul(v.im, alpha.im)), ff_mul(v.re, alpha.im)}
+                                 : cff_mul(v, alpha);
+                x = {ff_add(e.re, ff_neg(x.re)), ff_add(e.im, ff_neg(x.im))};
+                if (srow) {
+                    const float2 mk = __ldg(&srow[c]);
+                    x = mk.y == 0.0f ? cff{ff_mulf(x.re, mk.x), ff_mulf(x.im, mk.x)} : cff_mul_c64(x, mk);
+                }
+                mx = fmaxf(mx, fmaxf(fabsf(x.re.hi), fabsf(x.im.hi)));
+            }
+            w[gi][j] = x;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < 8; ++i) mx = fmaxf(mx, red[i]);
+        s_scale = pow2_above(mx);
+        scale_out[row] = s_scale;
+    }
+    __syncthreads();
+    const float inv = 1.0f / s_scale;
+#pragma unroll
+    for (int gi = 0; gi < G; ++gi) {
+        const int k0 = 4 * ((int)threadIdx.x + gi * 256);
+        if (k0 >= Kp) continue;
+        __half rs[3][4], is[3][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            slice3(w[gi][j].re, inv, rs[0][j], rs[1][j], rs[2][j]);
+            slice3(w[gi][j].im, inv, is[0][j], is[1][j], is[2][j]);
+        }
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+            __half* pl = planes + p * plane_stride + row * kpitch;
+            __half2 re01 = __halves2half2(rs[p][0], rs[p][1]), re23 = __halves2half2(rs[p][2], rs[p][3]);
+            __half2 im01 = __halves2half2(is[p][0], is[p][1]), im23 = __halves2half2(is[p][2], is[p][3]);
+            *reinterpret_cast<uint2*>(pl + k0) =
+                make_uint2(*reinterpret_cast<uint32_t*>(&re01), *reinterpret_cast<uint32_t*>(&re23));
+            *reinterpret_cast<uint2*>(pl + Kp + k0) =
+                make_uint2(*reinterpret_cast<uint32_t*>(&im01), *reinterpret_cast<uint32_t*>(&im23));
+        }
+    }
+}
+
 template <int SRC>
 int launch_babinet_src(FieldIO t, FieldIO src, const float2* stop, cff alpha, long long rows, int ny, int nx,
                        FieldIO out, int out_fmt, unsigned int* rowmax, cudaStream_t st) {
@@ -377,6 +507,17 @@ FieldIO carve_ff(Carver& c, long long n) {
 int launch_slice_rows(const FieldIO& src, long long ld, long long M, int K, const unsigned int* rowmax,
                       SliceMat& s, cudaStream_t st, bool emb = false) {
     if (M > 2147483647LL) return HX_ERR_UNSUPPORTED;
+    if (emb && !rowmax && s.Kp <= 4096) {
+        const unsigned grid = (unsigned)M;
+        const long long ps = s.plane_stride();
+        switch ((s.Kp + 1023) / 1024) {
+            case 1: slice_rows_reg_kernel<1><<<grid, 256, 0, st>>>(src, ld, K, s.Kp, s.planes, ps, s.kpitch, s.scale); break;
+            case 2: slice_rows_reg_kernel<2><<<grid, 256, 0, st>>>(src, ld, K, s.Kp, s.planes, ps, s.kpitch, s.scale); break;
+            case 3: slice_rows_reg_kernel<3><<<grid, 256, 0, st>>>(src, ld, K, s.Kp, s.planes, ps, s.kpitch, s.scale); break;
+            default: slice_rows_reg_kernel<4><<<grid, 256, 0, st>>>(src, ld, K, s.Kp, s.planes, ps, s.kpitch, s.scale);
+        }
+        return launch_status("slice_rows_reg_kernel");
+    }
     if (emb)
         slice_rows_kernel<1><<<(unsigned)M, 256, 0, st>>>(src, ld, K, s.Kp, rowmax, s.planes, s.plane_stride(),
                                                           s.kpitch, s.scale);
@@ -772,12 +913,24 @@ void carve_ws(Carver& c, const SplitMftPlan* p, int direction, int batch, Ws& w)
     w.counters = (unsigned int*)c.take(sizeof(unsigned int) * tiles);
 }
 
+// The sliced operand of a forward run's first GEMM in workspace ws: the first piece carve_ws takes.
+SliceMat forward_input_slices(const SplitMftPlan* p, int batch, void* ws) {
+    Carver c(ws);
+    SliceMat s;
+    const long long rows = (long long)batch * p->ny;
+    carve_slices(c, s, round_up(rows, BM), p->nx, rows);
+    return s;
+}
+
 // in/out: c64 or float-float fields.  in_max: optional precomputed maxima of the input in the orientation the
 // first GEMM slices it (forward: per stacked row; backward: per field and column, stride nu64).  out_rowmax /
-// out_colmax: optional maxima of the output for a following transform (zeroed by the caller).
+// out_colmax: optional maxima of the output for a following transform (zeroed by the caller).  in_sliced
+// (forward only): the caller has already written the first GEMM's sliced operand into the workspace (the first
+// piece carve_ws takes, see forward_input_slices), and `in` is not read.
 int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO& in, const unsigned int* in_max,
                   const FieldIO& out, double are, double aim, int epilogue, const float2* mask, const FieldIO& src,
-                  unsigned int* out_rowmax, unsigned int* out_colmax, void* ws, cudaStream_t st) {
+                  unsigned int* out_rowmax, unsigned int* out_colmax, void* ws, cudaStream_t st,
+                  bool in_sliced = false) {
     const int nx = p->nx, ny = p->ny, nu = p->nu, nv = p->nv;
     const long long nu64 = round_up(nu, 64);
     const long long rows = (long long)batch * ny;
@@ -788,7 +941,7 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
         HX_TRY(cuda_status(cudaMemsetAsync(w.t_max, 0, sizeof(unsigned int) * batch * nu64, st), "memset"));
         // G1: T = E . M2f, stacked over the batch (embedding on M2f); column maxima of T per field for the next
         // slicing.
-        HX_TRY(launch_slice_rows(in, nx, rows, nx, in_max, w.s1, st, true));
+        if (!in_sliced) HX_TRY(launch_slice_rows(in, nx, rows, nx, in_max, w.s1, st, true));
         GemmArgs g1 = base_args(p->status);
         g1.emb = 1;
         g1.M = (int)rows;
@@ -1000,13 +1153,44 @@ int split_lyot_execute(const SplitMftPlan* fpm, const SplitMftPlan* img, int bat
     const bool direct = lyot_out && !img;
     HX_TRY(split_mft_run(fpm, HX_BACKWARD, batch, ef, ef_colmax, lp, 1.0, 0.0, HX_EPI_NONE, nullptr, none, nullptr,
                          nullptr, inner, st));
+    // With only the image wanted, the row pass slices the Lyot plane for the image transform itself.
+    const long long rows = (long long)batch * fpm->ny;
+    const int kp_img = img ? (int)round_up(fpm->nx, 32) : 0;
+    const bool fused = img && !lyot_out && kp_img <= 4096 && rows <= 2147483647LL;
+    if (fused) {
+        GemmArgs ga;
+        set_alpha(ga, ab_re, ab_im);
+        const cff alpha = {{ga.alpha[0], ga.alpha[1]}, {ga.alpha[2], ga.alpha[3]}};
+        SliceMat s1 = forward_input_slices(img, batch, inner);
+        const int groups = (kp_img + 1023) / 1024;
+        auto run = [&](auto src_tag, auto g_tag) {
+            constexpr int SRC = decltype(src_tag)::value, G = decltype(g_tag)::value;
+            babinet_slice_rows_kernel<SRC, G><<<(unsigned)rows, 256, 0, st>>>(
+                lp, fe, stop, alpha, fpm->ny, fpm->nx, s1.Kp, s1.planes, s1.plane_stride(), s1.kpitch, s1.scale);
+        };
+        using I = std::integral_constant<int, FMT_C128>;
+        using J = std::integral_constant<int, FMT_C64>;
+        using G1 = std::integral_constant<int, 1>;
+        using G2 = std::integral_constant<int, 2>;
+        using G3 = std::integral_constant<int, 3>;
+        using G4 = std::integral_constant<int, 4>;
+        if (e_dtype == HX_C128) {
+            if (groups == 1) run(I(), G1()); else if (groups == 2) run(I(), G2());
+            else if (groups == 3) run(I(), G3()); else run(I(), G4());
+        } else {
+            if (groups == 1) run(J(), G1()); else if (groups == 2) run(J(), G2());
+            else if (groups == 3) run(J(), G3()); else run(J(), G4());
+        }
+        HX_TRY(launch_status("babinet_slice_rows_kernel"));
+        return split_mft_run(img, HX_FORWARD, batch, lp, nullptr, output_field(img_out, img_dtype), ai_re, ai_im,
+                             HX_EPI_NONE, nullptr, none, nullptr, nullptr, inner, st, true);
+    }
     {
         GemmArgs ga;
         set_alpha(ga, ab_re, ab_im);
         const cff alpha = {{ga.alpha[0], ga.alpha[1]}, {ga.alpha[2], ga.alpha[3]}};
         const FieldIO dst = direct ? output_field(lyot_out, lyot_dtype) : lp;
         const int out_fmt = direct ? output_fmt(dst) : FMT_FF;
-        const long long rows = (long long)batch * fpm->ny;
         if (e_dtype == HX_C128)
             HX_TRY(launch_babinet_src<FMT_C128>(lp, fe, stop, alpha, rows, fpm->ny, fpm->nx, dst, out_fmt,
                                                 direct ? nullptr : lp_rowmax, st));

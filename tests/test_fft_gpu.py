@@ -69,6 +69,26 @@ def test_fft_cfg2_size_and_round_trip():
     assert abs(e_out / e_in - 1) < 1e-5
 
 
+@pytest.mark.parametrize('dims,q,shift', [((40, 256), 2, (0.0, 0.0)), ((8, 256), 4, (0.3, -0.2)),
+                                           ((16, 128), 8, (0.0, 0.25)), ((16, 256), 16, (0.0, 0.0)),
+                                           ((12, 1024), 4, (-0.2, 0.1)), ((8, 512), 4, (0.0, 0.0)),
+                                           ((8, 1536), 8 / 3, (0.0, 0.1)), ((8, 384), 8 / 3, (0.0, 0.0)),
+                                           ((8, 768), 8 / 3, (0.2, 0.0)), ((8, 200), 10.24, (0.0, -0.3)),
+                                           ((8, 500), 8.192, (0.0, 0.0))])
+def test_fft_zero_padded_power_of_two_columns(dims, q, shift):
+    """complex64 transforms zero-padded along y to a power of two of 512-4096 points (the register-resident line
+    kernel on strided columns) with 1/2 to 1/16 of each column valid, shifted grids, forward and backward, against
+    the float64 oracle."""
+    rng = np.random.default_rng(dims[1] + int(10 * q))
+    pupil = hg.make_pupil_grid(dims, (1.0, 2.0))
+    fft = hg.FastFourierTransform(pupil, q=q, shift=shift)
+    plan = ofourier.FFTPlan(ogrids.RegularGrid(pupil.delta, pupil.dims, pupil.zero), q, 1, shift)
+    e = (rng.standard_normal(pupil.size) + 1j * rng.standard_normal(pupil.size)).astype(np.complex64)
+    f = (rng.standard_normal(fft.output_grid.size) + 1j * rng.standard_normal(fft.output_grid.size)).astype(np.complex64)
+    assert rel_err(fft.forward(e).numpy(), plan.forward(e.astype(complex))) < 2e-6
+    assert rel_err(fft.backward(f).numpy(), plan.backward(f.astype(complex))) < 2e-6
+
+
 def test_fft_tensor_field_batches():
     rng = np.random.default_rng(9)
     pupil = hg.make_pupil_grid(24, 1)
