@@ -197,13 +197,13 @@ template <> struct BlockW<double> {
 };
 
 template <typename T, int SPLIT>
-__global__ void __launch_bounds__(256, 3) influence_transpose_blocked_kernel(
+__global__ void __launch_bounds__(256) influence_transpose_blocked_kernel(
     int npix, int nact, const int* __restrict__ blk_ptr, const int* __restrict__ blk_pix,
     const T* __restrict__ blk_vals, int nvec, const T* __restrict__ g, T* __restrict__ g_act) {
     constexpr int VW = BlockW<T>::VW;
     constexpr int VPC = 8 * VW;  // vectors per CTA
-    __shared__ int s_pix[2][kTChunk];
-    __shared__ __align__(16) T s_w[2][kTChunk * kBA];
+    __shared__ int s_pix[kTChunk];
+    __shared__ __align__(16) T s_w[kTChunk * kBA];
     __shared__ __align__(16) T part[SPLIT][VPC * kBA];
     const int b = (int)blockIdx.x / SPLIT, rank = (int)blockIdx.x % SPLIT;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -217,40 +217,21 @@ __global__ void __launch_bounds__(256, 3) influence_transpose_blocked_kernel(
     for (int v = 0; v < VW; ++v)
 #pragma unroll
         for (int q = 0; q < kBA; ++q) acc[v][q] = T(0);
-    // chunks of the list staged with asynchronous copies, double-buffered: chunk i + 1 is in flight while the
-    // warps stream their vectors over chunk i
-    auto stage = [&](int buf, int c0) {
+    for (int c0 = e0; c0 < e1; c0 += kTChunk) {
         const int clen = min(kTChunk, e1 - c0);
+        if (c0 > e0) __syncthreads();  // the previous chunk is consumed
         for (int e = threadIdx.x; e < clen; e += blockDim.x) {
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(hx::ptx::smem_addr(&s_pix[buf][e])),
-                         "l"(blk_pix + c0 + e)
-                         : "memory");
+            s_pix[e] = __ldg(&blk_pix[c0 + e]);
 #pragma unroll
-            for (int c = 0; c < (int)(kBA * sizeof(T) / 16); ++c)
-                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
-                                 hx::ptx::smem_addr(&s_w[buf][e * kBA + c * (16 / sizeof(T))])),
-                             "l"(blk_vals + (long long)(c0 + e) * kBA + c * (16 / sizeof(T)))
-                             : "memory");
-        }
-        asm volatile("cp.async.commit_group;" ::: "memory");
-    };
-    if (e0 < e1) stage(0, e0);
-    for (int c0 = e0, it = 0; c0 < e1; c0 += kTChunk, ++it) {
-        const int clen = min(kTChunk, e1 - c0);
-        const int buf = it & 1;
-        if (c0 + kTChunk < e1) {
-            stage(buf ^ 1, c0 + kTChunk);  // its buffer was released by the barrier that ended chunk i - 1
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
+            for (int q = 0; q < kBA; ++q) s_w[e * kBA + q] = __ldg(&blk_vals[(long long)(c0 + e) * kBA + q]);
         }
         __syncthreads();
         if (nv > 0) {
 #pragma unroll 2
             for (int e = lane; e < clen; e += 32) {
-                const int p = s_pix[buf][e];
+                const int p = s_pix[e];
                 T w[kBA];
-                BlockW<T>::load(&s_w[buf][e * kBA], w);
+                BlockW<T>::load(s_w + e * kBA, w);
                 T x[VW];
 #pragma unroll
                 for (int v = 0; v < VW; ++v) x[v] = v < nv ? __ldg(&g[(long long)(v0 + v) * npix + p]) : T(0);
@@ -260,7 +241,6 @@ __global__ void __launch_bounds__(256, 3) influence_transpose_blocked_kernel(
                     for (int q = 0; q < kBA; ++q) acc[v][q] += w[q] * x[v];
             }
         }
-        __syncthreads();  // chunk i is consumed: its buffer takes chunk i + 2
     }
 #pragma unroll
     for (int v = 0; v < VW; ++v)
