@@ -18,7 +18,7 @@ namespace {
 
 // ---- extrusion ---------------------------------------------------------------------------------------------
 // The new slice (nslice values) is A (nslice x nst) . stencil + B (nslice x nb) . noise.  A cluster of XS CTAs
-// computes XRC new pixels; CTA `rank` takes the rank-th eighth of the stencil columns and of the noise columns
+// computes XRC (or 16) new pixels; CTA `rank` takes the rank-th eighth of the stencil columns and of the noise columns
 // (split-K): it gathers only its part of the stencil through the ring mapping into shared memory and streams its
 // column slice of the XRC rows of A and B (each warp XRC / 8 rows at once, 16-byte loads where the rows allow
 // them).  The XS partial sums of each pixel meet in the first CTA's shared memory (distributed shared memory) and
@@ -26,9 +26,8 @@ namespace {
 // stencil is gathered once per cluster.
 constexpr int XL_MAX = 8;       // extrusions per launch
 constexpr int XS = 8;           // CTAs per cluster (column slices)
-constexpr int XRC = 32;         // new pixels per cluster
+constexpr int XRC = 32;         // new pixels per cluster (16 when one wave of 32-pixel clusters would leave SMs idle)
 constexpr int XTHREADS = 256;
-constexpr int XRW = XRC / (XTHREADS / 32);  // rows per warp
 constexpr int XCHUNK = 2048;    // stencil values staged per pass
 
 template <typename T>
@@ -72,7 +71,7 @@ template <> struct Vec16<double> {
 
 // acc[q] += sum_k w_q[k] x[k] over k in [0, len) for the XRW rows w_q = w + q * ld (rows q >= nr are skipped),
 // lanes strided; 16-byte loads when every row and x are aligned.
-template <typename T>
+template <int XRW, typename T>
 __device__ __forceinline__ void dot_rows(T* acc, const T* __restrict__ w, long long ld, int nr,
                                          const T* __restrict__ x, int len, int lane) {
     using VT = Vec16<T>;
@@ -119,19 +118,20 @@ __device__ __forceinline__ void st_remote16(uint32_t addr, const T* v) {
                  : "memory");
 }
 
-// SPLIT: CTAs per cluster (XS, or 1 where clusters cannot be launched).  Six CTAs per SM for the float clusters
-// (40 registers): the three 1024^2 layers' 768 CTAs fit in one wave.
-template <typename T, int SPLIT>
+// SPLIT: CTAs per cluster (XS, or 1 where clusters cannot be launched); RC: new pixels per cluster (32 or 16).
+// Six CTAs per SM for the float clusters (40 registers): the three 1024^2 layers' 768 CTAs fit in one wave.
+template <typename T, int SPLIT, int RC>
 __global__ void __launch_bounds__(XTHREADS, (sizeof(T) == 4 && SPLIT > 1) ? 6 : 1)
     extrude_layers_kernel(const __grid_constant__ ExtrusionSet<T> set) {
+    constexpr int XRW = RC / (XTHREADS / 32);  // rows per warp
     __shared__ __align__(16) T st[XCHUNK];
-    __shared__ __align__(16) T part[SPLIT][XRC];
+    __shared__ __align__(16) T part[SPLIT][RC];
     int li = 0;
     for (int q = 1; q < set.count; ++q)
         if ((int)blockIdx.x >= set.l[q].block0) li = q;
     const Extrusion<T>& L = set.l[li];
     const int rank = SPLIT > 1 ? (int)((blockIdx.x - L.block0) % SPLIT) : 0;
-    const int r0 = (int)((blockIdx.x - L.block0) / SPLIT) * XRC;
+    const int r0 = (int)((blockIdx.x - L.block0) / SPLIT) * RC;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rw = r0 + warp * XRW;                     // first row of this warp
     const int nr = max(0, min(XRW, L.nslice - rw));     // rows of this warp inside the slice
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(XTHREADS, (sizeof(T) == 4 && SPLIT > 1) ? 6 : 
     const int s0 = slice_bound(L.nst, rank, SPLIT), s1 = slice_bound(L.nst, rank + 1, SPLIT);
     const int b0 = slice_bound(L.nb, rank, SPLIT), b1 = slice_bound(L.nb, rank + 1, SPLIT);
     // B . noise over this CTA's noise columns (independent of the stencil)
-    if (nr > 0 && b1 > b0) dot_rows(acc, L.B + (long long)rw * L.nb + b0, L.nb, nr, L.noise + b0, b1 - b0, lane);
+    if (nr > 0 && b1 > b0) dot_rows<XRW>(acc, L.B + (long long)rw * L.nb + b0, L.nb, nr, L.noise + b0, b1 - b0, lane);
     // A . stencil over this CTA's stencil columns, gathered through the ring in chunks
     for (int c0 = s0; c0 < s1; c0 += XCHUNK) {
         const int clen = min(XCHUNK, s1 - c0);
@@ -150,20 +150,26 @@ __global__ void __launch_bounds__(XTHREADS, (sizeof(T) == 4 && SPLIT > 1) ? 6 : 
         for (int k = threadIdx.x; k < clen; k += XTHREADS)
             st[k] = L.ring[ring_index(__ldg(&L.idx[c0 + k]), L.ny, L.nx, L.row0, L.col0, flip)];
         __syncthreads();
-        if (nr > 0) dot_rows(acc, L.A + (long long)rw * L.nst + c0, L.nst, nr, st, clen, lane);
+        if (nr > 0) dot_rows<XRW>(acc, L.A + (long long)rw * L.nst + c0, L.nst, nr, st, clen, lane);
     }
 #pragma unroll
     for (int r = 0; r < XRW; ++r)
         for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
     if constexpr (SPLIT > 1) {
         // every CTA of the cluster has started before the first remote store; the partial sums of this warp's
-        // XRW rows go to the first CTA as 16-byte stores
+        // XRW rows go to the first CTA as 16-byte stores (one 8-byte store for two float rows)
         hx::ptx::cluster_sync();
-        static_assert((XRW * sizeof(T)) % 16 == 0, "whole 16-byte stores");
+        static_assert((XRW * sizeof(T)) % 8 == 0, "whole 8-byte stores");
         if (lane == 0) {
             const uint32_t dst = hx::ptx::map_shared_rank(hx::ptx::smem_addr(&part[rank][warp * XRW]), 0);
+            if constexpr (XRW * sizeof(T) >= 16) {
 #pragma unroll
-            for (int c = 0; c < (int)(XRW * sizeof(T) / 16); ++c) st_remote16(dst + 16 * c, acc + c * (16 / sizeof(T)));
+                for (int c = 0; c < (int)(XRW * sizeof(T) / 16); ++c)
+                    st_remote16(dst + 16 * c, acc + c * (16 / sizeof(T)));
+            } else {
+                const uint2 u = *reinterpret_cast<const uint2*>(acc);
+                asm volatile("st.shared::cluster.v2.u32 [%0], {%1, %2};" ::"r"(dst), "r"(u.x), "r"(u.y) : "memory");
+            }
         }
         hx::ptx::cluster_sync();
         if (rank != 0) return;
@@ -176,7 +182,7 @@ __global__ void __launch_bounds__(XTHREADS, (sizeof(T) == 4 && SPLIT > 1) ? 6 : 
     }
     const int rl = threadIdx.x;
     const int r = r0 + rl;
-    if (rl >= XRC || r >= L.nslice) return;
+    if (rl >= RC || r >= L.nslice) return;
     T v = part[0][rl];
 #pragma unroll
     for (int q = 1; q < SPLIT; ++q) v += part[q][rl];
@@ -218,7 +224,7 @@ bool extrude_clusters_ok() {
         cfg.numAttrs = 1;
         int n = 0;
         const bool good =
-            cudaOccupancyMaxActiveClusters(&n, extrude_layers_kernel<T, XS>, &cfg) == cudaSuccess && n > 0;
+            cudaOccupancyMaxActiveClusters(&n, extrude_layers_kernel<T, XS, XRC>, &cfg) == cudaSuccess && n > 0;
         cudaGetLastError();
         ok[dev] = good ? 1 : 2;
     }
@@ -372,6 +378,18 @@ int hx_atmosphere_extrude_layers(const hx_extrusion* steps, int count, int dtype
         using T = std::remove_pointer_t<decltype(tag)>;
         const bool cl = extrude_clusters_ok<T>();
         const int split = cl ? XS : 1;
+        // float: 16-pixel clusters when they still fit in one wave (six CTAs per SM), so a single 1024-pixel
+        // extrusion runs 512 CTAs instead of 256
+        int rc = XRC;
+        if (cl && sizeof(T) == 4) {
+            int dev = 0, sms = 0;
+            long long c16 = 0;
+            for (int l = 0; l < count; ++l) c16 += hx::ceil_div(steps[l].where <= 1 ? steps[l].nx : steps[l].ny, 16);
+            if (cudaGetDevice(&dev) == cudaSuccess &&
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+                c16 * XS <= 6LL * sms)
+                rc = 16;
+        }
         ExtrusionSet<T> set{};
         double bytes = 0.0;
         int b0 = 0;
@@ -392,7 +410,7 @@ int hx_atmosphere_extrude_layers(const hx_extrusion* steps, int count, int dtype
             d.nb = e.nb;
             d.nslice = e.where <= 1 ? e.nx : e.ny;
             d.block0 = b0;
-            b0 += hx::ceil_div(d.nslice, XRC) * split;
+            b0 += hx::ceil_div(d.nslice, rc) * split;
             bytes += (double)esz * ((double)d.nslice * (e.nst + e.nb) + d.nslice) + (esz + 8.0) * e.nst + esz * e.nb;
         }
         set.count = count;
@@ -409,10 +427,14 @@ int hx_atmosphere_extrude_layers(const hx_extrusion* steps, int count, int dtype
             attr[0].val.clusterDim.z = 1;
             cfg.attrs = attr;
             cfg.numAttrs = 1;
-            HX_TRY(hx::cuda_status(cudaLaunchKernelEx(&cfg, extrude_layers_kernel<T, XS>, set),
-                                   "extrude_layers_kernel"));
+            if (rc == 16)
+                HX_TRY(hx::cuda_status(cudaLaunchKernelEx(&cfg, extrude_layers_kernel<T, XS, 16>, set),
+                                       "extrude_layers_kernel"));
+            else
+                HX_TRY(hx::cuda_status(cudaLaunchKernelEx(&cfg, extrude_layers_kernel<T, XS, XRC>, set),
+                                       "extrude_layers_kernel"));
         } else {
-            extrude_layers_kernel<T, 1><<<(unsigned)b0, XTHREADS, 0, st>>>(set);
+            extrude_layers_kernel<T, 1, XRC><<<(unsigned)b0, XTHREADS, 0, st>>>(set);
         }
         return hx::launch_status("extrude_layers_kernel");
     };
