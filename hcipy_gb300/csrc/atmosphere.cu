@@ -136,6 +136,8 @@ __global__ void __launch_bounds__(XTHREADS, (sizeof(T) == 4 && SPLIT > 1) ? 6 : 
     const int rw = r0 + warp * XRW;                     // first row of this warp
     const int nr = max(0, min(XRW, L.nslice - rw));     // rows of this warp inside the slice
     const bool flip = L.where == 1 || L.where == 3;
+    // first phase of the cluster barrier: arrive now, wait before the first remote store (every CTA has started)
+    if constexpr (SPLIT > 1) hx::ptx::cluster_arrive_relaxed();
     T acc[XRW];
 #pragma unroll
     for (int r = 0; r < XRW; ++r) acc[r] = T(0);
@@ -158,7 +160,7 @@ __global__ void __launch_bounds__(XTHREADS, (sizeof(T) == 4 && SPLIT > 1) ? 6 : 
     if constexpr (SPLIT > 1) {
         // every CTA of the cluster has started before the first remote store; the partial sums of this warp's
         // XRW rows go to the first CTA as 16-byte stores (one 8-byte store for two float rows)
-        hx::ptx::cluster_sync();
+        hx::ptx::cluster_wait();
         static_assert((XRW * sizeof(T)) % 8 == 0, "whole 8-byte stores");
         if (lane == 0) {
             const uint32_t dst = hx::ptx::map_shared_rank(hx::ptx::smem_addr(&part[rank][warp * XRW]), 0);

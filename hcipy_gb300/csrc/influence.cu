@@ -197,7 +197,7 @@ template <> struct BlockW<double> {
 };
 
 template <typename T, int SPLIT>
-__global__ void __launch_bounds__(256) influence_transpose_blocked_kernel(
+__global__ void __launch_bounds__(256, 4) influence_transpose_blocked_kernel(
     int npix, int nact, const int* __restrict__ blk_ptr, const int* __restrict__ blk_pix,
     const T* __restrict__ blk_vals, int nvec, const T* __restrict__ g, T* __restrict__ g_act) {
     constexpr int VW = BlockW<T>::VW;
@@ -212,6 +212,8 @@ __global__ void __launch_bounds__(256) influence_transpose_blocked_kernel(
     const int u0 = blk_ptr[b], u1 = blk_ptr[b + 1];
     const int e0 = u0 + (int)((long long)(u1 - u0) * rank / SPLIT);
     const int e1 = u0 + (int)((long long)(u1 - u0) * (rank + 1) / SPLIT);
+    // first phase of the cluster barrier: arrive now, wait before the first remote store (every CTA has started)
+    if constexpr (SPLIT > 1) hx::ptx::cluster_arrive_relaxed();
     T acc[VW][kBA];
 #pragma unroll
     for (int v = 0; v < VW; ++v)
@@ -249,7 +251,7 @@ __global__ void __launch_bounds__(256) influence_transpose_blocked_kernel(
             for (int o = 16; o > 0; o >>= 1) acc[v][q] += __shfl_xor_sync(0xffffffffu, acc[v][q], o);
     // partial sums of this warp's vectors: part[rank][(warp * VW + v) * kBA + q]
     if constexpr (SPLIT > 1) {
-        hx::ptx::cluster_sync();  // every CTA of the cluster has started before the first remote store
+        hx::ptx::cluster_wait();  // every CTA of the cluster has started before the first remote store
         if (lane == 0) {
             const uint32_t dst = hx::ptx::map_shared_rank(hx::ptx::smem_addr(&part[rank][warp * VW * kBA]), 0);
 #pragma unroll

@@ -98,7 +98,7 @@ void free_plan(hx_mft_plan* p) {
 // The products are associated by output rows (the same complex MACs as the two GEMMs); sums run in blocks of kBlk
 // terms added into the total, so FP32 rounding grows with sqrt(kBlk) + sqrt(K / kBlk) rather than sqrt(K).
 constexpr int kSmThreads = 256;
-constexpr int kSmRows = 4;     // output rows per cluster (RPC)
+constexpr int kSmRows = 8;     // output rows per cluster (RPC): a 256^2 -> 128^2 transform fills one wave (128 CTAs)
 constexpr int kSmSlices = 8;   // CTAs per cluster (CS)
 constexpr int kBlk = 16;       // terms per partial sum
 constexpr int kSmMaxBytes = 200 * 1024;

@@ -131,6 +131,13 @@ __device__ __forceinline__ void cluster_sync() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
+// The two halves of a cluster barrier phase, for a phase that overlaps work: every thread of every CTA arrives
+// (relaxed: no memory ordering) early and waits later; after the wait every CTA of the cluster has started.
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+    asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.aligned;" ::: "memory"); }
+
 // Address of the same shared-memory location in CTA `rank` of the cluster.
 __device__ __forceinline__ uint32_t map_shared_rank(uint32_t saddr, uint32_t rank) {
     uint32_t r;
