@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(kEfcThreads) efc_step_kernel(const double* __r
     const int nrows = min(kEfcRows, nact - row0);
     const long long ld = 2LL * n_dz;
     const int p0 = (int)((long long)n_dz * rank / SPLIT), p1 = (int)((long long)n_dz * (rank + 1) / SPLIT);
+    if constexpr (SPLIT > 1) hx::ptx::cluster_arrive_relaxed();  // first phase of the cluster barrier
     ff acc[kEfcRows];
 #pragma unroll
     for (int q = 0; q < kEfcRows; ++q) acc[q] = {0.0f, 0.0f};
@@ -102,8 +103,10 @@ __global__ void __launch_bounds__(kEfcThreads) efc_step_kernel(const double* __r
         red[q][0] = s;
     }
     if constexpr (SPLIT > 1) {
-        // every CTA of the cluster has started (its shared memory exists) before the first remote store
-        hx::ptx::cluster_sync();
+        // every CTA of the cluster has started (its shared memory exists) before the first remote store: the
+        // barrier phase opened at the kernel's start; the CTA barrier orders red[] for thread 0
+        __syncthreads();
+        hx::ptx::cluster_wait();
         if (threadIdx.x == 0) {
             static_assert(kEfcRows == 4, "two 16-byte stores carry the four partial sums");
             const uint32_t dst = hx::ptx::map_shared_rank(hx::ptx::smem_addr(&part[rank][0]), 0);

@@ -98,7 +98,7 @@ void free_plan(hx_mft_plan* p) {
 // The products are associated by output rows (the same complex MACs as the two GEMMs); sums run in blocks of kBlk
 // terms added into the total, so FP32 rounding grows with sqrt(kBlk) + sqrt(K / kBlk) rather than sqrt(K).
 constexpr int kSmThreads = 256;
-constexpr int kSmRows = 8;     // output rows per cluster (RPC): a 256^2 -> 128^2 transform fills one wave (128 CTAs)
+constexpr int kSmRows = 4;     // output rows per cluster (RPC)
 constexpr int kSmSlices = 8;   // CTAs per cluster (CS)
 constexpr int kBlk = 16;       // terms per partial sum
 constexpr int kSmMaxBytes = 200 * 1024;
@@ -156,6 +156,8 @@ __global__ void __launch_bounds__(kSmThreads) mft_small_kernel(int R, int K1, in
     const int x0 = q * L.xw;
     const int xn = max(0, min(L.xw, K2 - x0));  // columns of this slice
     const Cx zero = hx::make_c<T>(T(0), T(0));
+    // first phase of the cluster barrier: arrive now, wait before the first remote store
+    asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
     Cx* a_s = sm + L.a;
     Cx* x_s = sm + L.x;
     Cx* b_s = sm + L.b;
@@ -214,7 +216,7 @@ __global__ void __launch_bounds__(kSmThreads) mft_small_kernel(int R, int K1, in
     }
     __syncthreads();
     // partial image p[rr][u] = sum_xl w[rr][xl] B[x0 + xl][u], sent to the CTA that finishes column u
-    cluster_barrier();  // every CTA of the cluster may now receive
+    asm volatile("barrier.cluster.wait.aligned;" ::: "memory");  // every CTA of the cluster has started
     for (int i = threadIdx.x; i < kSmRows * C; i += kSmThreads) {
         const int rr = i / C, u = i - rr * C;
         Cx acc = zero;
