@@ -35,13 +35,6 @@ std::vector<int> factor_radices(int n, bool allow16 = false) {
     return r;
 }
 
-bool is_smooth(int n) { return n == 1 || !factor_radices(n).empty(); }
-
-int next_smooth(int n) {
-    while (!is_smooth(n)) ++n;
-    return n;
-}
-
 int next_pow2(int n) {
     int m = 1;
     while (m < n) m <<= 1;
