@@ -9,6 +9,7 @@
 // screen instead).  The extrusions of several layers (one step of each) run as one launch.  The quintic
 // sub-pixel shift (hcipy/_math/subpixel_shift.py:7-343: 7-tap B-spline, clamp to edge, rows then columns) reads
 // the rings and writes the layers' logical screens and their sum in one tiled pass.
+#include <cstdlib>
 #include <type_traits>
 
 #include "hx_common.cuh"
@@ -211,8 +212,12 @@ __global__ void __launch_bounds__(XTHREADS, (sizeof(T) == 4 && SPLIT > 1) ? 6 : 
 template <typename T>
 bool extrude_clusters_ok() {
     static int ok[64];  // per device: 0 unknown, 1 yes, 2 no
+    static const bool off = [] {  // HX_NO_CLUSTERS=1: the one-CTA form (tests of that path)
+        const char* e = getenv("HX_NO_CLUSTERS");
+        return e && e[0] == '1';
+    }();
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    if (off || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
     if (!ok[dev]) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(XS, 1, 1);

@@ -11,6 +11,8 @@
 // Products and sums run in float-float arithmetic on the FP32 pipe (the float64 inputs are split into hi + lo
 // with integer operations), each thread adding its strided terms in order and each CTA combining its threads in
 // a fixed tree, so the step is deterministic and keeps ~46 bits.
+#include <cstdlib>
+
 #include "hx_common.cuh"
 #include "split_gemm.cuh"
 #include "tc_ptx.cuh"
@@ -133,8 +135,12 @@ __global__ void __launch_bounds__(kEfcThreads) efc_step_kernel(const double* __r
 template <typename Cx>
 bool clusters_ok() {
     static int ok[64];  // per device: 0 unknown, 1 yes, 2 no
+    static const bool off = [] {  // HX_NO_CLUSTERS=1: the one-CTA form (tests of that path)
+        const char* e = getenv("HX_NO_CLUSTERS");
+        return e && e[0] == '1';
+    }();
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    if (off || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
     if (!ok[dev]) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(kEfcSplit, 1, 1);

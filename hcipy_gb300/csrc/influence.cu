@@ -12,6 +12,8 @@
 //    (DeformableMirror.forward/backward with c = +-2k, deformable_mirror.py:200-238; AtmosphericLayer
 //    forward/backward with c = +-1/lambda, hcipy/atmosphere/atmospheric_model.py:143-151), and its gradient
 //    for real s: g_s = c Im(conj(out) g_out), g_e = g_out exp(-i c s) summed over broadcast copies.
+#include <cstdlib>
+
 #include "hx_common.cuh"
 #include "tc_ptx.cuh"
 
@@ -292,8 +294,12 @@ __global__ void __launch_bounds__(256, 4) influence_transpose_blocked_kernel(
 template <typename T>
 bool transpose_clusters_ok() {
     static int ok[64];  // per device: 0 unknown, 1 yes, 2 no
+    static const bool off = [] {  // HX_NO_CLUSTERS=1: the one-CTA form (tests of that path)
+        const char* e = getenv("HX_NO_CLUSTERS");
+        return e && e[0] == '1';
+    }();
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    if (off || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
     if (!ok[dev]) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(kTS, 1, 1);
