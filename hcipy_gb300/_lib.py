@@ -94,6 +94,8 @@ SIGNATURES = {
     'hx_mft_execute_io': (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_double, c_double, c_int,
                                   c_void_p, c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
     'hx_lyot_workspace_bytes': (c_size_t, [c_void_p, c_void_p, c_int]),
+    'hx_mft_execute_phase': (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_double, c_void_p, c_int, c_double,
+                                     c_double, c_void_p, c_size_t, c_void_p]),
     'hx_lyot_execute': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p, c_double, c_double,
                                 c_double, c_double, c_double, c_double, c_void_p, c_int, c_void_p, c_int, c_void_p,
                                 c_size_t, c_void_p]),

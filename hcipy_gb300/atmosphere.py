@@ -352,6 +352,10 @@ class AtmosphericLayer(OpticalElement):
     def backward(self, wf):
         return self._apply(wf, -1.0)
 
+    def _pure_phase_screen(self):
+        """The screen s (radians at 1 m) whose forward is exp(i s / wavelength): a consumer may fuse the phase."""
+        return self._screen_tensor()
+
 
 _WHERE = {'bottom': 0, 'top': 1, 'left': 2, 'right': 3}
 
@@ -730,6 +734,10 @@ class MultiLayerAtmosphere(OpticalElement):
         if self._scintillation:
             raise ValueError('Cannot get the unwrapped phase for an atmosphere with scintillation.')
         return Field(self.combined_screen() / wavelength, self.layers[0].input_grid)
+
+    def _pure_phase_screen(self):
+        """The summed screen when the forward is exp(i s / wavelength) (no scintillation), else None."""
+        return None if self._scintillation else self.combined_screen()
 
     def _apply(self, wf, sign):
         e = as_tensor(wf.electric_field)

@@ -57,16 +57,32 @@ class BroadbandImager(object):
             self._streams = [torch.cuda.Stream() for _ in range(self.num_streams)]
         return self._streams
 
+    def _phase_screen(self):
+        """The screen of ``pre`` when it is a pure phase element (an atmosphere without scintillation), else None:
+        the split transforms then apply its phase while slicing their input (``forward_phase_screen``)."""
+        pre = self.pre
+        owner = getattr(pre, '__self__', None)  # a bound ``forward`` of an element counts as the element
+        if owner is not None and getattr(pre, '__func__', None) is getattr(type(owner), 'forward', None):
+            pre = owner
+        hook = getattr(pre, '_pure_phase_screen', None)
+        return hook() if hook is not None else None
+
+    def _one(self, t, wl, prop, screen):
+        """(image, field kept alive or None) of one wavelength."""
+        if screen is not None:
+            img = prop.forward_phase_screen(t, screen, 1.0 / wl, wl)
+            if img is not None:
+                return img, None
+        wf = Wavefront(Field(t, self.pupil_grid), wl)
+        if self.pre is not None:
+            wf = self.pre(wf)
+        return prop.forward(wf).electric_field.data, wf.electric_field.data
+
     def forward(self, e, concurrent=True):
         t = as_tensor(e.electric_field if isinstance(e, Wavefront) else e)
+        screen = self._phase_screen()
         if not concurrent or self.num_streams == 1:
-            out = []
-            for wl, prop in zip(self.wavelengths, self.props):
-                wf = Wavefront(Field(t, self.pupil_grid), wl)
-                if self.pre is not None:
-                    wf = self.pre(wf)
-                out.append(prop.forward(wf).electric_field.data)
-            return out
+            return [self._one(t, wl, prop, screen)[0] for wl, prop in zip(self.wavelengths, self.props)]
         main = torch.cuda.current_stream()
         streams = self._side_streams()
         capturing = torch.cuda.is_current_stream_capturing()
@@ -76,18 +92,25 @@ class BroadbandImager(object):
         # (record_stream guards that outside a capture; inside one only the reference does).
         fields = []
         for i, (wl, prop) in enumerate(zip(self.wavelengths, self.props)):
-            wf = Wavefront(Field(t, self.pupil_grid), wl)
-            if self.pre is not None:
-                wf = self.pre(wf)  # in order on the calling stream: ``pre`` may keep state
-            fields.append(wf.electric_field.data)
+            fused = screen is not None and prop.phase_screen_fusable(t, screen, wl)
+            wf = None
+            if not fused:
+                wf = Wavefront(Field(t, self.pupil_grid), wl)
+                if self.pre is not None:
+                    wf = self.pre(wf)  # in order on the calling stream: ``pre`` may keep state
+                fields.append(wf.electric_field.data)
             side = streams[i % len(streams)]
             side.wait_stream(main)
             with torch.cuda.stream(side):
-                img = prop.forward(wf).electric_field.data
+                if fused:
+                    img = prop.forward_phase_screen(t, screen, 1.0 / wl, wl)
+                else:
+                    img = prop.forward(wf).electric_field.data
             if not capturing:
                 # the field was made on the calling stream and is read on ``side``; the image is made on
                 # ``side`` and handed back: tell the allocator about both uses
-                wf.electric_field.data.record_stream(side)
+                if wf is not None:
+                    wf.electric_field.data.record_stream(side)
                 img.record_stream(main)
             out.append(img)
         for side in streams:
@@ -96,6 +119,7 @@ class BroadbandImager(object):
         return out
 
     __call__ = forward
+
 
     def capture(self, example):
         """Record ``forward`` for inputs shaped like ``example`` in a CUDA graph; ``replay`` then runs it.

@@ -80,6 +80,15 @@ template <typename C> __host__ __device__ inline C cmul(C a, C b) {
     return r;
 }
 
+// x exp(i ph) for a complex64 value with the products and sums rounded one by one (no contraction into FMAs),
+// so that every kernel that applies a phase screen to complex64 fields gives the same bits.
+__device__ __forceinline__ float2 phase_rotate(float2 x, float ph) {
+    float sn, cs;
+    sincosf(ph, &sn, &cs);
+    return make_float2(__fsub_rn(__fmul_rn(x.x, cs), __fmul_rn(x.y, sn)),
+                       __fadd_rn(__fmul_rn(x.x, sn), __fmul_rn(x.y, cs)));
+}
+
 }  // namespace hx
 
 #define HX_TRY(expr)                  \

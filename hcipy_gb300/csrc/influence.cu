@@ -360,10 +360,14 @@ __global__ void phase_apply_kernel(long long n, int batch, int batch_e, int batc
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int b = blockIdx.y;
     if (i >= n) return;
-    T sn, cs;
-    sincos_t(scale * s[(long long)(b % batch_s) * n + i], &sn, &cs);
     const auto x = e[(long long)(b % batch_e) * n + i];
-    out[(long long)b * n + i] = hx::make_c<T>(x.x * cs - x.y * sn, x.x * sn + x.y * cs);
+    if constexpr (sizeof(T) == 4) {
+        out[(long long)b * n + i] = hx::phase_rotate(x, __fmul_rn(scale, s[(long long)(b % batch_s) * n + i]));
+    } else {
+        T sn, cs;
+        sincos_t(scale * s[(long long)(b % batch_s) * n + i], &sn, &cs);
+        out[(long long)b * n + i] = hx::make_c<T>(x.x * cs - x.y * sn, x.x * sn + x.y * cs);
+    }
 }
 
 // One thread per pixel, looping over the batch: g_s for every output, g_e summed over the copies that share

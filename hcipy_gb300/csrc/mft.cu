@@ -526,6 +526,19 @@ int hx_mft_execute_io(const hx_mft_plan* p, int direction, int batch, const void
                                  (const float2*)mask, src, src_dtype, ws, ws_bytes, (cudaStream_t)stream);
 }
 
+int hx_mft_execute_phase(const hx_mft_plan* p, int batch, const void* in, const float* screen, double scale,
+                         void* out, int out_dtype, double are, double aim, void* ws, size_t ws_bytes, void* stream) {
+    HX_CHECK_ARG(p != nullptr, "hx_mft_execute_phase: plan is NULL");
+    HX_CHECK_ARG(p->precision == HX_PREC_SPLIT, "hx_mft_execute_phase: a split-precision plan is needed");
+    HX_CHECK_ARG(out_dtype == HX_C64 || out_dtype == HX_C128, "hx_mft_execute_phase: out dtype must be HX_C64 or HX_C128");
+    HX_CHECK_ARG(batch >= 1 && in && screen && out, "hx_mft_execute_phase: bad batch or NULL pointer");
+    const size_t need = hx_mft_workspace_bytes(p, HX_FORWARD, batch);
+    HX_CHECK_ARG(ws != nullptr && ws_bytes >= need, "hx_mft_execute_phase: workspace of %zu bytes needed", need);
+    if (hx::fault_injected("launch")) return HX_ERR_INJECTED;
+    return hx::split_mft_execute_phase(p->split, batch, in, screen, scale, out, out_dtype, are, aim, ws,
+                                       (cudaStream_t)stream);
+}
+
 size_t hx_lyot_workspace_bytes(const hx_mft_plan* fpm, const hx_mft_plan* img, int batch) {
     if (!fpm || batch <= 0) return 0;
     if (fpm->precision == HX_PREC_SPLIT)

@@ -127,9 +127,13 @@ __global__ void slice_rows_kernel(FieldIO src, long long ld, int K, int Kp, cons
 // slice_rows_kernel<1> for a row whose maximum is not known yet and that fits in registers (Kp <= 1024 G): the
 // CTA reads the row once into registers (G groups of four consecutive points per thread), takes its maximum and
 // slices from the registers, where slice_rows_kernel reads the row twice.  Same slices, same scales.
-template <int G>
+// PHASE: the row is a complex64 field times exp(i scale screen) (a phase screen of screen_rows x K values shared by
+// the stacked fields), applied here as hx::phase_rotate does, so the phase-screened field is never stored.
+template <int G, bool PHASE>
 __global__ void __launch_bounds__(256) slice_rows_reg_kernel(FieldIO src, long long ld, int K, int Kp, __half* planes,
-                                                             long long plane_stride, int kpitch, float* scale_out) {
+                                                             long long plane_stride, int kpitch, float* scale_out,
+                                                             const float* __restrict__ screen, int screen_rows,
+                                                             float phase_scale) {
     const long long m = blockIdx.x;
     __shared__ float red[8];
     __shared__ float s_scale;
@@ -138,7 +142,18 @@ __global__ void __launch_bounds__(256) slice_rows_reg_kernel(FieldIO src, long l
 #pragma unroll
     for (int gi = 0; gi < G; ++gi) {
         const int k0 = 4 * ((int)threadIdx.x + gi * 256);
-        if (k0 + 4 <= K) {
+        if constexpr (PHASE) {
+            const float* srow = screen + (m % screen_rows) * (long long)K;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                cff x = {};
+                if (k0 + j < K) {
+                    const float2 e = hx::phase_rotate(src.c64[m * ld + k0 + j], __fmul_rn(phase_scale, srow[k0 + j]));
+                    x = {{e.x, 0.0f}, {e.y, 0.0f}};
+                }
+                v[gi][j] = x;
+            }
+        } else if (k0 + 4 <= K) {
             load4_field(src, m * ld + k0, v[gi]);
         } else {
 #pragma unroll
@@ -504,18 +519,42 @@ FieldIO carve_ff(Carver& c, long long n) {
     return f;
 }
 
+// phase (optional, emb rows of a complex64 field only): the rows are the field times exp(i phase->scale screen).
+struct RowPhase {
+    const float* screen;
+    int rows;
+    float scale;
+};
+
 int launch_slice_rows(const FieldIO& src, long long ld, long long M, int K, const unsigned int* rowmax,
-                      SliceMat& s, cudaStream_t st, bool emb = false) {
+                      SliceMat& s, cudaStream_t st, bool emb = false, const RowPhase* phase = nullptr) {
     if (M > 2147483647LL) return HX_ERR_UNSUPPORTED;
+    if (phase && (!emb || rowmax || s.Kp > 4096 || !src.c64 || src.c128 || src.re_hi)) {
+        set_error("a phase screen is applied only while slicing complex64 rows of at most 4096 points");
+        return HX_ERR_UNSUPPORTED;
+    }
     if (emb && !rowmax && s.Kp <= 4096) {
         const unsigned grid = (unsigned)M;
         const long long ps = s.plane_stride();
-        switch ((s.Kp + 1023) / 1024) {
-            case 1: slice_rows_reg_kernel<1><<<grid, 256, 0, st>>>(src, ld, K, s.Kp, s.planes, ps, s.kpitch, s.scale); break;
-            case 2: slice_rows_reg_kernel<2><<<grid, 256, 0, st>>>(src, ld, K, s.Kp, s.planes, ps, s.kpitch, s.scale); break;
-            case 3: slice_rows_reg_kernel<3><<<grid, 256, 0, st>>>(src, ld, K, s.Kp, s.planes, ps, s.kpitch, s.scale); break;
-            default: slice_rows_reg_kernel<4><<<grid, 256, 0, st>>>(src, ld, K, s.Kp, s.planes, ps, s.kpitch, s.scale);
-        }
+        const float* scr = phase ? phase->screen : nullptr;
+        const int sr = phase ? phase->rows : 1;
+        const float sc = phase ? phase->scale : 0.0f;
+        auto run = [&](auto g_tag, auto p_tag) {
+            constexpr int G = decltype(g_tag)::value;
+            constexpr bool P = decltype(p_tag)::value;
+            slice_rows_reg_kernel<G, P><<<grid, 256, 0, st>>>(src, ld, K, s.Kp, s.planes, ps, s.kpitch, s.scale, scr,
+                                                              sr, sc);
+        };
+        auto by_g = [&](auto p_tag) {
+            switch ((s.Kp + 1023) / 1024) {
+                case 1: run(std::integral_constant<int, 1>(), p_tag); break;
+                case 2: run(std::integral_constant<int, 2>(), p_tag); break;
+                case 3: run(std::integral_constant<int, 3>(), p_tag); break;
+                default: run(std::integral_constant<int, 4>(), p_tag);
+            }
+        };
+        if (phase) by_g(std::true_type());
+        else by_g(std::false_type());
         return launch_status("slice_rows_reg_kernel");
     }
     if (emb)
@@ -930,7 +969,7 @@ SliceMat forward_input_slices(const SplitMftPlan* p, int batch, void* ws) {
 int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO& in, const unsigned int* in_max,
                   const FieldIO& out, double are, double aim, int epilogue, const float2* mask, const FieldIO& src,
                   unsigned int* out_rowmax, unsigned int* out_colmax, void* ws, cudaStream_t st,
-                  bool in_sliced = false) {
+                  bool in_sliced = false, const RowPhase* in_phase = nullptr) {
     const int nx = p->nx, ny = p->ny, nu = p->nu, nv = p->nv;
     const long long nu64 = round_up(nu, 64);
     const long long rows = (long long)batch * ny;
@@ -941,7 +980,7 @@ int split_mft_run(const SplitMftPlan* p, int direction, int batch, const FieldIO
         HX_TRY(cuda_status(cudaMemsetAsync(w.t_max, 0, sizeof(unsigned int) * batch * nu64, st), "memset"));
         // G1: T = E . M2f, stacked over the batch (embedding on M2f); column maxima of T per field for the next
         // slicing.
-        if (!in_sliced) HX_TRY(launch_slice_rows(in, nx, rows, nx, in_max, w.s1, st, true));
+        if (!in_sliced) HX_TRY(launch_slice_rows(in, nx, rows, nx, in_max, w.s1, st, true, in_phase));
         GemmArgs g1 = base_args(p->status);
         g1.emb = 1;
         g1.M = (int)rows;
@@ -1112,6 +1151,20 @@ int split_mft_execute(const SplitMftPlan* p, int direction, int batch, const voi
     }
     return split_mft_run(p, direction, batch, input_field(in, in_dtype), nullptr, output_field(out, out_dtype), are,
                          aim, epilogue, mask, input_field(src, src_dtype), nullptr, nullptr, ws, st);
+}
+
+// Forward transform of complex64 fields times exp(i scale screen) (screen: ny x nx float32, shared by the batch):
+// the phase is applied while the first GEMM's operand is sliced.
+int split_mft_execute_phase(const SplitMftPlan* p, int batch, const void* in, const float* screen, double scale,
+                            void* out, int out_dtype, double are, double aim, void* ws, cudaStream_t st) {
+    if (!p) {
+        set_error("the split tensor-core MFT plan is missing");
+        return HX_ERR_INVALID;
+    }
+    const RowPhase ph{screen, p->ny, (float)scale};
+    FieldIO none;
+    return split_mft_run(p, HX_FORWARD, batch, input_field(in, HX_C64), nullptr, output_field(out, out_dtype), are,
+                         aim, HX_EPI_NONE, nullptr, none, nullptr, nullptr, ws, st, false, &ph);
 }
 
 // Lyot coronagraph (and final image) with float-float fields between the transforms.

@@ -17,6 +17,10 @@ size_t split_mft_workspace_bytes(const SplitMftPlan* p, int direction, int batch
 int split_mft_execute(const SplitMftPlan* p, int direction, int batch, const void* in, int in_dtype, void* out,
                       int out_dtype, double are, double aim, int epilogue, const float2* mask, const void* src,
                       int src_dtype, void* ws, size_t ws_bytes, cudaStream_t stream);
+// Forward transform of complex64 fields times exp(i scale screen), the phase applied while slicing (screen: the
+// plan's ny x nx float32 values, shared by the batch).
+int split_mft_execute_phase(const SplitMftPlan* p, int batch, const void* in, const float* screen, double scale,
+                            void* out, int out_dtype, double are, double aim, void* ws, cudaStream_t stream);
 // Lyot coronagraph and (if img != NULL) its final image, with the focal-plane and Lyot-plane fields in
 // float-float between the transforms.
 size_t split_lyot_workspace_bytes(const SplitMftPlan* fpm, const SplitMftPlan* img, int batch);

@@ -169,6 +169,15 @@ class _MftPlan(object):
                                         _lib.dptr(workspace), nbytes, _lib.stream_handle())
         _lib.check(rc, 'hx_mft_execute_io')
 
+    def execute_phase(self, batch, inp, screen, scale, out, alpha):
+        """Split plans, forward: complex64 fields times exp(i scale screen), the phase applied while slicing."""
+        nbytes = self.workspace_bytes(_lib.HX_FORWARD, batch)
+        workspace = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=inp.device)
+        rc = self.lib.hx_mft_execute_phase(self.handle, batch, _lib.dptr(inp), _lib.dptr(screen), float(scale),
+                                           _lib.dptr(out), _lib.dtype_code(out.dtype), float(alpha.real),
+                                           float(alpha.imag), _lib.dptr(workspace), nbytes, _lib.stream_handle())
+        _lib.check(rc, 'hx_mft_execute_phase')
+
     def set_schedule(self, code):
         _lib.check(self.lib.hx_mft_plan_set_schedule(self.handle, code), 'hx_mft_plan_set_schedule')
 

@@ -3,7 +3,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .field import Field
+from .field import Field, as_tensor
 from .fourier import make_fourier_transform, MatrixFourierTransform
 from .optics import AgnosticOpticalElement, Wavefront, make_agnostic_forward, make_agnostic_backward
 
@@ -79,6 +79,39 @@ class FraunhoferPropagator(AgnosticOpticalElement):
 
     def get_output_grid(self, input_grid, wavelength):
         return self._output_grid
+
+    def phase_screen_fusable(self, t, screen, wavelength=1):
+        """Whether ``forward_phase_screen`` applies to these device tensors (checks only, no launch)."""
+        inst = self.get_instance_data(self._input_grid, None, wavelength)
+        ft = inst.fourier_transform
+        if not isinstance(ft, MatrixFourierTransform) or ft.precision != 'split':
+            return False
+        if t.dtype != torch.complex64 or screen.dtype != torch.float32 or ft._win is not None or ft._wout is not None:
+            return False
+        if torch.is_grad_enabled() and (t.requires_grad or screen.requires_grad):
+            return False
+        n = ft.input_grid.size
+        return t.shape[-1] == n and screen.numel() == n
+
+    def forward_phase_screen(self, e, screen, scale, wavelength=1):
+        """``forward`` of the field ``e`` times exp(i scale screen) (a pure phase element such as an atmosphere
+        without scintillation ahead of the lens), with the phase applied while the transform slices its input:
+        split precision, complex64 fields, uniformly weighted grids; None when the propagator cannot do that here
+        (the caller then applies the phase and calls ``forward``)."""
+        t = as_tensor(e)
+        s = as_tensor(screen)
+        if not self.phase_screen_fusable(t, s, wavelength):
+            return None
+        inst = self.get_instance_data(self._input_grid, None, wavelength)
+        ft = inst.fourier_transform
+        t = t.contiguous()
+        lead = tuple(t.shape[:-1])
+        batch = int(np.prod(lead)) if lead else 1
+        out = torch.empty(lead + (ft.output_grid.size,), dtype=torch.complex128, device=t.device)
+        if batch > 0:
+            alpha = complex(ft._w_in_scalar) * inst.norm_factor
+            ft._plan(t.dtype).execute_phase(batch, t, s.contiguous(), scale, out, alpha)
+        return out
 
     @make_agnostic_forward
     def forward(self, instance_data, wavefront):

@@ -142,6 +142,15 @@ HX_API int hx_mft_execute_io(const hx_mft_plan* plan, int direction, int batch,
                       const void* in, int in_dtype, void* out, int out_dtype,
                       double alpha_re, double alpha_im, int epilogue, const void* mask,
                       const void* src, int src_dtype, void* workspace, size_t workspace_bytes, void* stream);
+/* Forward transform of complex64 fields (batch stacked fields of the plan's input grid) times exp(i scale screen)
+ * with screen (ny x nx float32, device, shared by the batch) a phase screen in radians at unit scale: a phase
+ * element (the atmosphere's AtmosphericLayer/MultiLayerAtmosphere forward with scale = 1 / wavelength,
+ * hcipy/atmosphere/atmospheric_model.py:143-151) followed by the transform, with the phase applied while the
+ * first GEMM's operand is sliced.  Split-precision plans only (HX_ERR_INVALID otherwise); the workspace is that
+ * of a forward execute.  The phase screen is applied to complex64 values exactly as hx_phase_apply does. */
+HX_API int hx_mft_execute_phase(const hx_mft_plan* plan, int batch, const void* in, const float* screen,
+                                double scale, void* out, int out_dtype, double alpha_re, double alpha_im, void* ws,
+                                size_t ws_bytes, void* stream);
 
 /* ------------------------------------------------------------------------
  * Lyot coronagraph and its final image in one call.

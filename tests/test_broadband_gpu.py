@@ -132,3 +132,50 @@ def test_captured_dm_probes():
     assert not torch.equal(first, graph(2 * cmd))
     with pytest.raises(ValueError):
         graph(cmd, cmd)
+
+
+def test_phase_screen_fused_into_the_slicing():
+    """With an atmosphere without scintillation as ``pre`` (the element or its bound ``forward``), the split
+    transforms apply its phase while slicing their input (``hx_mft_execute_phase``): the images equal those of the
+    phase kernel followed by the transform (an opaque ``pre`` forces that path) bit for bit, directly,
+    concurrently and from a captured graph that replays the current screens; complex128 fields and the FP32 form
+    keep the separate phase kernel."""
+    from hcipy_gb300 import _lib, workloads
+    w = workloads.broadband_turbulence_workload(pupil_n=96, diameter=2.0, num_wavelengths=4, q=3.3, num_airy=8)
+    pupil, wls, grids = w['pupil'], w['wavelengths'], w['focal_grids']
+    layers = [hg.InfiniteAtmosphericLayer(pupil, hg.Cn_squared_from_fried_parameter(lay['r0'], 500e-9),
+                                          L0=w['L0'], velocity=lay['velocity'], seed=8 + i, dtype=torch.float32)
+              for i, lay in enumerate(w['layers'])]
+    atm = hg.MultiLayerAtmosphere(layers)
+    atm.evolve_until(4 * w['frame_time'])
+    e = torch.from_numpy(w['aperture'].astype(np.complex64)).cuda()
+    kw = dict(focal_length=w['focal_length'], precision='split')
+    fused = hg.BroadbandImager(pupil, wls, grids, pre=atm.forward, **kw)
+    by_element = hg.BroadbandImager(pupil, wls, grids, pre=atm, **kw)
+    plain = hg.BroadbandImager(pupil, wls, grids, pre=lambda wf: atm.forward(wf), **kw)
+    assert fused._phase_screen() is not None and by_element._phase_screen() is not None
+    assert plain._phase_screen() is None
+    for concurrent in (False, True):
+        a = fused.forward(e, concurrent=concurrent)
+        b = plain.forward(e, concurrent=concurrent)
+        c = by_element.forward(e, concurrent=concurrent)
+        torch.cuda.synchronize()
+        for x, y, z in zip(a, b, c):
+            assert torch.equal(x, y) and torch.equal(x, z)
+    fused.capture(e)
+    plain.capture(e)
+    atm.evolve_until(8 * w['frame_time'])
+    for x, y in zip(fused.replay(e), plain.replay(e)):
+        assert torch.equal(x, y)
+    # not fusable: complex128 fields, FP32 transforms
+    prop = fused.props[0]
+    assert not prop.phase_screen_fusable(e.to(torch.complex128), atm.combined_screen(), wls[0])
+    fp32 = hg.FraunhoferPropagator(pupil, grids[0], focal_length=w['focal_length'])
+    assert fp32.forward_phase_screen(e, atm.combined_screen(), 1 / wls[0], wls[0]) is None
+    # the C ABI refuses a plain plan
+    ft = fp32.get_instance_data(pupil, None, wls[0]).fourier_transform
+    plan = ft._plan(torch.complex64)
+    out = torch.empty(grids[0].size, dtype=torch.complex128, device='cuda')
+    rc = _lib.lib().hx_mft_execute_phase(plan.handle, 1, _lib.dptr(e), _lib.dptr(atm.combined_screen()), 1.0,
+                                         _lib.dptr(out), _lib.HX_C128, 1.0, 0.0, None, 0, _lib.stream_handle())
+    assert rc == _lib.HX_ERR_INVALID
