@@ -446,7 +446,8 @@ def run_broadband(args, dev, peaks):
     layers (r0 0.1/0.2/0.3 m, L0 25 m, winds 10/15/25 m/s along x, seeds 5/6/7), 1 ms frames.  A frame evolves the
     layers (extrusions with host-drawn noise, quintic shifts, the summed screen) and replays one CUDA graph that
     holds, per wavelength, the phase of the summed screen and the matrix Fourier transform onto that wavelength's
-    grid; the split GEMMs run with the tiles the autotuner picked during the capture's warm-up."""
+    grid (in the split form the phase is applied while the transform slices its input); the split GEMMs run with
+    the tiles the autotuner picked during the capture's warm-up."""
     import torch
     import hcipy_gb300 as hg
     from hcipy_gb300 import _lib, workloads
