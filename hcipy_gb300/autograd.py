@@ -137,18 +137,19 @@ class LyotFunction(torch.autograd.Function):
         a_bwd = complex(ft._w_out_scalar / (2 * np.pi)**ft.ndim) / inst.norm_factor
         one_minus, stop = lyot._fused_masks(torch.complex64 if ft.precision == 'split' else g.dtype)
         u = g if stop is None else g * stop.conj().to(g.dtype)
+        if ft.precision == 'split':
+            # u - P^H[(1 - M)^* (P^-1)^H u] is the Lyot chain itself with the conjugated mask and alphas and no
+            # stop (P^H and P^-1 share their matrices on uniform grids): one hx_lyot_execute, whose row pass forms
+            # the difference and writes the input's dtype
+            m_conj = one_minus.conj().resolve_conj().contiguous()
+            res = lyot._lyot_call(u, inst, m_conj, None, _conj(a_bwd), _conj(a_fwd), ctx.in_dtype)
+            return res, None, None
         # v = (1 - M)^* . (P^-1)^H u  : forward-direction transform, mask fused in the epilogue
         v = ft._run(u, ft.input_grid, ft.output_grid, _lib.HX_FORWARD, _conj(a_bwd), epilogue=_lib.HX_EPI_MUL,
                     mask=one_minus.conj()).data
-        # E^* = u - P^H v  : adjoint-direction transform, then the subtraction.  On the CUDA cores the subtraction
-        # is fused into the last GEMM's epilogue; the tensor-core GEMM's epilogue runs on few warps per SM, so
-        # there it is a separate full-occupancy elementwise pass.
-        if ft.precision == 'split':
-            t = ft._run(v, ft.output_grid, ft.input_grid, _lib.HX_ADJOINT, _conj(a_fwd)).data
-            res = u.to(t.dtype) - t
-        else:
-            res = ft._run(v, ft.output_grid, ft.input_grid, _lib.HX_ADJOINT, _conj(a_fwd),
-                          epilogue=_lib.HX_EPI_BABINET, src=u).data
+        # E^* = u - P^H v  : adjoint-direction transform with the subtraction fused into the last GEMM's epilogue
+        res = ft._run(v, ft.output_grid, ft.input_grid, _lib.HX_ADJOINT, _conj(a_fwd), epilogue=_lib.HX_EPI_BABINET,
+                      src=u).data
         return res.to(ctx.in_dtype), None, None
 
 

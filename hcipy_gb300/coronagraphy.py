@@ -79,14 +79,19 @@ class LyotCoronagraph(OpticalElement):
     def _lyot_tensor(self, t, inst):
         """The fused chain on a tensor of pupil fields (..., n): one library call."""
         ft = inst.fourier_transform
-        t = t.detach().contiguous()
-        split = ft.precision == 'split'
         one_minus, stop = self._fused_masks(t.dtype)
         a_fwd = complex(ft._w_in_scalar) * inst.norm_factor
         a_bwd = complex(ft._w_out_scalar / (2 * np.pi)**ft.ndim) / inst.norm_factor
+        out_dtype = torch.complex128 if ft.precision == 'split' else t.dtype
+        return self._lyot_call(t, inst, one_minus, stop, a_fwd, a_bwd, out_dtype)
+
+    def _lyot_call(self, t, inst, one_minus, stop, a_fwd, a_bwd, out_dtype):
+        """S (E - a_bwd P^-1[a_fwd P(E) (1 - M)]) for the given masks, alphas and output dtype (hx_lyot_execute)."""
+        ft = inst.fourier_transform
+        t = t.detach().contiguous()
         lead = tuple(t.shape[:-1])
         batch = int(np.prod(lead)) if lead else 1
-        out = torch.empty(lead + (t.shape[-1],), dtype=torch.complex128 if split else t.dtype, device=t.device)
+        out = torch.empty(lead + (t.shape[-1],), dtype=out_dtype, device=t.device)
         if batch == 0:
             return out
         plan = ft._plan(t.dtype)
