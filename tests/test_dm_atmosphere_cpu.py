@@ -139,3 +139,63 @@ def test_scintillation_element_order():
     assert all(isinstance(e, hg.FresnelPropagator) for e in (els[1], els[3]))
     els = hg.MultiLayerAtmosphere([Stub(300.0), Stub(1000.0)], scintillation=True).calculate_propagators()
     assert [getattr(e, 'distance', None) for e in els] == [None, 700.0, None, 300.0]
+
+
+@pytest.mark.parametrize('block', [4, 3])
+def test_actuator_block_lists_reproduce_the_transpose(block):
+    """The plan-time union lists of the blocked DM transpose (blocks of consecutive actuators, the union of their
+    pixels, one weight per actuator of the block and zero where it does not reach): summing weight x gradient
+    over every list in numpy gives M^T g exactly as the CSC product does, for a ragged last block, empty columns
+    and a Gaussian-influence basis."""
+    import scipy.sparse as sp
+    import hcipy_gb300 as hg
+    from hcipy_gb300.kernels import _actuator_blocks
+    rng = np.random.default_rng(block)
+    grid = hg.make_pupil_grid(48, 1)
+    gauss = sp.csc_matrix(hg.make_gaussian_influence_functions(grid, 7, 1 / 7).transformation_matrix)
+    rand = sp.random(500, 23, density=0.1, random_state=3, format='lil')
+    rand[:, 5] = 0  # an actuator that reaches no pixel
+    rand = sp.csc_matrix(rand)
+    rand.eliminate_zeros()
+    for m in (gauss, rand):
+        m.sort_indices()
+        ptr, pix, vals = _actuator_blocks(m, block)
+        vals = vals.reshape(-1, block)
+        nact = m.shape[1]
+        assert ptr.size == -(-nact // block) + 1 and ptr[-1] == pix.size == vals.shape[0]
+        g = rng.standard_normal((3, m.shape[0]))
+        out = np.zeros((3, nact))
+        for b in range(ptr.size - 1):
+            seg = slice(ptr[b], ptr[b + 1])
+            assert np.all(np.diff(pix[seg]) > 0)  # sorted, no repeats
+            for q in range(block):
+                a = b * block + q
+                if a < nact:
+                    out[:, a] = g[:, pix[seg]] @ vals[seg, q]
+        np.testing.assert_allclose(out, g @ m.toarray(), rtol=1e-12, atol=1e-12)
+
+
+def test_broadband_phase_screen_hook_resolution():
+    """BroadbandImager fuses the phase of ``pre`` only when ``pre`` is a pure phase element: the element itself or
+    its bound ``forward``; any other callable keeps the separate phase application (host logic)."""
+    import hcipy_gb300 as hg
+
+    class Screen(object):
+        def __init__(self):
+            self.calls = 0
+
+        def forward(self, wf):
+            return wf
+
+        __call__ = forward
+
+        def _pure_phase_screen(self):
+            self.calls += 1
+            return 'screen'
+
+    s = Screen()
+    pupil = hg.make_pupil_grid(16, 1)
+    grids = [hg.make_focal_grid(2, 4)]
+    for pre, expect in ((s, 'screen'), (s.forward, 'screen'), (lambda wf: s.forward(wf), None), (None, None)):
+        imager = hg.BroadbandImager(pupil, [1.0], grids, pre=pre)
+        assert imager._phase_screen() == expect
