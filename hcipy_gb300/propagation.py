@@ -91,7 +91,8 @@ class FraunhoferPropagator(AgnosticOpticalElement):
         if torch.is_grad_enabled() and (t.requires_grad or screen.requires_grad):
             return False
         n = ft.input_grid.size
-        return t.shape[-1] == n and screen.numel() == n
+        nx = int(ft.input_grid.dims[0])  # the slicing keeps a row of up to 4096 points in registers
+        return t.shape[-1] == n and screen.numel() == n and -(-nx // 32) * 32 <= 4096
 
     def forward_phase_screen(self, e, screen, scale, wavelength=1):
         """``forward`` of the field ``e`` times exp(i scale screen) (a pure phase element such as an atmosphere
