@@ -206,13 +206,17 @@ def efc_step(efc_matrix, field, dark_zone, actuators, gain):
     e = field.data if isinstance(field, Field) else field
     e = torch.as_tensor(e).reshape(-1)
     _check_pixels(e.numel(), int(dz.numel()))
+    idx = _dark_zone_index(dz).to(torch.int32).contiguous()
+    m, _ = _device_matrix(efc_matrix)
+    return _efc_update(m.to(torch.float64).contiguous(), e, idx, actuators, gain)
+
+
+def _efc_update(m, e, idx, actuators, gain):
+    """hx_efc_step with the float64 matrix and the int32 dark-zone indices already on the device."""
     e = _to_device(e)
     if e.dtype not in (torch.complex64, torch.complex128):
         e = e.to(torch.complex128)
     e = e.contiguous()
-    idx = _dark_zone_index(dz).to(torch.int32).contiguous()
-    m, _ = _device_matrix(efc_matrix)
-    m = m.to(torch.float64).contiguous()
     if m.shape[1] != 2 * idx.numel():
         raise ValueError('The EFC matrix has %d columns; the dark zone needs %d.' % (m.shape[1], 2 * idx.numel()))
     a = torch.as_tensor(actuators.data if isinstance(actuators, Field) else actuators)
@@ -231,10 +235,16 @@ def run_efc(measure, dark_zone, efc_matrix, actuators, iterations, gain=0.5):
     (``measure`` takes one (num_modes,) command tensor and returns the focal-plane field) and update them.
     Returns the list of commands applied and the list of fields measured."""
     a = torch.as_tensor(actuators).to(device=_DEVICE, dtype=torch.float64)
+    dz = _mask(dark_zone)
+    idx = _dark_zone_index(dz).to(torch.int32).contiguous()  # once: the loop then never waits on the device
+    m = _device_matrix(efc_matrix)[0].to(torch.float64).contiguous()
     history, fields = [], []
     for _ in range(iterations):
         e = measure(a)
         history.append(a.clone())
         fields.append(e)
-        a = efc_step(efc_matrix, e, dark_zone, a, gain)
+        f = e.data if isinstance(e, Field) else e
+        f = torch.as_tensor(f).reshape(-1)
+        _check_pixels(f.numel(), int(dz.numel()))
+        a = _efc_update(m, f, idx, a, gain)
     return history, fields
