@@ -175,19 +175,21 @@ def poke_jacobian(measure, dark_zone, num_modes, epsilon, num_amplitudes=2, batc
     epsilon, num_modes, num_amplitudes = float(epsilon), int(num_modes), int(num_amplitudes)
     amps = torch.linspace(-epsilon, epsilon, num_amplitudes, dtype=torch.float64)
     var = float(amps.var(unbiased=False))
-    idx = amps_dev = jac = None
+    idx = jac = None
+    amps_dev = amps.to(_DEVICE)
     for start in range(0, num_modes, batch):
         nb = min(batch, num_modes - start)
-        cmds = torch.zeros((nb, num_amplitudes, num_modes), dtype=torch.float64)
-        for i in range(nb):
-            cmds[i, :, start + i] = amps
-        fields = measure(cmds.reshape(nb * num_amplitudes, num_modes).to(device=_DEVICE, dtype=dtype))
+        # the pokes are written on the device (a host-built batch would be a synchronous copy per batch)
+        cmds = torch.zeros((nb, num_amplitudes, num_modes), dtype=torch.float64, device=_DEVICE)
+        rows = torch.arange(nb, device=_DEVICE)
+        cmds[rows, :, start + rows] = amps_dev
+        fields = measure(cmds.reshape(nb * num_amplitudes, num_modes).to(dtype=dtype))
         fields = torch.as_tensor(fields.data if isinstance(fields, Field) else fields)
         if fields.numel() != nb * num_amplitudes * npix:
             raise ValueError('measure() returned %s for %d command vectors of a %d-pixel focal grid.'
                              % (tuple(fields.shape), nb * num_amplitudes, npix))
         if jac is None:
-            idx, amps_dev = _dark_zone_index(dz), amps.to(_DEVICE)
+            idx = _dark_zone_index(dz)
             jac = torch.empty((2 * n_dz, num_modes), dtype=torch.float64, device=_DEVICE)
         f = fields.reshape(nb, num_amplitudes, npix).index_select(2, idx).to(torch.complex128)
         resp = (amps_dev.view(1, -1, 1) * f).sum(1) / var
