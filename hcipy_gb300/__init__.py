@@ -12,10 +12,10 @@ from .optics import (Wavefront, OpticalElement, AgnosticOpticalElement, Apodizer
                      make_agnostic_forward, make_agnostic_backward)
 from .propagation import FraunhoferPropagator, AngularSpectrumPropagator, FresnelPropagator
 from .fft import FastFourierTransform, ChirpZTransform, ZoomFastFourierTransform, FourierFilter
-from .wavefront_sensing import PyramidWavefrontSensorOptics
+from .wavefront_sensing import PyramidWavefrontSensorOptics, ModulatedPyramidWavefrontSensorOptics
 from .graphs import CapturedCall
 from .coronagraphy import LyotCoronagraph, MultiScaleCoronagraph, VortexCoronagraph
-from .deformable_mirror import (ModeBasis, DeformableMirror, make_actuator_positions,
+from .deformable_mirror import (ModeBasis, DeformableMirror, TipTiltMirror, make_actuator_positions,
                                 make_gaussian_influence_functions, find_illuminated_actuators)
 from .atmosphere import (AtmosphericLayer, InfiniteAtmosphericLayer, MultiLayerAtmosphere,
                          Cn_squared_from_fried_parameter, fried_parameter_from_Cn_squared, subpixel_shift,
@@ -35,7 +35,8 @@ __all__ = [
     'Wavefront', 'OpticalElement', 'AgnosticOpticalElement', 'Apodizer', 'PhaseApodizer',
     'make_agnostic_forward', 'make_agnostic_backward',
     'FraunhoferPropagator', 'AngularSpectrumPropagator', 'FresnelPropagator', 'LyotCoronagraph',
-    'MultiScaleCoronagraph', 'VortexCoronagraph', 'PyramidWavefrontSensorOptics', 'SurfaceApodizer',
+    'MultiScaleCoronagraph', 'VortexCoronagraph', 'PyramidWavefrontSensorOptics',
+    'ModulatedPyramidWavefrontSensorOptics', 'SurfaceApodizer', 'TipTiltMirror',
     'CapturedCall', 'HXError',
     'launch_count',
     'FastFourierTransform', 'ChirpZTransform', 'ZoomFastFourierTransform', 'FourierFilter',

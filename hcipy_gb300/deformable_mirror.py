@@ -260,3 +260,15 @@ class DeformableMirror(OpticalElement):
     def backward(self, wavefront):
         """E exp(-2ik S) (deformable_mirror.py:219-238)."""
         return self._reflect(wavefront, -1.0)
+
+
+class TipTiltMirror(DeformableMirror):
+    """A tip-tilt mirror (hcipy/optics/tip_tilt_mirror.py): a deformable mirror whose two modes are the input grid's
+    x and y coordinates, so its two actuators are the surface's slopes along x and y (OPD-controlled, as in the
+    reference).  A tensor of commands of shape (..., 2) reflects the wavefront at every command in one launch."""
+
+    def __init__(self, input_grid, dtype=torch.float32):
+        x, y = _grid_xy(input_grid)
+        super(TipTiltMirror, self).__init__(ModeBasis(np.stack([x, y], axis=1), input_grid), dtype)
+        self.input_grid = input_grid
+        self._actuators = np.zeros((2,))

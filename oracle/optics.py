@@ -51,6 +51,98 @@ def dm_forward(e, surface, wavelength):
     return np.asarray(e) * np.exp(2j * k * np.asarray(surface))
 
 
+def circular_aperture(grid, diameter):
+    """hcipy/aperture/generic.py:31-44: 1 where x^2 + y^2 <= (diameter / 2)^2."""
+    x, y = grid.coords()
+    return ((x**2 + y**2) <= (diameter / 2)**2).astype(np.float64)
+
+
+def surface_apodize(e, sag, n, wavelength):
+    """hcipy/optics/apodization.py:88-93: E * exp(i (n - 1) sag k)."""
+    return np.asarray(e) * np.exp(1j * (n - 1) * np.asarray(sag) * (2 * np.pi / wavelength))
+
+
+def supersampled_mean(fn, grid, oversampling):
+    """hcipy/field/util.py:651-690 for a separated grid: the mean of fn over oversampling^2 dithered copies of the
+    grid, each axis dithered by (i + 1/2) / oversampling - 1/2 of its local spacing (central differences inside,
+    one-sided at the ends), dither points taken with x fastest."""
+    from .grids import make_uniform_grid
+    dithers = make_uniform_grid([oversampling, oversampling], 1)
+    dxs, dys = dithers.coords()
+    axes = grid.separated_coords
+    spacing = [np.concatenate(([c[1] - c[0]], (c[2:] - c[:-2]) / 2., [c[-1] - c[-2]])) for c in axes]
+    acc = 0
+    for tx, ty in zip(dxs, dys):
+        x = axes[0] + float(tx) * spacing[0]
+        y = axes[1] + float(ty) * spacing[1]
+        xx, yy = np.meshgrid(x, y)
+        acc = acc + fn(xx.ravel(), yy.ravel())
+    return acc / len(dxs)
+
+
+class PyramidOptics(object):
+    """hcipy/wavefront_sensing/pyramid.py:94-181: lens, circular field stop, glass pyramid (SurfaceApodizer), lens."""
+
+    def __init__(self, pupil, out_grid, separation, pupil_diameter, wavelength_0, refractive_index):
+        from .grids import make_pupil_grid
+        d_in = pupil.delta * pupil.dims
+        d_out = out_grid.delta * out_grid.dims
+        q = np.ceil(max(np.max(d_out / d_in), 2))  # pyramid.py:129-135
+        self.num_airy = np.max(pupil.shape) / 2
+        num_pixels = 2 * int(self.num_airy * q)
+        self.focal = make_pupil_grid(num_pixels, 2 * (wavelength_0 / pupil_diameter) * self.num_airy)
+        self.pupil, self.out_grid = pupil, out_grid
+        self.separation, self.wavelength_0, self.refractive_index = separation, wavelength_0, refractive_index
+        self.stop = circular_aperture(self.focal, 2 * self.num_airy * wavelength_0 / pupil_diameter)
+        self.sag = self.sag_function(*self.focal.coords())
+
+    def sag_function(self, x, y):
+        """pyramid.py:148 (and :54-55): -separation / (2 (n(lambda_0) - 1)) (|x| + |y|)."""
+        return -self.separation / (2 * (self.refractive_index(self.wavelength_0) - 1)) * (np.abs(x) + np.abs(y))
+
+    def to_focal(self, e, wavelength):
+        """pyramid.py:176: the first lens and the field stop."""
+        return fraunhofer_forward(e, self.pupil, self.focal, wavelength) * self.stop
+
+    def forward(self, e, wavelength, sag=None):
+        """pyramid.py:175-181, with another pyramid sag when given."""
+        f = surface_apodize(self.to_focal(e, wavelength), self.sag if sag is None else sag,
+                            self.refractive_index(wavelength), wavelength)
+        return fraunhofer_forward(f, self.focal, self.out_grid, wavelength)
+
+
+def tip_tilt_forward(e, pupil, command, wavelength):
+    """hcipy/optics/tip_tilt_mirror.py with deformable_mirror.py:200-217: the surface x a_0 + y a_1 reflected,
+    E exp(2 i k S)."""
+    x, y = pupil.coords()
+    return dm_forward(e, x * command[0] + y * command[1], wavelength)
+
+
+def modulation_positions(modulation, num_steps):
+    """hcipy/wavefront_sensing/pyramid.py:39-44."""
+    theta = np.linspace(0, 2 * np.pi, num_steps, endpoint=False)
+    return np.stack((modulation / 2 * np.cos(theta), modulation / 2 * np.sin(theta)), axis=1)
+
+
+def modulated_pyramid_forward(optics, e, wavelength, modulation, num_steps, fast=False):
+    """hcipy/wavefront_sensing/pyramid.py:65-88, both methods: (num_steps, npix_out).
+
+    Tip-tilt method: the pyramid optics applied to the input tilted to each modulation position.  Fast method:
+    one focal-plane field through the stop, then per step the pyramid sag on the focal grid shifted by twice the
+    position, sampled 4x per axis and averaged (pyramid.py:50-63), and the second lens."""
+    pos = modulation_positions(modulation, num_steps)
+    if not fast:
+        return np.stack([optics.forward(tip_tilt_forward(e, optics.pupil, p, wavelength), wavelength) for p in pos])
+    focal = optics.to_focal(e, wavelength)
+    n = optics.refractive_index(wavelength)
+    out = []
+    for p in pos:
+        sag = supersampled_mean(optics.sag_function, optics.focal.shifted(2 * p), 4)
+        out.append(fraunhofer_forward(surface_apodize(focal, sag, n, wavelength), optics.focal, optics.out_grid,
+                                      wavelength))
+    return np.stack(out)
+
+
 def intensity(e):
     """hcipy/optics/wavefront.py:113-143 scalar branch."""
     return np.abs(e)**2

@@ -285,6 +285,34 @@ def make_pyramid_case(hp, out):
     out['pyramid'] = rec
 
 
+def make_modulated_pyramid_case(hp, out):
+    """ModulatedPyramidWavefrontSensorOptics (hcipy/wavefront_sensing/pyramid.py:10-91): 6 modulation steps of
+    radius 3 lambda/D, the tip-tilt form at one wavelength and the shifted-pyramid form at two; TipTiltMirror
+    (hcipy/optics/tip_tilt_mirror.py) alone for one command."""
+    rng = np.random.default_rng(53)
+    pupil = hp.make_pupil_grid(32, 1.0)
+    wfs_grid = hp.make_pupil_grid(40, 2.0)
+    pwfs = hp.PyramidWavefrontSensorOptics(pupil, wfs_grid, separation=1.0, pupil_diameter=1.0, wavelength_0=1.0,
+                                           refractive_index=lambda wl: 1.5 + 0.01 * (wl - 1.0))
+    aperture = hp.make_circular_aperture(1.0)(pupil)
+    e = aperture * np.exp(0.2j * rng.standard_normal(pupil.size))
+    rec = {'E': e, 'modulation': np.float64(3.0), 'num_steps': np.int64(6)}
+    slow = hp.ModulatedPyramidWavefrontSensorOptics(pwfs, 3.0, num_steps=6)
+    rec['positions'] = np.asarray(slow.modulation_positions.points)
+    rec['slow'] = np.stack([np.asarray(w.electric_field) for w in slow.forward(hp.Wavefront(hp.Field(e, pupil), 1.0))])
+    fast = hp.ModulatedPyramidWavefrontSensorOptics(pwfs, 3.0, num_steps=6, fast_modulation_method=True)
+    for k, wl in enumerate((1.0, 1.2)):
+        wfs = fast.forward(hp.Wavefront(hp.Field(e, pupil), wl))
+        rec['fast_%d' % k] = np.stack([np.asarray(w.electric_field) for w in wfs])
+        rec['wavelength_%d' % k] = np.float64(wl)
+    rec['fast_surface_3'] = np.asarray(fast._pyramid_apodizers[3].surface_sag)
+    ttm = hp.TipTiltMirror(pupil)
+    ttm.actuators = np.array([2e-3, -1e-3])
+    rec['tip_tilt_command'] = np.asarray(ttm.actuators)
+    rec['tip_tilt'] = np.asarray(ttm.forward(hp.Wavefront(hp.Field(e, pupil), 0.8)).electric_field)
+    out['modulated_pyramid'] = rec
+
+
 def make_lyot_case(hp, out):
     """A 128^2 pupil Lyot chain: focal-plane mask radius 4 lambda/D on a q=8 num_airy=8 grid."""
     pupil = hp.make_pupil_grid(128, 1)
@@ -498,7 +526,7 @@ def save(out):
 
 
 CASES = ['mft_cases', 'fraunhofer_cfg1', 'fft_cases', 'czt_cases', 'asp_cases', 'fresnel_cases', 'vortex_cases',
-         'pyramid_case', 'lyot_case', 'subpixel_cases', 'atmosphere_case', 'dm_case', 'efc_case', 'pickle_case',
+         'pyramid_case', 'modulated_pyramid_case', 'lyot_case', 'subpixel_cases', 'atmosphere_case', 'dm_case', 'efc_case', 'pickle_case',
          'spectral_noise_case']
 
 

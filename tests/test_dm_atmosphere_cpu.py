@@ -199,3 +199,25 @@ def test_broadband_phase_screen_hook_resolution():
     for pre, expect in ((s, 'screen'), (s.forward, 'screen'), (lambda wf: s.forward(wf), None), (None, None)):
         imager = hg.BroadbandImager(pupil, [1.0], grids, pre=pre)
         assert imager._phase_screen() == expect
+
+
+def test_modulated_pyramid_plan_time_host_data():
+    """The modulated pyramid's plan-time data, built on the host: the modulation positions and the shifted
+    pyramid's supersampled sags equal the reference's bit for bit; the tip-tilt mirror's modes are the grid's x
+    and y; backward is refused as in the reference."""
+    import hcipy_gb300 as hg
+    g = load_golden('modulated_pyramid')
+    pupil = hg.make_pupil_grid(32, 1.0)
+    pwfs = hg.PyramidWavefrontSensorOptics(pupil, hg.make_pupil_grid(40, 2.0), separation=1.0, pupil_diameter=1.0,
+                                           wavelength_0=1.0, refractive_index=lambda wl: 1.5 + 0.01 * (wl - 1.0))
+    mod = hg.ModulatedPyramidWavefrontSensorOptics(pwfs, float(g['modulation']), num_steps=int(g['num_steps']),
+                                                   fast_modulation_method=True)
+    assert np.array_equal(mod.modulation_positions.points, g['positions'])
+    assert np.array_equal(mod._sags[3], g['fast_surface_3'])
+    assert mod._sags.shape == (int(g['num_steps']), pwfs.focal_grid.size)
+    slow = hg.ModulatedPyramidWavefrontSensorOptics(pwfs, 3.0, num_steps=5)
+    assert slow._sags is None and len(slow.modulation_positions.points) == 5
+    m = slow.tip_tilt_mirror.influence_functions.transformation_matrix
+    assert np.array_equal(m[:, 0], pupil.x) and np.array_equal(m[:, 1], pupil.y)
+    with pytest.raises(RuntimeError):
+        slow.backward(None)

@@ -231,3 +231,34 @@ def test_infinite_layer_initial_screen_oracle():
     assert rel_err(screen, g['screen0']) < 1e-12
     noise = rng.normal(0, np.sqrt(float(g['cn2'])), size=g['noise_0'].shape[1])
     assert np.array_equal(noise, g['noise_0'][0])
+
+
+def _pyramid_optics(pupil_n, wfs_n):
+    return optics.PyramidOptics(grids.make_pupil_grid(pupil_n, 1.0), grids.make_pupil_grid(wfs_n, 2.0), 1.0, 1.0, 1.0,
+                                lambda wl: 1.5 + 0.01 * (wl - 1.0))
+
+
+def test_pyramid_oracle():
+    """The pyramid optics (hcipy/wavefront_sensing/pyramid.py:94-181) at two wavelengths of a dispersive glass."""
+    g = load_golden('pyramid')
+    po = _pyramid_optics(48, 96)
+    np.testing.assert_array_equal(po.focal.dims, g['focal_dims'])
+    for k in range(2):
+        assert rel_err(po.forward(g['E'], float(g['wavelength_%d' % k])), g['fwd_%d' % k]) < 1e-12, k
+
+
+def test_modulated_pyramid_oracle():
+    """The modulated pyramid (pyramid.py:10-91): both methods, the shifted pyramid's supersampled sag bit for bit,
+    and the tip-tilt mirror (hcipy/optics/tip_tilt_mirror.py)."""
+    g = load_golden('modulated_pyramid')
+    po = _pyramid_optics(32, 40)
+    mod, steps = float(g['modulation']), int(g['num_steps'])
+    assert np.array_equal(optics.modulation_positions(mod, steps), g['positions'])
+    assert rel_err(optics.modulated_pyramid_forward(po, g['E'], 1.0, mod, steps), g['slow']) < 1e-12
+    for k in range(2):
+        out = optics.modulated_pyramid_forward(po, g['E'], float(g['wavelength_%d' % k]), mod, steps, fast=True)
+        assert rel_err(out, g['fast_%d' % k]) < 1e-12, k
+    sag = optics.supersampled_mean(po.sag_function, po.focal.shifted(2 * g['positions'][3]), 4)
+    assert np.array_equal(sag, g['fast_surface_3'])
+    pupil = grids.make_pupil_grid(32, 1.0)
+    assert rel_err(optics.tip_tilt_forward(g['E'], pupil, g['tip_tilt_command'], 0.8), g['tip_tilt']) < 1e-14
