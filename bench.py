@@ -873,6 +873,56 @@ def run_small_fraunhofer(args, dev, peaks):
     return out
 
 
+def run_modulated_pyramid(args, dev):
+    """The modulated pyramid wavefront sensor: a 256^2 pupil (Zernike 2-21 at 0.5 rad RMS) through 12 modulation
+    steps of radius 3 lambda/D onto a 256^2 sensor plane of twice the pupil's extent (512^2 focal grid, q = 2),
+    complex64 on the FP32 transforms; the tip-tilt method (the reference's default: every step tilted, then two
+    transforms) and the shifted-pyramid method (one transform, a phase per step, one transform).  Frames/s with
+    Python launches, the steps against the float64 oracle, and the oracle port timed on the host for one frame."""
+    import torch
+    import hcipy_gb300 as hg
+    from hcipy_gb300 import workloads
+    from oracle import optics
+    from oracle.grids import make_pupil_grid as o_pupil
+    n, steps, mod = 256, 12, 3.0
+    pupil, wfs_grid = hg.make_pupil_grid(n, 1.0), hg.make_pupil_grid(n, 2.0)
+    ap = workloads.circular_aperture(pupil, 1.0)
+    e_h = ap * np.exp(1j * workloads.zernike_phase(pupil, 1.0, 2, 21, 0.5, 3))
+    e = torch.from_numpy(e_h.astype(np.complex64)).to(dev)
+    pwfs = hg.PyramidWavefrontSensorOptics(pupil, wfs_grid)
+    po = optics.PyramidOptics(o_pupil(n, 1.0), o_pupil(n, 2.0), 1.0, 1.0, 1, lambda x: 1.5)
+    nf = int(pwfs.focal_grid.dims[0])
+    cmacs = steps * (workloads.mft_complex_macs(n, n, nf, nf) + workloads.mft_complex_macs(nf, nf, n, n))
+    out = {'workload': '256^2 pupil, Zernike 2-21 at 0.5 rad RMS -> 12 modulation steps of 3 lambda/D -> 512^2 '
+                       'focal grid -> 256^2 sensor plane, complex64', 'complex_macs_per_frame_tip_tilt': int(cmacs)}
+    for name, fast in (('tip_tilt', False), ('shifted_pyramid', True)):
+        m = hg.ModulatedPyramidWavefrontSensorOptics(pwfs, mod, num_steps=steps, fast_modulation_method=fast)
+        wf = hg.Wavefront(hg.Field(e, pupil), 1.0)
+        for _ in range(3):
+            res = m.forward(wf)
+        torch.cuda.synchronize()
+        k = 30
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(k):
+            m.forward(wf)
+        t1.record()
+        t1.synchronize()
+        ms = t0.elapsed_time(t1) / k
+        got = np.stack([w.electric_field.numpy() for w in res]).astype(np.complex128)
+        ref = optics.modulated_pyramid_forward(po, e_h.astype(np.complex64).astype(np.complex128), 1.0, mod, steps,
+                                               fast=fast)
+        out[name] = {'frames_per_s': 1e3 / ms, 'ms_per_frame': ms, 'steps_per_s': steps * 1e3 / ms,
+                     'rel_err_vs_fp64': float(np.linalg.norm(got - ref) / np.linalg.norm(ref))}
+        if not fast:
+            c0 = time.perf_counter()
+            optics.modulated_pyramid_forward(po, e_h, 1.0, mod, steps)
+            cpu_s = time.perf_counter() - c0
+            out['cpu_baseline'] = {'frames_per_s': 1 / cpu_s, 'cores': host_cores(), 'kind': 'port',
+                                   'sample': 'one frame of the tip-tilt method through the numpy port, complex128'}
+    return out
+
+
 def run_fft_family(args, dev, peaks):
     """A 1024^2 pupil of 8 m behind a von Karman screen (r0 0.15 m, L0 20 m) at 1.6 um: the zero-padded FFT to
     4096^2 (q=4) and angular-spectrum propagation over 0.5 m and 5 m (2048^2 padded).  Per-call time with CUDA
@@ -1178,6 +1228,7 @@ def run_ours(args, rank, world, dist):
         line['dm_probes'] = run_dm_probes(args, dev)
         line['efc'] = run_efc(args, dev)
         line['fraunhofer_256'] = run_small_fraunhofer(args, dev, peaks)
+        line['modulated_pyramid_256'] = run_modulated_pyramid(args, dev)
         line['fft_family_1024'] = run_fft_family(args, dev, peaks)
     # The accuracy conditions of the metric and the side-by-side rates come last, so that a reader who keeps only
     # the end of the line (or of stderr, where the same summary is printed) still has them.
