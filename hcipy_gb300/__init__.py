@@ -14,7 +14,7 @@ from .propagation import FraunhoferPropagator, AngularSpectrumPropagator, Fresne
 from .fft import FastFourierTransform, ChirpZTransform, ZoomFastFourierTransform, FourierFilter
 from .wavefront_sensing import PyramidWavefrontSensorOptics, ModulatedPyramidWavefrontSensorOptics
 from .graphs import CapturedCall
-from .coronagraphy import LyotCoronagraph, MultiScaleCoronagraph, VortexCoronagraph
+from .coronagraphy import LyotCoronagraph, MultiScaleCoronagraph, VortexCoronagraph, VectorVortexCoronagraph
 from .deformable_mirror import (ModeBasis, DeformableMirror, TipTiltMirror, make_actuator_positions,
                                 make_gaussian_influence_functions, find_illuminated_actuators)
 from .atmosphere import (AtmosphericLayer, InfiniteAtmosphericLayer, MultiLayerAtmosphere,
@@ -35,7 +35,7 @@ __all__ = [
     'Wavefront', 'OpticalElement', 'AgnosticOpticalElement', 'Apodizer', 'PhaseApodizer',
     'make_agnostic_forward', 'make_agnostic_backward',
     'FraunhoferPropagator', 'AngularSpectrumPropagator', 'FresnelPropagator', 'LyotCoronagraph',
-    'MultiScaleCoronagraph', 'VortexCoronagraph', 'PyramidWavefrontSensorOptics',
+    'MultiScaleCoronagraph', 'VortexCoronagraph', 'VectorVortexCoronagraph', 'PyramidWavefrontSensorOptics',
     'ModulatedPyramidWavefrontSensorOptics', 'SurfaceApodizer', 'TipTiltMirror',
     'CapturedCall', 'HXError',
     'launch_count',

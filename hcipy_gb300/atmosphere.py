@@ -344,7 +344,7 @@ class AtmosphericLayer(OpticalElement):
             out = phase_apply(e, s, sign / wf.wavelength)
         else:
             out = apply_phase(e, s, sign / wf.wavelength)
-        return Wavefront(Field(out, wf.electric_field.grid), wf.wavelength)
+        return wf._carry(Field(out, wf.electric_field.grid))
 
     def forward(self, wf):
         return self._apply(wf, 1.0)
@@ -747,7 +747,7 @@ class MultiLayerAtmosphere(OpticalElement):
             out = phase_apply(e, s, sign / wf.wavelength)
         else:
             out = apply_phase(e, s, sign / wf.wavelength)
-        return Wavefront(Field(out, wf.electric_field.grid), wf.wavelength)
+        return wf._carry(Field(out, wf.electric_field.grid))
 
     def forward(self, wavefront):
         if self._scintillation:

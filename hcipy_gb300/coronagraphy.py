@@ -1,11 +1,13 @@
-"""Lyot coronagraph (hcipy/coronagraphy/lyot.py:7-122) with the Babinet chain fused into the MFT GEMMs."""
+"""Coronagraphs: the Lyot coronagraph (hcipy/coronagraphy/lyot.py:7-122) with the Babinet chain fused into the MFT
+GEMMs, and the multi-scale, vortex and vector-vortex coronagraphs (multi_scale.py, vortex.py)."""
 import numpy as np
 import torch
 
 from . import _lib
 from .field import Field, as_tensor
 from .fourier import MatrixFourierTransform
-from .optics import OpticalElement, Apodizer, Wavefront
+from .optics import (AgnosticOpticalElement, OpticalElement, Apodizer, Wavefront, make_agnostic_backward,
+                     make_agnostic_forward)
 from .propagation import FraunhoferPropagator
 
 
@@ -74,7 +76,7 @@ class LyotCoronagraph(OpticalElement):
             out = LyotFunction.apply(t, self, inst)
         else:
             out = self._lyot_tensor(t, inst)
-        return Wavefront(Field(out, e.grid), wavefront.wavelength)
+        return wavefront._carry(Field(out, e.grid))
 
     def _lyot_tensor(self, t, inst):
         """The fused chain on a tensor of pupil fields (..., n): one library call."""
@@ -109,9 +111,9 @@ class LyotCoronagraph(OpticalElement):
     def _forward_unfused(self, wavefront):
         wf_foc = self.prop.forward(wavefront)
         masked = self.focal_plane_mask.forward(wf_foc).electric_field
-        wf_foc = Wavefront(wf_foc.electric_field - masked, wavefront.wavelength)
+        wf_foc = wavefront._carry(wf_foc.electric_field - masked)
         lyot = self.prop.backward(wf_foc)
-        lyot = Wavefront(wavefront.electric_field - lyot.electric_field, wavefront.wavelength)
+        lyot = wavefront._carry(wavefront.electric_field - lyot.electric_field)
         if self.lyot_stop is not None:
             lyot = self.lyot_stop.forward(lyot)
         return lyot
@@ -121,9 +123,9 @@ class LyotCoronagraph(OpticalElement):
         wf = self.lyot_stop.backward(wavefront) if self.lyot_stop is not None else wavefront
         wf_foc = self.prop.forward(wf)
         masked = self.focal_plane_mask.backward(wf_foc).electric_field
-        wf_foc = Wavefront(wf_foc.electric_field - masked, wavefront.wavelength)
+        wf_foc = wavefront._carry(wf_foc.electric_field - masked)
         pup = self.prop.backward(wf_foc)
-        return Wavefront(wf.electric_field - pup.electric_field, wavefront.wavelength)
+        return wavefront._carry(wf.electric_field - pup.electric_field)
 
 
 class MultiScaleCoronagraph(OpticalElement):
@@ -207,7 +209,7 @@ class MultiScaleCoronagraph(OpticalElement):
     def forward(self, wavefront):
         """multi_scale.py:95-128."""
         e = as_tensor(wavefront.electric_field).contiguous()
-        lyot = Wavefront(Field(self._propagate(e, False), self.input_grid), wavefront.wavelength)
+        lyot = wavefront._carry(Field(self._propagate(e, False), self.input_grid))
         if self.lyot_stop is not None:
             lyot = self.lyot_stop.forward(lyot)
         return lyot
@@ -217,7 +219,7 @@ class MultiScaleCoronagraph(OpticalElement):
         if self.lyot_stop is not None:
             wavefront = self.lyot_stop.backward(wavefront)
         e = as_tensor(wavefront.electric_field).contiguous()
-        return Wavefront(Field(self._propagate(e, True), self.input_grid), wavefront.wavelength)
+        return wavefront._carry(Field(self._propagate(e, True), self.input_grid))
 
 
 class VortexCoronagraph(MultiScaleCoronagraph):
@@ -233,3 +235,101 @@ class VortexCoronagraph(MultiScaleCoronagraph):
             return np.exp(1j * charge * np.arctan2(y, x)) * (1 - centre)
 
         MultiScaleCoronagraph.__init__(self, input_grid, complex_mask, lyot_stop, q, scaling_factor, window_size)
+
+
+class VectorVortexCoronagraph(AgnosticOpticalElement):
+    """A vector vortex of ``charge`` (hcipy/coronagraphy/vortex.py:17-246): a linear retarder in the focal plane whose
+    fast axis turns as charge / 2 times the azimuth, resolved on the multi-scale focal grids; same arguments.
+
+    The retarder's Jones matrix (polarization.py:141-160, retardance G, fast-axis angle a)
+    j11 = e^{iG/2} cos^2 a + e^{-iG/2} sin^2 a,  j12 = j21 = (e^{iG/2} - e^{-iG/2}) cos a sin a,
+    j22 = e^{iG/2} sin^2 a + e^{-iG/2} cos^2 a
+    is symmetric, and each step of the multi-scale construction (the central pinhole, the Tukey windows, the
+    subtraction of the coarser levels) and of the propagation acts on every entry alone.  The coronagraph is
+    therefore three scalar multi-scale coronagraphs C11, C12, C22, one per distinct entry: an unpolarised field E
+    gives the Lyot-plane Jones matrix [[C11 E, C12 E], [C12 E, C22 E]] (the reference's E times the identity,
+    Stokes vector (1, 0, 0, 0)); a polarised wavefront's (2, 2, n) Jones matrix gives L_ik = sum_j C_ij(E_jk), each
+    C applied to a batch of two fields.  ``backward`` applies the conjugate masks, which for a symmetric J is the
+    conjugate transpose the reference applies.  The propagation is at unit wavelength (the masks are in lambda/D);
+    the retardance may depend on the wavelength.
+    """
+
+    def __init__(self, charge, lyot_stop=None, phase_retardation=np.pi, q=1024, scaling_factor=4, window_size=32):
+        self.charge = charge
+        if hasattr(lyot_stop, 'forward') or lyot_stop is None:
+            self.lyot_stop = lyot_stop
+        else:
+            self.lyot_stop = Apodizer(lyot_stop)
+        self.phase_retardation = phase_retardation
+        self.q = q
+        self.scaling_factor = scaling_factor
+        self.window_size = window_size
+        self._entries = {}
+        AgnosticOpticalElement.__init__(self)
+
+    def _jones_entry(self, retardance, which):
+        charge = self.charge
+
+        def mask(grid):
+            x, y = grid.points_list()
+            a = charge / 2 * np.arctan2(y, x)
+            plus, minus = np.exp(1j * retardance / 2), np.exp(-1j * retardance / 2)
+            if which == 'j11':
+                j = plus * np.cos(a)**2 + minus * np.sin(a)**2
+            elif which == 'j22':
+                j = plus * np.sin(a)**2 + minus * np.cos(a)**2
+            else:
+                j = (plus - minus) * np.cos(a) * np.sin(a)
+            centre = np.hypot(x, y) <= 0.5e-9  # make_circular_aperture(1e-9), boundary inclusive
+            return j * (1 - centre)
+        return mask
+
+    def make_instance(self, instance_data, input_grid, output_grid, wavelength):
+        from .field import grid_key
+        retardance = float(self.evaluate_parameter(self.phase_retardation, input_grid, output_grid, wavelength))
+        key = (grid_key(input_grid), retardance)
+        entries = self._entries.get(key)
+        if entries is None:
+            # the same retardance at another wavelength reuses the three coronagraphs
+            entries = tuple(MultiScaleCoronagraph(input_grid, self._jones_entry(retardance, w), None, self.q,
+                                                  self.scaling_factor, self.window_size)
+                            for w in ('j11', 'j12', 'j22'))
+            self._entries[key] = entries
+        instance_data.entries = entries
+
+    def get_input_grid(self, output_grid, wavelength):
+        return output_grid
+
+    def get_output_grid(self, input_grid, wavelength):
+        return input_grid
+
+    def _propagate(self, entries, wavefront, conj):
+        c11, c12, c22 = entries
+        e = as_tensor(wavefront.electric_field).contiguous()
+        if wavefront.is_polarized:
+            stokes = wavefront.input_stokes_vector
+            row0 = c11._propagate(e[0], conj) + c12._propagate(e[1], conj)
+            row1 = c12._propagate(e[0], conj) + c22._propagate(e[1], conj)
+            out = torch.stack((row0, row1))
+        else:
+            if e.dim() != 1:
+                raise ValueError('The vector vortex takes one scalar field or a polarised wavefront.')
+            stokes = (1, 0, 0, 0)
+            j11, j12, j22 = (c._propagate(e, conj) for c in entries)
+            out = torch.stack((torch.stack((j11, j12)), torch.stack((j12, j22))))
+        return Wavefront(Field(out, wavefront.electric_field.grid), wavefront.wavelength, stokes)
+
+    @make_agnostic_forward
+    def forward(self, instance_data, wavefront):
+        """vortex.py:160-202."""
+        lyot = self._propagate(instance_data.entries, wavefront, False)
+        if self.lyot_stop is not None:
+            lyot = self.lyot_stop.forward(lyot)
+        return lyot
+
+    @make_agnostic_backward
+    def backward(self, instance_data, wavefront):
+        """vortex.py:204-246."""
+        if self.lyot_stop is not None:
+            wavefront = self.lyot_stop.backward(wavefront)
+        return self._propagate(instance_data.entries, wavefront, True)

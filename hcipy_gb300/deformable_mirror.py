@@ -251,7 +251,7 @@ class DeformableMirror(OpticalElement):
         else:
             from .kernels import apply_phase
             out = apply_phase(e, s, scale)
-        return Wavefront(Field(out, wavefront.electric_field.grid), wavefront.wavelength)
+        return wavefront._carry(Field(out, wavefront.electric_field.grid))
 
     def forward(self, wavefront):
         """E exp(2ik S) (deformable_mirror.py:200-217)."""

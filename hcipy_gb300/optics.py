@@ -18,14 +18,33 @@ from .field import Field, as_tensor, grid_key
 
 
 class Wavefront(object):
-    """A scalar wavefront: a device Field of the electric field and a wavelength."""
+    """A wavefront: a device Field of the electric field and a wavelength (hcipy/optics/wavefront.py).
+
+    Leading axes of the field are a batch of scalar fields.  With ``input_stokes_vector`` (I, Q, U, V) the wavefront
+    is partially polarised (wavefront.py:47-66): its field is the 2x2 Jones matrix of the system at every point,
+    shape (2, 2, n), which a scalar field becomes as E times the identity; the Stokes parameters of the light are
+    then the Mueller matrix of that Jones matrix applied to the input Stokes vector.
+    """
 
     def __init__(self, electric_field, wavelength=1, input_stokes_vector=None):
+        stokes = None
         if input_stokes_vector is not None:
-            raise NotImplementedError('Polarised wavefronts are not part of the GPU diffraction path.')
+            if not hasattr(electric_field, 'grid'):
+                raise ValueError('The electric field must be a Field.')
+            t = as_tensor(electric_field)
+            if t.dim() == 1:
+                z = torch.zeros_like(t)
+                t = torch.stack((torch.stack((t, z)), torch.stack((z, t))))
+            elif tuple(t.shape[:-1]) != (2, 2):
+                raise ValueError('When supplying a Stokes vector, the electric field must be either a scalar or '
+                                 '2-tensor field.')
+            electric_field = Field(t, electric_field.grid)
+            stokes = np.array(input_stokes_vector, dtype=np.float64)
+            if stokes.shape != (4,):
+                raise ValueError('A Stokes vector has four components (I, Q, U, V).')
         self.electric_field = electric_field
         self.wavelength = wavelength
-        self._input_stokes_vector = None
+        self._input_stokes_vector = stokes
 
     @property
     def electric_field(self):
@@ -45,7 +64,18 @@ class Wavefront(object):
 
     @property
     def input_stokes_vector(self):
+        """The Stokes vector of the light that the Jones matrices act on (None for a scalar wavefront)."""
         return self._input_stokes_vector
+
+    @property
+    def is_polarized(self):
+        return self._input_stokes_vector is not None
+
+    is_partially_polarized = is_polarized
+
+    @property
+    def is_scalar(self):
+        return self._input_stokes_vector is None
 
     @property
     def wavenumber(self):
@@ -56,14 +86,90 @@ class Wavefront(object):
         return self._electric_field.grid
 
     def copy(self):
-        return Wavefront(self._electric_field.copy(), self.wavelength)
+        return Wavefront(self._electric_field.copy(), self.wavelength, self._input_stokes_vector)
+
+    def _carry(self, field):
+        """A wavefront of ``field`` with this wavefront's wavelength and input Stokes vector."""
+        return Wavefront(field, self.wavelength, self._input_stokes_vector)
+
+    def _stokes(self):
+        """(I, Q, U, V) of a polarised wavefront: 1/2 M s, M the Mueller matrix of the Jones matrix
+        J = [[x, y], [z, w]] at every point (written with the products x y*, z w*, ... of its entries), s the
+        input Stokes vector (wavefront.py:103-235)."""
+        e = self._electric_field.data
+        x, y, z, w = e[0, 0], e[0, 1], e[1, 0], e[1, 1]
+        ax, ay, az, aw = (t.real * t.real + t.imag * t.imag for t in (x, y, z, w))
+        xy, zw = x * y.conj(), z * w.conj()
+        xz, yw = x * z.conj(), y * w.conj()
+        xw, yz = x * w.conj(), y * z.conj()
+        rows = (
+            (ax + ay + az + aw, ax - ay + az - aw, 2 * (xy + zw).real, 2 * (xy + zw).imag),
+            (ax + ay - az - aw, ax - ay - az + aw, 2 * (xy - zw).real, 2 * (xy - zw).imag),
+            (2 * (xz + yw).real, 2 * (xz - yw).real, 2 * (xw + yz).real, 2 * (xw - yz).imag),
+            (-2 * (xz + yw).imag, -2 * (xz - yw).imag, -2 * (xw + yz).imag, 2 * (xw - yz).real),
+        )
+        s = [float(v) for v in self._input_stokes_vector]
+        return [0.5 * (r[0] * s[0] + r[1] * s[1] + r[2] * s[2] + r[3] * s[3]) for r in rows]
 
     @property
-    def intensity(self):
+    def I(self):  # noqa: N802
+        if self.is_polarized:
+            return Field(self._stokes()[0], self.grid)
         e = self._electric_field.data
         return Field(e.real * e.real + e.imag * e.imag, self.grid)
 
-    I = intensity  # noqa: E741
+    intensity = I
+
+    def _stokes_part(self, k):
+        if self.is_polarized:
+            return Field(self._stokes()[k], self.grid)
+        e = self._electric_field.data
+        return Field(torch.zeros(e.shape, dtype=e.real.dtype, device=e.device), self.grid)
+
+    @property
+    def Q(self):  # noqa: N802
+        return self._stokes_part(1)
+
+    @property
+    def U(self):  # noqa: N802
+        return self._stokes_part(2)
+
+    @property
+    def V(self):  # noqa: N802
+        return self._stokes_part(3)
+
+    @property
+    def stokes_vector(self):
+        """(4, n): I, Q, U, V (a scalar wavefront is unpolarised: I = |E|^2, the rest 0)."""
+        if self.is_polarized:
+            return Field(torch.stack(self._stokes()), self.grid)
+        i = self.I.data
+        out = torch.zeros(tuple(i.shape[:-1]) + (4, i.shape[-1]), dtype=i.dtype, device=i.device)
+        out[..., 0, :] = i
+        return Field(out, self.grid)
+
+    @property
+    def degree_of_polarization(self):
+        i, q, u, v = self.I.data, self.Q.data, self.U.data, self.V.data
+        return Field(torch.sqrt(q**2 + u**2 + v**2) / i, self.grid)
+
+    @property
+    def degree_of_linear_polarization(self):
+        i, q, u = self.I.data, self.Q.data, self.U.data
+        return Field(torch.sqrt(q**2 + u**2) / i, self.grid)
+
+    @property
+    def angle_of_linear_polarization(self):
+        return Field(0.5 * torch.atan2(self.U.data, self.Q.data), self.grid)
+
+    @property
+    def degree_of_circular_polarization(self):
+        return Field(self.V.data / self.I.data, self.grid)
+
+    @property
+    def ellipticity(self):
+        i, q, u, v = self.I.data, self.Q.data, self.U.data, self.V.data
+        return Field(v / (i + torch.sqrt(q**2 + u**2)), self.grid)
 
     @property
     def amplitude(self):
@@ -77,7 +183,7 @@ class Wavefront(object):
     def power(self):
         w = self.grid.weights
         w = torch.as_tensor(w, device=self._electric_field.data.device) if not np.isscalar(w) else w
-        return Field(self.intensity.data * w, self.grid)
+        return Field(self.I.data * w, self.grid)
 
     @property
     def total_power(self):
@@ -209,13 +315,13 @@ class Apodizer(OpticalElement):
     def forward(self, wavefront):
         e = wavefront.electric_field
         a = _apodization_tensor(self.apodization, wavefront.wavelength, e.data)
-        return Wavefront(Field(e.data * a, e.grid), wavefront.wavelength)
+        return wavefront._carry(Field(e.data * a, e.grid))
 
     def backward(self, wavefront):
         e = wavefront.electric_field
         a = _apodization_tensor(self.apodization, wavefront.wavelength, e.data)
         a = a.conj() if isinstance(a, torch.Tensor) else np.conj(a)
-        return Wavefront(Field(e.data * a, e.grid), wavefront.wavelength)
+        return wavefront._carry(Field(e.data * a, e.grid))
 
 
 class PhaseApodizer(OpticalElement):
@@ -236,7 +342,7 @@ class PhaseApodizer(OpticalElement):
                                device=e.data.device)
         else:
             phase = as_tensor(self._phase, e.data.device)
-        return Wavefront(Field(apply_phase(e.data, phase, sign), e.grid), wavefront.wavelength)
+        return wavefront._carry(Field(apply_phase(e.data, phase, sign), e.grid))
 
     def forward(self, wavefront):
         return self._apply(wavefront, 1.0)
@@ -261,7 +367,7 @@ class SurfaceApodizer(OpticalElement):
         e = wavefront.electric_field
         scale = sign * (self._get_refractive_index(wavefront.wavelength) - 1) * 2 * np.pi / wavefront.wavelength
         sag = as_tensor(self.surface_sag, e.data.device)
-        return Wavefront(Field(apply_phase(e.data, sag, scale), e.grid), wavefront.wavelength)
+        return wavefront._carry(Field(apply_phase(e.data, sag, scale), e.grid))
 
     def forward(self, wavefront):
         return self._apply(wavefront, 1.0)

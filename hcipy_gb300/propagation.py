@@ -29,8 +29,8 @@ def _filter_apply(ff, wavefront, adjoint):
     if _differentiable(e):
         from .autograd import linear_apply
         res = linear_apply(e.data, lambda t: fwd(t).data, lambda g: adj(g).data)
-        return Wavefront(Field(res, e.grid), wavefront.wavelength)
-    return Wavefront(fwd(e), wavefront.wavelength)
+        return wavefront._carry(Field(res, e.grid))
+    return wavefront._carry(fwd(e))
 
 
 def _differentiable(field):
@@ -123,8 +123,7 @@ class FraunhoferPropagator(AgnosticOpticalElement):
             alpha = complex(ft._w_in_scalar) * instance_data.norm_factor
             if _differentiable(e):
                 from .autograd import mft_apply
-                return Wavefront(Field(mft_apply(ft, e.data, _lib.HX_FORWARD, alpha), instance_data.output_grid),
-                                 wavefront.wavelength)
+                return wavefront._carry(Field(mft_apply(ft, e.data, _lib.HX_FORWARD, alpha), instance_data.output_grid))
             res = ft._run(e, ft.input_grid, ft.output_grid, _lib.HX_FORWARD, alpha)
         else:
             norm = instance_data.norm_factor
@@ -133,9 +132,9 @@ class FraunhoferPropagator(AgnosticOpticalElement):
                 adj = _adjoint_of_forward(ft)
                 res = linear_apply(e.data, lambda t: ft.forward(t).data * norm,
                                    lambda g: adj(g) * np.conj(norm))
-                return Wavefront(Field(res, instance_data.output_grid), wavefront.wavelength)
+                return wavefront._carry(Field(res, instance_data.output_grid))
             res = ft.forward(e) * norm
-        return Wavefront(Field(res.data, instance_data.output_grid), wavefront.wavelength)
+        return wavefront._carry(Field(res.data, instance_data.output_grid))
 
     @make_agnostic_backward
     def backward(self, instance_data, wavefront):
@@ -146,8 +145,7 @@ class FraunhoferPropagator(AgnosticOpticalElement):
             alpha = complex(ft._w_out_scalar / (2 * np.pi)**ft.ndim) / instance_data.norm_factor
             if _differentiable(e):
                 from .autograd import mft_apply
-                return Wavefront(Field(mft_apply(ft, e.data, _lib.HX_BACKWARD, alpha), instance_data.input_grid),
-                                 wavefront.wavelength)
+                return wavefront._carry(Field(mft_apply(ft, e.data, _lib.HX_BACKWARD, alpha), instance_data.input_grid))
             res = ft._run(e, ft.output_grid, ft.input_grid, _lib.HX_BACKWARD, alpha)
         else:
             norm = instance_data.norm_factor
@@ -157,9 +155,9 @@ class FraunhoferPropagator(AgnosticOpticalElement):
                 # backward = forward^H / c, so its adjoint is forward / c
                 res = linear_apply(e.data, lambda t: ft.backward(t).data / norm,
                                    lambda g: ft.forward(g).data / (fwd_scale * np.conj(norm)))
-                return Wavefront(Field(res, instance_data.input_grid), wavefront.wavelength)
+                return wavefront._carry(Field(res, instance_data.input_grid))
             res = ft.backward(e) / norm
-        return Wavefront(Field(res.data, instance_data.input_grid), wavefront.wavelength)
+        return wavefront._carry(Field(res.data, instance_data.input_grid))
 
 
 class AngularSpectrumPropagator(AgnosticOpticalElement):

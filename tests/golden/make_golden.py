@@ -265,6 +265,40 @@ def make_vortex_cases(hp, out):
         out['vortex_%d' % i] = rec
 
 
+def make_vector_vortex_case(hp, out):
+    """VectorVortexCoronagraph (hcipy/coronagraphy/vortex.py:17-246), charge 2 on a 48^2 pupil (q 32, scaling
+    factor 2, window 16, a Lyot stop, a retardance that depends on the wavelength): the Lyot-plane Jones matrix of
+    an unpolarised aberrated pupil at two wavelengths and the Stokes parameters of its image (the polarised
+    wavefront's I/Q/U/V, hcipy/optics/wavefront.py:103-255); a partially polarised input; the backward propagation
+    of a random Jones-matrix field and of a scalar field."""
+    rng = np.random.default_rng(49)
+    pupil = hp.make_pupil_grid(48, 1.0)
+    aperture = hp.make_circular_aperture(1.0)(pupil)
+    stop = hp.make_circular_aperture(0.9)(pupil)
+    e = aperture * np.exp(1j * 0.05 * rng.standard_normal(pupil.size))
+    vvc = hp.VectorVortexCoronagraph(2, lyot_stop=stop, phase_retardation=lambda wl: np.pi * (1 + 0.05 * (wl - 1)),
+                                     q=32, scaling_factor=2, window_size=16)
+    prop = hp.FraunhoferPropagator(pupil, hp.make_focal_grid(4, 8))
+    rec = {'E': e, 'stop': np.asarray(stop)}
+    for k, wl in enumerate((1.0, 1.1)):
+        lyot = vvc.forward(hp.Wavefront(hp.Field(e, pupil), wl))
+        rec['lyot_%d' % k] = np.asarray(lyot.electric_field)
+        rec['lyot_stokes_%d' % k] = np.asarray(lyot.input_stokes_vector, np.float64)
+        img = prop(lyot)
+        rec['image_%d' % k] = np.stack([np.asarray(img.I), np.asarray(img.Q), np.asarray(img.U), np.asarray(img.V)])
+        rec['wavelength_%d' % k] = np.float64(wl)
+    ej = (rng.standard_normal((2, 2, pupil.size)) + 1j * rng.standard_normal((2, 2, pupil.size))) * aperture
+    stokes = np.array([1.0, 0.3, -0.2, 0.1])
+    lyot = vvc.forward(hp.Wavefront(hp.Field(ej, pupil), 1.0, stokes))
+    rec.update({'EJ': ej, 'stokes': stokes, 'lyot_pol': np.asarray(lyot.electric_field),
+                'lyot_pol_stokes': np.asarray(lyot.stokes_vector)})
+    g = rng.standard_normal((2, 2, pupil.size)) + 1j * rng.standard_normal((2, 2, pupil.size))
+    rec['G'] = g
+    rec['back'] = np.asarray(vvc.backward(hp.Wavefront(hp.Field(g, pupil), 1.0, stokes)).electric_field)
+    rec['back_scalar'] = np.asarray(vvc.backward(hp.Wavefront(hp.Field(g[0, 0], pupil), 1.0)).electric_field)
+    out['vector_vortex'] = rec
+
+
 def make_pyramid_case(hp, out):
     """PyramidWavefrontSensorOptics (hcipy/wavefront_sensing/pyramid.py:94-199): forward of an aberrated pupil at
     two wavelengths (the pyramid phase depends on the refractive index and the wavenumber), backward of a random
@@ -526,8 +560,8 @@ def save(out):
 
 
 CASES = ['mft_cases', 'fraunhofer_cfg1', 'fft_cases', 'czt_cases', 'asp_cases', 'fresnel_cases', 'vortex_cases',
-         'pyramid_case', 'modulated_pyramid_case', 'lyot_case', 'subpixel_cases', 'atmosphere_case', 'dm_case', 'efc_case', 'pickle_case',
-         'spectral_noise_case']
+         'vector_vortex_case', 'pyramid_case', 'modulated_pyramid_case', 'lyot_case', 'subpixel_cases',
+         'atmosphere_case', 'dm_case', 'efc_case', 'pickle_case', 'spectral_noise_case']
 
 
 def main():

@@ -60,3 +60,71 @@ def test_lazy_conjugate_views_are_materialised():
     out = mft._run(e, mft.input_grid, mft.output_grid, _lib.HX_FORWARD, complex(mft._w_in_scalar),
                    epilogue=_lib.HX_EPI_MUL, mask=m.conj()).numpy()
     assert rel_err(out, mft.forward(e).numpy() * np.conj(m.cpu().numpy())) < 1e-12
+
+
+def _vector_vortex(g, stop=True):
+    pupil = hg.make_pupil_grid(48, 1.0)
+    return pupil, hg.VectorVortexCoronagraph(2, lyot_stop=hg.Field(g['stop'], pupil) if stop else None,
+                                             phase_retardation=lambda wl: np.pi * (1 + 0.05 * (wl - 1)), q=32,
+                                             scaling_factor=2, window_size=16)
+
+
+def test_vector_vortex_matches_reference():
+    """VectorVortexCoronagraph (hcipy/coronagraphy/vortex.py:17-246) against the reference: the Lyot-plane Jones
+    matrix of an unpolarised pupil at two wavelengths (a chromatic retardance) and the Stokes parameters of its image
+    through a lens (the polarised wavefront's I/Q/U/V, wavefront.py:103-255); a partially polarised input; backward
+    of a Jones-matrix field and of a scalar field; complex64.  Tolerances: fields 1e-10, Stokes parameters 1e-9
+    (complex128); complex64 2e-5."""
+    g = load_golden('vector_vortex')
+    pupil, vvc = _vector_vortex(g)
+    prop = hg.FraunhoferPropagator(pupil, hg.make_focal_grid(4, 8))
+    for k in range(2):
+        wl = float(g['wavelength_%d' % k])
+        lyot = vvc.forward(hg.Wavefront(hg.Field(g['E'], pupil), wl))
+        assert lyot.is_polarized and lyot.wavelength == wl
+        assert np.array_equal(lyot.input_stokes_vector, g['lyot_stokes_%d' % k])
+        assert rel_err(lyot.electric_field.numpy(), g['lyot_%d' % k]) < 1e-10, k
+        img = prop(lyot)
+        assert img.is_polarized
+        iquv = np.stack([img.I.numpy(), img.Q.numpy(), img.U.numpy(), img.V.numpy()])
+        assert rel_err(iquv, g['image_%d' % k]) < 1e-9, k
+        assert rel_err(img.stokes_vector.numpy(), g['image_%d' % k]) < 1e-9
+    assert len(vvc._entries) == 2  # one set of three scalar coronagraphs per retardance
+    pol = vvc.forward(hg.Wavefront(hg.Field(g['EJ'], pupil), 1.0, g['stokes']))
+    assert np.array_equal(pol.input_stokes_vector, g['stokes'])
+    assert rel_err(pol.electric_field.numpy(), g['lyot_pol']) < 1e-10
+    assert rel_err(pol.stokes_vector.numpy(), g['lyot_pol_stokes']) < 1e-9
+    back = vvc.backward(hg.Wavefront(hg.Field(g['G'], pupil), 1.0, g['stokes']))
+    assert rel_err(back.electric_field.numpy(), g['back']) < 1e-10
+    back = vvc.backward(hg.Wavefront(hg.Field(g['G'][0, 0], pupil), 1.0))
+    assert rel_err(back.electric_field.numpy(), g['back_scalar']) < 1e-10
+    _, bare = _vector_vortex(g, stop=False)
+    lyot32 = bare.forward(hg.Wavefront(hg.Field(g['E'].astype(np.complex64), pupil), 1.0)).electric_field.numpy()
+    assert lyot32.dtype == np.complex64 and rel_err(lyot32 * g['stop'], g['lyot_0']) < 2e-5
+    with pytest.raises(ValueError):
+        vvc.forward(hg.Wavefront(hg.Field(np.stack([g['E'], g['E']]), pupil), 1.0))
+
+
+def test_polarised_wavefront_stokes_parameters():
+    """A scalar field with a Stokes vector becomes E times the identity, whose Stokes parameters are |E|^2 times the
+    input vector; a scalar wavefront is unpolarised (Q = U = V = 0); elements keep the input Stokes vector."""
+    pupil = hg.make_pupil_grid(16, 1.0)
+    rng = np.random.default_rng(3)
+    e = rng.standard_normal(pupil.size) + 1j * rng.standard_normal(pupil.size)
+    s = np.array([1.0, 0.4, -0.3, 0.2])
+    wf = hg.Wavefront(hg.Field(e, pupil), 1.0, s)
+    j = wf.electric_field.numpy()
+    assert j.shape == (2, 2, pupil.size)
+    assert np.array_equal(j[0, 0], e) and np.array_equal(j[1, 1], e) and not j[0, 1].any() and not j[1, 0].any()
+    ref = np.abs(e)**2 * s[:, np.newaxis]
+    assert rel_err(wf.stokes_vector.numpy(), ref) < 1e-15
+    assert rel_err(wf.power.numpy(), ref[0] * pupil.weights) < 1e-15
+    dop = wf.degree_of_polarization.numpy()
+    assert np.allclose(dop, np.sqrt(0.4**2 + 0.3**2 + 0.2**2), rtol=1e-14)
+    out = hg.Apodizer(hg.Field(np.ones(pupil.size) * 0.5, pupil)).forward(wf)
+    assert np.array_equal(out.input_stokes_vector, s) and rel_err(out.I.numpy(), 0.25 * ref[0]) < 1e-15
+    scalar = hg.Wavefront(hg.Field(e, pupil), 1.0)
+    assert scalar.is_scalar and not scalar.Q.numpy().any()
+    assert rel_err(scalar.stokes_vector.numpy()[0], np.abs(e)**2) < 1e-15
+    with pytest.raises(ValueError):
+        hg.Wavefront(hg.Field(np.stack([e, e, e]), pupil), 1.0, s)
