@@ -33,7 +33,7 @@ import torch
 from . import _lib
 from .field import Field, as_tensor
 from .kernels import apply_phase
-from .optics import OpticalElement, Wavefront
+from .optics import OpticalElement
 
 
 # ---- turbulence statistics (hcipy/atmosphere/atmospheric_model.py:321-420) -------------------------------

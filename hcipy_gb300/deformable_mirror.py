@@ -13,7 +13,7 @@ import torch
 
 from .field import CartesianGrid, RegularCoords, Field, as_tensor, make_uniform_grid
 from .kernels import SparseBasis
-from .optics import OpticalElement, Wavefront
+from .optics import OpticalElement
 
 
 class ModeBasis(object):

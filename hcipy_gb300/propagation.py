@@ -5,7 +5,7 @@ import torch
 from . import _lib
 from .field import Field, as_tensor
 from .fourier import make_fourier_transform, MatrixFourierTransform
-from .optics import AgnosticOpticalElement, Wavefront, make_agnostic_forward, make_agnostic_backward
+from .optics import AgnosticOpticalElement, make_agnostic_forward, make_agnostic_backward
 
 
 def _adjoint_scale(ft):

@@ -221,3 +221,24 @@ def test_modulated_pyramid_plan_time_host_data():
     assert np.array_equal(m[:, 0], pupil.x) and np.array_equal(m[:, 1], pupil.y)
     with pytest.raises(RuntimeError):
         slow.backward(None)
+
+
+def test_vector_vortex_jones_entries():
+    """The vector vortex's focal-plane masks (host plan data): the three entries form the Jones matrix of a linear
+    retarder R(-a) diag(e^{iG/2}, e^{-iG/2}) R(a) with fast axis a = charge theta / 2 (symmetric and unitary), and
+    all vanish at the singularity."""
+    import hcipy_gb300 as hg
+    grid = hg.make_uniform_grid([9, 9], [2.0, 2.0])  # odd: a point on the singularity
+    vvc = hg.VectorVortexCoronagraph(4, phase_retardation=0.9 * np.pi)
+    j11, j12, j22 = (vvc._jones_entry(0.9 * np.pi, w)(grid) for w in ('j11', 'j12', 'j22'))
+    x, y = grid.points_list()
+    a = 2 * np.arctan2(y, x)
+    centre = np.hypot(x, y) == 0
+    assert centre.sum() == 1 and j11[centre] == 0 and j12[centre] == 0 and j22[centre] == 0
+    for k in np.flatnonzero(~centre):
+        c, s = np.cos(a[k]), np.sin(a[k])
+        rot = np.array([[c, s], [-s, c]])
+        ref = rot.T @ np.diag([np.exp(0.45j * np.pi), np.exp(-0.45j * np.pi)]) @ rot
+        got = np.array([[j11[k], j12[k]], [j12[k], j22[k]]])
+        assert np.allclose(got, ref, rtol=0, atol=1e-15)
+        assert np.allclose(got @ got.conj().T, np.eye(2), rtol=0, atol=1e-15)
