@@ -4,8 +4,10 @@ This package restates, in plain numpy (float64 / complex128), the reference
 algorithms of the path that the CUDA library implements: the matrix Fourier
 transform, the zero-padded FFT, the chirp-Z / zoom FFT, the Fourier filter and
 angular-spectrum transfer function, the Lyot-coronagraph Babinet chain, the
-deformable-mirror phase and the infinite-atmospheric-layer extrusion with its
-quintic sub-pixel shift.  Each function cites the reference file and lines it
+multi-scale, vortex and vector-vortex coronagraphs with the Stokes parameters
+of a polarised wavefront, the pyramid wavefront-sensor optics (plain and
+modulated), the deformable-mirror phase and the infinite-atmospheric-layer
+extrusion with its quintic sub-pixel shift.  Each function cites the reference file and lines it
 follows (paths are relative to the HCIPy source tree).
 
 Parity status: pinned.  ``tests/test_oracle_golden.py`` checks every function

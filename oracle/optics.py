@@ -1,4 +1,6 @@
 """Propagators and coronagraph chain of the reference, restated in float64 (test infrastructure only)."""
+import math
+
 import numpy as np
 
 from . import fourier
@@ -62,24 +64,6 @@ def surface_apodize(e, sag, n, wavelength):
     return np.asarray(e) * np.exp(1j * (n - 1) * np.asarray(sag) * (2 * np.pi / wavelength))
 
 
-def supersampled_mean(fn, grid, oversampling):
-    """hcipy/field/util.py:651-690 for a separated grid: the mean of fn over oversampling^2 dithered copies of the
-    grid, each axis dithered by (i + 1/2) / oversampling - 1/2 of its local spacing (central differences inside,
-    one-sided at the ends), dither points taken with x fastest."""
-    from .grids import make_uniform_grid
-    dithers = make_uniform_grid([oversampling, oversampling], 1)
-    dxs, dys = dithers.coords()
-    axes = grid.separated_coords
-    spacing = [np.concatenate(([c[1] - c[0]], (c[2:] - c[:-2]) / 2., [c[-1] - c[-2]])) for c in axes]
-    acc = 0
-    for tx, ty in zip(dxs, dys):
-        x = axes[0] + float(tx) * spacing[0]
-        y = axes[1] + float(ty) * spacing[1]
-        xx, yy = np.meshgrid(x, y)
-        acc = acc + fn(xx.ravel(), yy.ravel())
-    return acc / len(dxs)
-
-
 class PyramidOptics(object):
     """hcipy/wavefront_sensing/pyramid.py:94-181: lens, circular field stop, glass pyramid (SurfaceApodizer), lens."""
 
@@ -137,10 +121,128 @@ def modulated_pyramid_forward(optics, e, wavelength, modulation, num_steps, fast
     n = optics.refractive_index(wavelength)
     out = []
     for p in pos:
-        sag = supersampled_mean(optics.sag_function, optics.focal.shifted(2 * p), 4)
+        sag = fourier.supersampled_mean(optics.sag_function, optics.focal.shifted(2 * p), 4)
         out.append(fraunhofer_forward(surface_apodize(focal, sag, n, wavelength), optics.focal, optics.out_grid,
                                       wavelength))
     return np.stack(out)
+
+
+def vortex_mask(charge):
+    """hcipy/coronagraphy/vortex.py:13-14: exp(i charge theta), zero inside make_circular_aperture(1e-9)."""
+    def mask(grid):
+        x, y = grid.coords()
+        return np.exp(1j * charge * np.arctan2(y, x)) * (1 - (x**2 + y**2 <= (1e-9 / 2)**2))
+    return mask
+
+
+def retarder_jones(retardance, fast_axis):
+    """hcipy/optics/polarization.py:141-160 for a linear retarder (circularity 0): the (2, 2, n) Jones matrix."""
+    plus, minus = np.exp(1j * retardance / 2), np.exp(-1j * retardance / 2)
+    c, s = np.cos(fast_axis), np.sin(fast_axis)
+    j11 = plus * c**2 + minus * s**2
+    j12 = (plus - minus) * np.exp(-1j * 0) * c * s
+    j21 = (plus - minus) * np.exp(1j * 0) * c * s
+    j22 = plus * s**2 + minus * c**2
+    return np.array([[j11, j12], [j21, j22]])
+
+
+def vector_vortex_mask(charge, retardance):
+    """hcipy/coronagraphy/vortex.py:94-100: the retarder with fast axis charge / 2 * theta, zero at the centre."""
+    def mask(grid):
+        x, y = grid.coords()
+        j = retarder_jones(retardance, charge / 2 * np.arctan2(y, x))
+        return j * (1 - (x**2 + y**2 <= (1e-9 / 2)**2))
+    return mask
+
+
+def _field_dot(a, b):
+    """hcipy/field/field.py field_dot for a (2, 2, n) matrix field and a (2, n) or (2, 2, n) field."""
+    return np.einsum('ij...n,j...n->i...n', a, b)
+
+
+class MultiScaleOptics(object):
+    """hcipy/coronagraphy/multi_scale.py:62-161 (and, for a (2, 2, n) Jones-matrix mask, the vector vortex's
+    vortex.py:79-246): level 0 a Fourier filter at q = 2, level i > 0 a window scaling_factor times finer with the
+    coarser levels' contribution subtracted, propagated at unit wavelength and focal length."""
+
+    def __init__(self, pupil, complex_mask, q=1024, scaling_factor=4, window_size=32):
+        from scipy.signal import windows
+        from .grids import make_focal_grid
+        self.pupil = pupil
+        diameter = pupil.dims * pupil.delta
+        levels = int(math.ceil(math.log(q / 2) / math.log(scaling_factor))) + 1
+        qs = [2 * scaling_factor**i for i in range(levels)]
+        num_airys = [tuple(n / 2 for n in pupil.dims)]
+        for i in range(1, levels):
+            num_airys.append(tuple(n * window_size / (2 * qs[i - 1] * n) for n in num_airys[i - 1]))
+        self.focal_grids, self.masks = [], []
+        for i in range(levels):
+            focal = make_focal_grid(qs[i], num_airys[i], spatial_resolution=1 / diameter)
+            m = np.asarray(complex_mask(focal), np.complex128)
+            if i != levels - 1:
+                w = np.outer(windows.tukey(window_size, 1, False), windows.tukey(window_size, 1, False))
+                w = np.pad(w, tuple((n_foc - n_w) // 2 for n_foc, n_w in zip(focal.shape, w.shape)), 'constant')
+                m = m * (1 - w.ravel())
+            for j in range(i):
+                fft = fourier.FFTPlan(self.focal_grids[j])
+                x, y = focal.separated_coords
+                u, v = fft.output_grid.separated_coords
+                back = np.array([fourier.mft_backward(fft.forward(mj), x, y, u, v, fft.output_grid.weights)
+                                 for mj in self.masks[j].reshape(-1, self.focal_grids[j].size)])
+                m = m - back.reshape(m.shape)
+            self.focal_grids.append(focal)
+            self.masks.append(m)
+        self.jones = self.masks[0].ndim == 3
+        tf = self.masks[0].reshape(-1, self.focal_grids[0].size)
+        self.filters = [fourier.FourierFilterPlan(pupil, t, qs[0]) for t in tf]
+
+    def _filter(self, e, adjoint):
+        if not self.jones:
+            return self.filters[0].apply(e, adjoint)
+        # fourier_operations.py:112-121: FFT of every entry, the matrix product with the transfer function (its
+        # conjugate transpose for the adjoint), inverse FFT
+        plan = self.filters[0]
+        tfs = np.array([f.tf for f in self.filters]).reshape((2, 2) + plan.internal_grid.shape)
+        if adjoint:
+            tfs = np.conj(np.swapaxes(tfs, 0, 1))
+        lead = e.shape[:-1]
+        spec = []
+        for ej in e.reshape((-1, e.shape[-1])):
+            f = np.zeros(plan.internal_grid.shape, dtype=np.complex128)
+            f[plan.cutout] = ej.reshape(plan.shape_in)
+            spec.append(np.fft.fftn(f))
+        spec = np.array(spec).reshape(lead + plan.internal_grid.shape)
+        prod = np.einsum('ij...,j...->i...', tfs, spec)
+        out = [np.fft.ifftn(p)[plan.cutout].ravel() for p in prod.reshape((-1,) + plan.internal_grid.shape)]
+        return np.array(out).reshape(lead + (plan.shape_in[0] * plan.shape_in[1],))
+
+    def propagate(self, e, adjoint=False):
+        """Lyot plane of e (multi_scale.py:95-128, vortex.py:160-202), or with ``adjoint`` the backward
+        propagation (multi_scale.py:130-161, vortex.py:204-246).  For a Jones-matrix mask a scalar e is taken as
+        e times the identity."""
+        e = np.asarray(e, np.complex128)
+        if self.jones and e.ndim == 1:
+            e = np.array([[e, np.zeros_like(e)], [np.zeros_like(e), e]])
+        lyot = self._filter(e, adjoint)
+        for focal, m in zip(self.focal_grids[1:], self.masks[1:]):
+            f = np.array([fraunhofer_forward(ek, self.pupil, focal) for ek in e.reshape((-1, e.shape[-1]))])
+            f = f.reshape(e.shape[:-1] + (focal.size,))
+            m = np.conj(m) if adjoint else m  # vortex.py:240: the conjugate, not the conjugate transpose
+            f = _field_dot(m, f) if self.jones else m * f
+            back = np.array([fraunhofer_backward(fk, self.pupil, focal) for fk in f.reshape((-1, focal.size))])
+            lyot = lyot + back.reshape(lyot.shape)
+        return lyot
+
+
+def stokes_parameters(jones, stokes):
+    """hcipy/optics/wavefront.py:103-235 for a partially polarised wavefront: (I, Q, U, V) of the (2, 2, n)
+    Jones-matrix field acting on the input Stokes vector, through the Mueller matrix A (J kron J*) A^-1."""
+    a = np.array([[1, 0, 0, 1], [1, 0, 0, -1], [0, 1, 1, 0], [0, 1j, -1j, 0]])
+    ainv = np.linalg.inv(a)
+    j = np.moveaxis(np.asarray(jones), -1, 0)
+    kron = np.einsum('nij,nkl->nikjl', j, np.conj(j)).reshape(-1, 4, 4)
+    mueller = np.einsum('ab,nbc,cd->nad', a, kron, ainv)
+    return np.einsum('nab,b->an', mueller, np.asarray(stokes, np.float64)).real
 
 
 def intensity(e):

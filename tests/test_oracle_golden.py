@@ -262,3 +262,40 @@ def test_modulated_pyramid_oracle():
     assert np.array_equal(sag, g['fast_surface_3'])
     pupil = grids.make_pupil_grid(32, 1.0)
     assert rel_err(optics.tip_tilt_forward(g['E'], pupil, g['tip_tilt_command'], 0.8), g['tip_tilt']) < 1e-14
+
+
+@pytest.mark.parametrize('case', ['vortex_0', 'vortex_1'])
+def test_vortex_oracle(case):
+    """The multi-scale vortex (hcipy/coronagraphy/multi_scale.py, vortex.py:12-15): level masks, Lyot plane and
+    backward propagation."""
+    g = load_golden(case)
+    ms = optics.MultiScaleOptics(grids.make_pupil_grid(int(g['n']), 1.0), optics.vortex_mask(int(g['charge'])),
+                                 int(g['q']), int(g['scaling_factor']), int(g['window_size']))
+    assert len(ms.masks) == int(g['levels'])
+    for k, m in enumerate(ms.masks):
+        assert rel_err(m, g['mask_%d' % k]) < 1e-12, k
+    assert rel_err(ms.propagate(g['E']), g['lyot_c128']) < 1e-12
+    assert rel_err(ms.propagate(g['G'], adjoint=True), g['back_c128']) < 1e-12
+
+
+def test_vector_vortex_oracle():
+    """The vector vortex (vortex.py:17-246) in the reference's own tensor form (a Jones-matrix transfer function and
+    field_dot at every level), and the Stokes parameters of a partially polarised wavefront (wavefront.py:103-235)
+    through the Mueller matrix."""
+    g = load_golden('vector_vortex')
+    pupil = grids.make_pupil_grid(48, 1.0)
+    focal = grids.make_focal_grid(4, 8)
+    stop = g['stop']
+    for k in range(2):
+        wl = float(g['wavelength_%d' % k])
+        vv = optics.MultiScaleOptics(pupil, optics.vector_vortex_mask(2, np.pi * (1 + 0.05 * (wl - 1))), 32, 2, 16)
+        lyot = vv.propagate(g['E']) * stop
+        assert rel_err(lyot, g['lyot_%d' % k]) < 1e-12, k
+        img = np.array([[optics.fraunhofer_forward(lyot[i, j], pupil, focal, wavelength=wl) for j in range(2)]
+                        for i in range(2)])
+        assert rel_err(optics.stokes_parameters(img, g['lyot_stokes_%d' % k]), g['image_%d' % k]) < 1e-12, k
+    vv = optics.MultiScaleOptics(pupil, optics.vector_vortex_mask(2, np.pi), 32, 2, 16)
+    assert rel_err(vv.propagate(g['EJ']) * stop, g['lyot_pol']) < 1e-12
+    assert rel_err(optics.stokes_parameters(g['lyot_pol'], g['stokes']), g['lyot_pol_stokes']) < 1e-13
+    assert rel_err(vv.propagate(g['G'] * stop, adjoint=True), g['back']) < 1e-12
+    assert rel_err(vv.propagate(g['G'][0, 0] * stop, adjoint=True), g['back_scalar']) < 1e-12
