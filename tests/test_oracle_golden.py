@@ -258,7 +258,7 @@ def test_modulated_pyramid_oracle():
     for k in range(2):
         out = optics.modulated_pyramid_forward(po, g['E'], float(g['wavelength_%d' % k]), mod, steps, fast=True)
         assert rel_err(out, g['fast_%d' % k]) < 1e-12, k
-    sag = optics.supersampled_mean(po.sag_function, po.focal.shifted(2 * g['positions'][3]), 4)
+    sag = fourier.supersampled_mean(po.sag_function, po.focal.shifted(2 * g['positions'][3]), 4)
     assert np.array_equal(sag, g['fast_surface_3'])
     pupil = grids.make_pupil_grid(32, 1.0)
     assert rel_err(optics.tip_tilt_forward(g['E'], pupil, g['tip_tilt_command'], 0.8), g['tip_tilt']) < 1e-14
