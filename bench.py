@@ -51,6 +51,7 @@ def parse_args():
     p.add_argument('--no-graph', action='store_true', help='launch the step from Python instead of a CUDA graph')
     p.add_argument('--no-autotune', action='store_true', help='built-in tile choice instead of measured tiles')
     p.add_argument('--no-small', action='store_true', help='skip the 256^2 Fraunhofer and the FFT-family legs')
+    p.add_argument('--vortex', action='store_true', help='add the multi-scale vortex and vector-vortex leg')
     p.add_argument('--broadband-frames', type=int, default=256,
                    help='frames of the broadband-through-turbulence leg (0: skip it)')
     p.add_argument('--lyot-batch', type=int, default=8,
@@ -923,6 +924,69 @@ def run_modulated_pyramid(args, dev):
     return out
 
 
+def run_vortex(args, dev):
+    """Multi-scale vortex coronagraphs on a 256^2 pupil with the reference's default sampling (charge 2, q = 1024,
+    scaling factor 4, window 32: six levels, a 512^2 Fourier filter and five 256^2 <-> 128^2 MFT pairs), no Lyot
+    stop: Lyot-plane fields/s with Python launches for the scalar vortex in complex64 and complex128 and for the
+    vector vortex (its three scalar coronagraphs) in complex64, the plan times, the errors against the float64
+    oracle and the oracle port timed on the host."""
+    import torch
+    import hcipy_gb300 as hg
+    from hcipy_gb300 import workloads
+    from oracle import optics
+    from oracle.grids import make_pupil_grid as o_pupil
+    n = 256
+    pupil = hg.make_pupil_grid(n, 1.0)
+    e_h = workloads.circular_aperture(pupil, 1.0) * np.exp(1j * workloads.zernike_phase(pupil, 1.0, 2, 21, 0.05, 5))
+    out = {'workload': '256^2 pupil, Zernike 2-21 at 0.05 rad RMS, charge-2 vortex (q 1024, scaling factor 4, '
+                       'window 32: 6 levels), Lyot plane without a stop'}
+
+    def timed(fn, k=20):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(k):
+            fn()
+        t1.record()
+        t1.synchronize()
+        return t0.elapsed_time(t1) / k
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    c0 = time.perf_counter()
+    vc = hg.VortexCoronagraph(pupil, 2)
+    torch.cuda.synchronize()
+    out['scalar_plan_s'] = time.perf_counter() - c0
+    oracle = optics.MultiScaleOptics(o_pupil(n, 1.0), optics.vortex_mask(2), 1024, 4, 32)
+    for name, dtype in (('scalar_c64', np.complex64), ('scalar_c128', np.complex128)):
+        wf = hg.Wavefront(hg.Field(torch.from_numpy(e_h.astype(dtype)).to(dev), pupil), 1.0)
+        ms = timed(lambda: vc.forward(wf))
+        got = vc.forward(wf).electric_field.numpy().astype(np.complex128)
+        ref = oracle.propagate(e_h.astype(dtype).astype(np.complex128))
+        out[name] = {'lyot_fields_per_s': 1e3 / ms, 'ms_per_field': ms, 'rel_err_vs_fp64': rel(got, ref)}
+    vvc = hg.VectorVortexCoronagraph(2)
+    wf = hg.Wavefront(hg.Field(torch.from_numpy(e_h.astype(np.complex64)).to(dev), pupil), 1.0)
+    c0 = time.perf_counter()
+    vvc.forward(wf)
+    torch.cuda.synchronize()
+    out['vector_plan_s'] = time.perf_counter() - c0
+    ms = timed(lambda: vvc.forward(wf))
+    got = vvc.forward(wf).electric_field.numpy().astype(np.complex128)
+    ref = optics.MultiScaleOptics(o_pupil(n, 1.0), optics.vector_vortex_mask(2, np.pi), 1024, 4, 32).propagate(
+        e_h.astype(np.complex64).astype(np.complex128))
+    out['vector_c64'] = {'lyot_fields_per_s': 1e3 / ms, 'ms_per_field': ms, 'rel_err_vs_fp64': rel(got, ref)}
+    k, c0 = 0, time.perf_counter()
+    while k < 5 or time.perf_counter() - c0 < 1.0:
+        oracle.propagate(e_h)
+        k += 1
+    out['cpu_baseline'] = {'lyot_fields_per_s': k / (time.perf_counter() - c0), 'cores': host_cores(), 'kind': 'port',
+                           'sample': '%d scalar propagations through the numpy port, complex128' % k}
+    return out
+
+
 def run_fft_family(args, dev, peaks):
     """A 1024^2 pupil of 8 m behind a von Karman screen (r0 0.15 m, L0 20 m) at 1.6 um: the zero-padded FFT to
     4096^2 (q=4) and angular-spectrum propagation over 0.5 m and 5 m (2048^2 padded).  Per-call time with CUDA
@@ -1229,6 +1293,8 @@ def run_ours(args, rank, world, dist):
         line['efc'] = run_efc(args, dev)
         line['fraunhofer_256'] = run_small_fraunhofer(args, dev, peaks)
         line['modulated_pyramid_256'] = run_modulated_pyramid(args, dev)
+    if args.vortex:
+        line['vortex_256'] = run_vortex(args, dev)
         line['fft_family_1024'] = run_fft_family(args, dev, peaks)
     # The accuracy conditions of the metric and the side-by-side rates come last, so that a reader who keeps only
     # the end of the line (or of stderr, where the same summary is printed) still has them.
