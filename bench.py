@@ -50,8 +50,8 @@ def parse_args():
     p.add_argument('--no-atmosphere', action='store_true', help='skip the atmospheric-layer leg')
     p.add_argument('--no-graph', action='store_true', help='launch the step from Python instead of a CUDA graph')
     p.add_argument('--no-autotune', action='store_true', help='built-in tile choice instead of measured tiles')
-    p.add_argument('--no-small', action='store_true', help='skip the 256^2 Fraunhofer and the FFT-family legs')
-    p.add_argument('--vortex', action='store_true', help='add the multi-scale vortex and vector-vortex leg')
+    p.add_argument('--no-small', action='store_true',
+                   help='skip the probe, EFC, 256^2 Fraunhofer, FFT-family, pyramid and vortex legs')
     p.add_argument('--broadband-frames', type=int, default=256,
                    help='frames of the broadband-through-turbulence leg (0: skip it)')
     p.add_argument('--lyot-batch', type=int, default=8,
@@ -1293,7 +1293,6 @@ def run_ours(args, rank, world, dist):
         line['efc'] = run_efc(args, dev)
         line['fraunhofer_256'] = run_small_fraunhofer(args, dev, peaks)
         line['modulated_pyramid_256'] = run_modulated_pyramid(args, dev)
-    if args.vortex:
         line['vortex_256'] = run_vortex(args, dev)
         line['fft_family_1024'] = run_fft_family(args, dev, peaks)
     # The accuracy conditions of the metric and the side-by-side rates come last, so that a reader who keeps only
