@@ -1,5 +1,7 @@
 """Coronagraphs: the Lyot coronagraph (hcipy/coronagraphy/lyot.py:7-122) with the Babinet chain fused into the MFT
 GEMMs, and the multi-scale, vortex and vector-vortex coronagraphs (multi_scale.py, vortex.py)."""
+import collections
+
 import numpy as np
 import torch
 
@@ -264,7 +266,7 @@ class VectorVortexCoronagraph(AgnosticOpticalElement):
         self.q = q
         self.scaling_factor = scaling_factor
         self.window_size = window_size
-        self._entries = {}
+        self._entries = collections.OrderedDict()
         AgnosticOpticalElement.__init__(self)
 
     def _jones_entry(self, retardance, which):
@@ -290,10 +292,13 @@ class VectorVortexCoronagraph(AgnosticOpticalElement):
         key = (grid_key(input_grid), retardance)
         entries = self._entries.get(key)
         if entries is None:
-            # the same retardance at another wavelength reuses the three coronagraphs
+            # the same retardance at another wavelength reuses the three coronagraphs; at most as many sets as
+            # the instance cache holds, first in first out
             entries = tuple(MultiScaleCoronagraph(input_grid, self._jones_entry(retardance, w), None, self.q,
                                                   self.scaling_factor, self.window_size)
                             for w in ('j11', 'j12', 'j22'))
+            if len(self._entries) >= self._max_in_cache:
+                self._entries.popitem(last=False)
             self._entries[key] = entries
         instance_data.entries = entries
 

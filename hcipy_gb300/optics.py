@@ -1,9 +1,9 @@
 """Wavefronts and optical elements on the device (hcipy/optics).
 
-``Wavefront`` mirrors hcipy/optics/wavefront.py:15-361 for scalar fields:
-the electric field is cast to complex of the input bit depth, ``copy`` is a
-device copy, ``intensity`` / ``power`` / ``total_power`` are computed on the
-GPU.  ``AgnosticOpticalElement`` keeps the reference's instance cache
+``Wavefront`` mirrors hcipy/optics/wavefront.py:15-361 for scalar and
+partially polarised fields: the electric field is cast to complex of the input
+bit depth, ``copy`` is a device copy, the Stokes parameters, ``power`` and
+``total_power`` are computed on the GPU.  ``AgnosticOpticalElement`` keeps the reference's instance cache
 (hcipy/optics/optical_element.py:261-790): instances keyed by input grid,
 output grid and a logarithmic wavelength key, at most 11, first in first out.
 """
@@ -15,6 +15,31 @@ import numpy as np
 import torch
 
 from .field import Field, as_tensor, grid_key
+
+
+def jones_stokes(jones, stokes, rows=(0, 1, 2, 3)):
+    """Stokes parameters (I, Q, U, V; the ``rows`` asked for) of light with Stokes vector ``stokes`` after the
+    Jones matrices ``jones`` (a (2, 2, n) complex tensor): 1/2 M s with M the Mueller matrix of J = [[x, y], [z, w]]
+    at every point, written with the products x y*, z w*, ... of its entries (wavefront.py:103-235)."""
+    x, y, z, w = jones[0, 0], jones[0, 1], jones[1, 0], jones[1, 1]
+    ax, ay, az, aw = (t.real * t.real + t.imag * t.imag for t in (x, y, z, w))
+    s = [float(v) for v in stokes]
+    out = []
+    for k in rows:
+        if k == 0:
+            xy, zw = x * y.conj(), z * w.conj()
+            m = (ax + ay + az + aw, ax - ay + az - aw, 2 * (xy + zw).real, 2 * (xy + zw).imag)
+        elif k == 1:
+            xy, zw = x * y.conj(), z * w.conj()
+            m = (ax + ay - az - aw, ax - ay - az + aw, 2 * (xy - zw).real, 2 * (xy - zw).imag)
+        elif k == 2:
+            xz, yw, xw, yz = x * z.conj(), y * w.conj(), x * w.conj(), y * z.conj()
+            m = (2 * (xz + yw).real, 2 * (xz - yw).real, 2 * (xw + yz).real, 2 * (xw - yz).imag)
+        else:
+            xz, yw, xw, yz = x * z.conj(), y * w.conj(), x * w.conj(), y * z.conj()
+            m = (-2 * (xz + yw).imag, -2 * (xz - yw).imag, -2 * (xw + yz).imag, 2 * (xw - yz).real)
+        out.append(0.5 * (m[0] * s[0] + m[1] * s[1] + m[2] * s[2] + m[3] * s[3]))
+    return out
 
 
 class Wavefront(object):
@@ -92,29 +117,10 @@ class Wavefront(object):
         """A wavefront of ``field`` with this wavefront's wavelength and input Stokes vector."""
         return Wavefront(field, self.wavelength, self._input_stokes_vector)
 
-    def _stokes(self):
-        """(I, Q, U, V) of a polarised wavefront: 1/2 M s, M the Mueller matrix of the Jones matrix
-        J = [[x, y], [z, w]] at every point (written with the products x y*, z w*, ... of its entries), s the
-        input Stokes vector (wavefront.py:103-235)."""
-        e = self._electric_field.data
-        x, y, z, w = e[0, 0], e[0, 1], e[1, 0], e[1, 1]
-        ax, ay, az, aw = (t.real * t.real + t.imag * t.imag for t in (x, y, z, w))
-        xy, zw = x * y.conj(), z * w.conj()
-        xz, yw = x * z.conj(), y * w.conj()
-        xw, yz = x * w.conj(), y * z.conj()
-        rows = (
-            (ax + ay + az + aw, ax - ay + az - aw, 2 * (xy + zw).real, 2 * (xy + zw).imag),
-            (ax + ay - az - aw, ax - ay - az + aw, 2 * (xy - zw).real, 2 * (xy - zw).imag),
-            (2 * (xz + yw).real, 2 * (xz - yw).real, 2 * (xw + yz).real, 2 * (xw - yz).imag),
-            (-2 * (xz + yw).imag, -2 * (xz - yw).imag, -2 * (xw + yz).imag, 2 * (xw - yz).real),
-        )
-        s = [float(v) for v in self._input_stokes_vector]
-        return [0.5 * (r[0] * s[0] + r[1] * s[1] + r[2] * s[2] + r[3] * s[3]) for r in rows]
-
     @property
     def I(self):  # noqa: N802
         if self.is_polarized:
-            return Field(self._stokes()[0], self.grid)
+            return Field(jones_stokes(self._electric_field.data, self._input_stokes_vector, (0,))[0], self.grid)
         e = self._electric_field.data
         return Field(e.real * e.real + e.imag * e.imag, self.grid)
 
@@ -122,7 +128,7 @@ class Wavefront(object):
 
     def _stokes_part(self, k):
         if self.is_polarized:
-            return Field(self._stokes()[k], self.grid)
+            return Field(jones_stokes(self._electric_field.data, self._input_stokes_vector, (k,))[0], self.grid)
         e = self._electric_field.data
         return Field(torch.zeros(e.shape, dtype=e.real.dtype, device=e.device), self.grid)
 
@@ -142,7 +148,7 @@ class Wavefront(object):
     def stokes_vector(self):
         """(4, n): I, Q, U, V (a scalar wavefront is unpolarised: I = |E|^2, the rest 0)."""
         if self.is_polarized:
-            return Field(torch.stack(self._stokes()), self.grid)
+            return Field(torch.stack(jones_stokes(self._electric_field.data, self._input_stokes_vector)), self.grid)
         i = self.I.data
         out = torch.zeros(tuple(i.shape[:-1]) + (4, i.shape[-1]), dtype=i.dtype, device=i.device)
         out[..., 0, :] = i

@@ -117,3 +117,44 @@ def test_tikhonov_paths_agree_with_the_svd_form(monkeypatch, rcond, tol):
     assert rel_err(efc.inverse_tikhonov(m, rcond), oefc.inverse_tikhonov(m, rcond)) < tol
     out = efc.inverse_tikhonov(torch.from_numpy(m), rcond)
     assert isinstance(out, torch.Tensor) and rel_err(out.numpy(), oefc.inverse_tikhonov(m, rcond)) < tol
+
+
+def test_jones_stokes_matches_the_mueller_form():
+    """The polarised wavefront's Stokes parameters (``optics.jones_stokes``, torch on any device) against the
+    oracle's Mueller matrix A (J kron J*) A^-1 applied to the input Stokes vector (wavefront.py:103-235), on the
+    CPU; any subset of rows equals the full computation."""
+    import torch
+    from hcipy_gb300.optics import jones_stokes
+    from oracle import optics as ooptics
+    rng = np.random.default_rng(4)
+    j = rng.standard_normal((2, 2, 50)) + 1j * rng.standard_normal((2, 2, 50))
+    s = np.array([1.0, 0.3, -0.2, 0.1])
+    got = torch.stack(jones_stokes(torch.from_numpy(j), s)).numpy()
+    ref = ooptics.stokes_parameters(j, s)
+    assert np.max(np.abs(got - ref)) < 1e-14 * np.max(np.abs(ref))
+    for k in range(4):
+        assert np.array_equal(jones_stokes(torch.from_numpy(j), s, (k,))[0].numpy(), got[k])
+
+
+def test_vector_vortex_coronagraph_sets_are_shared_and_bounded(monkeypatch):
+    """The vector vortex builds its three scalar coronagraphs once per (grid, retardance): wavelengths with the
+    same retardance share them, and at most as many sets as the instance cache holds are kept (first in, first
+    out).  Host logic only: the scalar coronagraph is replaced by a recorder."""
+    from hcipy_gb300 import coronagraphy
+    built = []
+
+    class Recorder(object):
+        def __init__(self, grid, mask, *args):
+            built.append(mask)
+
+    monkeypatch.setattr(coronagraphy, 'MultiScaleCoronagraph', Recorder)
+    grid = hg.make_pupil_grid(8, 1.0)
+    fixed = hg.VectorVortexCoronagraph(2)
+    a = fixed.get_instance_data(grid, None, 1.0)
+    b = fixed.get_instance_data(grid, None, 1.3)
+    assert a is not b and a.entries is b.entries and len(built) == 3
+    chromatic = hg.VectorVortexCoronagraph(2, phase_retardation=lambda wl: np.pi * wl)
+    for k in range(14):
+        chromatic.get_instance_data(grid, None, 1.0 + 0.01 * k)
+    assert len(chromatic._entries) == chromatic._max_in_cache == 11
+    assert len(built) == 3 + 3 * 14
