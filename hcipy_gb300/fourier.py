@@ -489,6 +489,17 @@ def make_fourier_transform(input_grid, output_grid=None, q=1, fov=1, shift=0, pl
     reference would pick (and its numerical behaviour); ``'gpu'`` ranks them with
     the GB300 cost model of this package; ``'measure'`` times each on the device.
     """
+    options, expected, output_grid, (q, fov, shift) = _planned_methods(input_grid, output_grid, q, fov, shift,
+                                                                        planner)
+    best = min(expected, key=expected.get)
+    if best == 'fft':
+        return options['fft'](input_grid, q, fov, shift)
+    return options[best](input_grid, output_grid)
+
+
+def _planned_methods(input_grid, output_grid, q, fov, shift, planner):
+    """The planner's candidates and their expected times: (classes by method, times by supported method, the
+    output grid, the FFT parameters).  Without construction for the 'estimate' and 'gpu' planners."""
     options = {'mft': MatrixFourierTransform}
     try:
         from .fft import FastFourierTransform, ZoomFastFourierTransform
@@ -520,10 +531,7 @@ def make_fourier_transform(input_grid, output_grid=None, q=1, fov=1, shift=0, pl
             raise ValueError('planner must be "estimate", "gpu" or "measure"')
     if not expected:
         raise ValueError('No Fourier transform supports these grids (unstructured grids need a naive DFT).')
-    best = min(expected, key=expected.get)
-    if best == 'fft':
-        return options['fft'](input_grid, q, fov, shift)
-    return options[best](input_grid, output_grid)
+    return options, expected, output_grid, (q, fov, shift)
 
 
 def _time_device(fn, repeat=5):

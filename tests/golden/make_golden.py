@@ -299,6 +299,58 @@ def make_vector_vortex_case(hp, out):
     out['vector_vortex'] = rec
 
 
+def make_planner_case(hp, out):
+    """The method choice of make_fourier_transform(planner='estimate') (hcipy/fourier/fourier_transform.py:217-300)
+    over pupils of 16^2 to 2048^2 and rectangular ones, FFT output grids of q 1-16 and fov 1-0.1 and focal grids
+    that are not FFT grids: for every case the expected time of each supported method (the reference's operation
+    counts and time model) and the method it picks, taken from the reference's own classes."""
+    from hcipy.fourier.fast_fourier_transform import FastFourierTransform
+    from hcipy.fourier.matrix_fourier_transform import MatrixFourierTransform
+    from hcipy.fourier.naive_fourier_transform import NaiveFourierTransform
+    from hcipy.fourier.zoom_fast_fourier_transform import ZoomFastFourierTransform
+    methods = [('fft', FastFourierTransform), ('mft', MatrixFourierTransform), ('naive', NaiveFourierTransform),
+               ('zft', ZoomFastFourierTransform)]
+    rec = {'methods': np.array([m for m, _ in methods])}
+    cases = []
+    for dims, diam in [(16, 1.0), (32, 1.0), (64, 2.0), (100, 1.0), (128, 1.0), (256, 1.0), (512, 8.0), (1024, 8.0),
+                       (2048, 1.0), ((96, 64), (1.5, 1.0)), ((33, 47), 1.0)]:
+        for q in (1, 2, 4, 8, 16):
+            for fov in (1, 0.5, 0.25, 0.1):
+                cases.append((dims, diam, q, fov, None))
+        for q, num_airy in ((2, 8), (4, 16), (8, 32), (3.3, 12.5)):
+            cases.append((dims, diam, q, num_airy, 'focal'))
+    inputs, params, kinds, times, best = [], [], [], [], []
+    for dims, diam, q, x, kind in cases:
+        pupil = hp.make_pupil_grid(dims, diam)
+        if kind is None:
+            output_grid = hp.make_fft_grid(pupil, q, x)
+            allowed = [m for m, _ in methods]
+        else:
+            # a focal grid in angular-frequency units, as FraunhoferPropagator builds it (not an FFT grid)
+            output_grid = hp.make_focal_grid(q, x, spatial_resolution=1.0).scaled(2 * np.pi / np.max(
+                np.asarray(pupil.delta) * np.asarray(pupil.dims)))
+            allowed = [m for m, _ in methods]
+            try:
+                hp.fourier.fast_fourier_transform.get_fft_parameters(output_grid, pupil)
+            except ValueError:
+                allowed.remove('fft')
+        t = []
+        for m, cls in methods:
+            if m in allowed and cls.is_supported(pupil, output_grid):
+                t.append(cls.compute_complexity(pupil, output_grid).expected_execution_time)
+            else:
+                t.append(np.nan)
+        inputs.append(np.broadcast_to(np.asarray(dims, np.int64), (2,)))
+        params.append([np.max(np.broadcast_to(np.asarray(diam, np.float64), (2,))) if kind else 0.0, q, x,
+                       1.0 if kind else 0.0])
+        kinds.append(np.broadcast_to(np.asarray(diam, np.float64), (2,)))
+        times.append(t)
+        best.append(int(np.nanargmin(t)))
+    rec.update({'dims': np.array(inputs), 'diameter': np.array(kinds), 'params': np.array(params),
+                'times': np.array(times), 'best': np.array(best)})
+    out['planner'] = rec
+
+
 def make_pyramid_case(hp, out):
     """PyramidWavefrontSensorOptics (hcipy/wavefront_sensing/pyramid.py:94-199): forward of an aberrated pupil at
     two wavelengths (the pyramid phase depends on the refractive index and the wavenumber), backward of a random
@@ -560,7 +612,7 @@ def save(out):
 
 
 CASES = ['mft_cases', 'fraunhofer_cfg1', 'fft_cases', 'czt_cases', 'asp_cases', 'fresnel_cases', 'vortex_cases',
-         'vector_vortex_case', 'pyramid_case', 'modulated_pyramid_case', 'lyot_case', 'subpixel_cases',
+         'vector_vortex_case', 'planner_case', 'pyramid_case', 'modulated_pyramid_case', 'lyot_case', 'subpixel_cases',
          'atmosphere_case', 'dm_case', 'efc_case', 'pickle_case', 'spectral_noise_case']
 
 

@@ -158,3 +158,31 @@ def test_vector_vortex_coronagraph_sets_are_shared_and_bounded(monkeypatch):
         chromatic.get_instance_data(grid, None, 1.0 + 0.01 * k)
     assert len(chromatic._entries) == chromatic._max_in_cache == 11
     assert len(built) == 3 + 3 * 14
+
+
+def test_planner_picks_the_reference_method():
+    """make_fourier_transform(planner='estimate') ranks the methods with the reference's operation counts and time
+    model: over 264 grid pairs (pupils of 16^2-2048^2 and rectangular ones; FFT output grids with q 1-16 and fov
+    1-0.1; focal grids that are not FFT grids) every supported method's expected time equals the reference's
+    (fourier_transform.py:217-300) and the pick is the reference's (it never picks its naive DFT here)."""
+    from hcipy_gb300.fourier import _planned_methods
+    g = load_golden('planner')
+    methods = [str(m) for m in g['methods']]
+    for i in range(len(g['best'])):
+        pupil = hg.make_pupil_grid(tuple(int(d) for d in g['dims'][i]), tuple(float(d) for d in g['diameter'][i]))
+        _, q, x, focal = g['params'][i]
+        if focal:
+            out = hg.make_focal_grid(q, x, spatial_resolution=1.0).scaled(
+                2 * np.pi / np.max(np.asarray(pupil.delta) * np.asarray(pupil.dims)))
+            _, expected, _, _ = _planned_methods(pupil, out, 1, 1, 0, 'estimate')
+        else:
+            _, expected, _, _ = _planned_methods(pupil, None, q, x, 0, 'estimate')
+        for k, m in enumerate(methods):
+            ref = g['times'][i, k]
+            if m == 'naive':
+                continue
+            if np.isnan(ref):
+                assert m not in expected, (i, m)
+            else:
+                assert abs(expected[m] - ref) <= 1e-12 * ref, (i, m, expected[m], ref)
+        assert min(expected, key=expected.get) == methods[int(g['best'][i])], i
