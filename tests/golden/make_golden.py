@@ -351,6 +351,25 @@ def make_planner_case(hp, out):
     out['planner'] = rec
 
 
+def make_fft_grid_case(hp, out):
+    """FFT-grid algebra (hcipy/fourier/fast_fourier_transform.py:23-154) over square, rectangular and odd pupils with
+    q, fov and shift varied: the output grid of make_fft_grid and what get_fft_parameters recovers from it."""
+    rows = []
+    for dims, diam in [(16, 1.0), (33, 1.0), (64, 2.0), (100, 1.3), ((96, 64), (1.5, 1.0)), ((31, 48), (0.7, 1.1))]:
+        pupil = hp.make_pupil_grid(dims, diam)
+        for q in (1, 1.5, 2, 4, 8):
+            for fov in (1, 0.5, 0.3):
+                for shift in (0, 0.25, (0.5, -1.2)):
+                    g = hp.make_fft_grid(pupil, q, fov, shift)
+                    qq, ff, ss = hp.fourier.fast_fourier_transform.get_fft_parameters(g, pupil)
+                    b = lambda v: np.broadcast_to(np.asarray(v, np.float64), (2,))  # noqa: E731
+                    rows.append(np.concatenate([b(dims), b(diam), [q, fov], b(shift), b(g.delta), b(g.dims),
+                                                b(g.zero), b(qq), b(ff), b(ss)]))
+    out['fft_grids'] = {'rows': np.array(rows),
+                        'columns': np.array(['dims', 'diameter', 'q', 'fov', 'shift', 'delta', 'out_dims', 'zero',
+                                             'q_found', 'fov_found', 'shift_found'])}
+
+
 def make_pyramid_case(hp, out):
     """PyramidWavefrontSensorOptics (hcipy/wavefront_sensing/pyramid.py:94-199): forward of an aberrated pupil at
     two wavelengths (the pyramid phase depends on the refractive index and the wavenumber), backward of a random
@@ -612,7 +631,7 @@ def save(out):
 
 
 CASES = ['mft_cases', 'fraunhofer_cfg1', 'fft_cases', 'czt_cases', 'asp_cases', 'fresnel_cases', 'vortex_cases',
-         'vector_vortex_case', 'planner_case', 'pyramid_case', 'modulated_pyramid_case', 'lyot_case', 'subpixel_cases',
+         'vector_vortex_case', 'planner_case', 'fft_grid_case', 'pyramid_case', 'modulated_pyramid_case', 'lyot_case', 'subpixel_cases',
          'atmosphere_case', 'dm_case', 'efc_case', 'pickle_case', 'spectral_noise_case']
 
 

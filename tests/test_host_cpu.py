@@ -186,3 +186,21 @@ def test_planner_picks_the_reference_method():
             else:
                 assert abs(expected[m] - ref) <= 1e-12 * ref, (i, m, expected[m], ref)
         assert min(expected, key=expected.get) == methods[int(g['best'][i])], i
+
+
+def test_fft_grid_algebra_sweep():
+    """make_fft_grid and get_fft_parameters (fast_fourier_transform.py:23-154) against the reference over 270
+    cases: square, rectangular and odd pupils, q 1-8 (including 1.5), fov 1-0.3, scalar and per-axis shifts."""
+    g = load_golden('fft_grids')
+    for r in g['rows']:
+        dims, diam = tuple(int(d) for d in r[0:2]), tuple(r[2:4])
+        q, fov, shift = r[4], r[5], tuple(r[6:8])
+        pupil = hg.make_pupil_grid(dims, diam)
+        out = hg.make_fft_grid(pupil, q, fov, shift)
+        np.testing.assert_array_equal(out.dims, r[10:12])
+        np.testing.assert_allclose(out.delta, r[8:10], rtol=1e-15)
+        np.testing.assert_allclose(out.zero, r[12:14], rtol=1e-13, atol=1e-13)
+        qq, ff, ss = hg.get_fft_parameters(out, pupil)
+        np.testing.assert_allclose(np.broadcast_to(qq, (2,)), r[14:16], rtol=1e-12)
+        np.testing.assert_allclose(np.broadcast_to(ff, (2,)), r[16:18], rtol=1e-12)
+        np.testing.assert_allclose(np.broadcast_to(ss, (2,)), r[18:20], rtol=1e-12, atol=1e-12)
