@@ -370,6 +370,45 @@ def make_fft_grid_case(hp, out):
                                              'q_found', 'fov_found', 'shift_found'])}
 
 
+def make_host_functions_case(hp, out):
+    """Host helpers with the reference's outputs: make_uniform_grid (odd and even sizes, centres, has_center),
+    make_pupil_grid, make_focal_grid (spatial resolution, pupil diameter + focal length + wavelength, f-number),
+    the Cn^2 / Fried-parameter conversions and the von Karman covariance and PSD
+    (hcipy/field/util.py:68-318, hcipy/atmosphere/atmospheric_model.py:321-399)."""
+    grids = []
+
+    def row(g):
+        """ndim, then delta, dims and zero per axis, padded to two axes with NaN."""
+        vals = [np.asarray(v, np.float64).ravel() for v in (g.delta, g.dims, g.zero)]
+        pad = [np.concatenate([v, np.full(2 - len(v), np.nan)]) for v in vals]
+        return np.concatenate([[len(vals[0])]] + pad)
+
+    for dims, extent, center, has_center in [(8, 1.0, 0, False), (9, 1.0, 0, False), (9, 2.0, 0, True),
+                                             (10, 2.0, 0, True), ((6, 7), (1.0, 1.4), (0.1, -0.3), False),
+                                             ((6, 7), (1.0, 1.4), (0.1, -0.3), True)]:
+        g = hp.make_uniform_grid(dims, extent, center, has_center)
+        grids.append(row(g))
+    for dims, diam in [(64, 1.0), (65, 2.0), ((40, 30), (1.0, 0.75))]:
+        g = hp.make_pupil_grid(dims, diam)
+        grids.append(row(g))
+    for kw in [dict(q=4, num_airy=16), dict(q=3.3, num_airy=(8, 5.5)), dict(q=2, num_airy=10, spatial_resolution=0.5),
+               dict(q=4, num_airy=8, pupil_diameter=8.0, focal_length=20.0, reference_wavelength=1.6e-6),
+               dict(q=5, num_airy=6, f_number=12.0, reference_wavelength=7e-7)]:
+        g = hp.make_focal_grid(**kw)
+        grids.append(row(g))
+    r0s = np.array([0.05, 0.1, 0.15, 0.3])
+    wls = np.array([500e-9, 1.6e-6])
+    cn2 = np.array([[hp.Cn_squared_from_fried_parameter(r, wl) for r in r0s] for wl in wls])
+    back = np.array([[hp.fried_parameter_from_Cn_squared(c, wl) for c in row] for row, wl in zip(cn2, wls)])
+    fg = hp.make_pupil_grid(24, 40.0)
+    psd = np.asarray(hp.power_spectral_density_von_karman(0.12, 22.0)(fg))
+    r = np.array([0.0, 1e-3, 0.05, 0.3, 1.0, 4.0, 25.0])
+    from hcipy.atmosphere.atmospheric_model import phase_covariance_von_karman
+    cov = np.asarray(phase_covariance_von_karman(0.12, 22.0)(hp.CartesianGrid(hp.UnstructuredCoords((r, 0 * r)))))
+    out['host_functions'] = {'grids': np.array(grids), 'r0': r0s, 'wavelengths': wls, 'cn2': cn2,
+                             'r0_back': back, 'psd': psd, 'cov_r': r, 'cov': cov}
+
+
 def make_pyramid_case(hp, out):
     """PyramidWavefrontSensorOptics (hcipy/wavefront_sensing/pyramid.py:94-199): forward of an aberrated pupil at
     two wavelengths (the pyramid phase depends on the refractive index and the wavenumber), backward of a random
@@ -631,7 +670,8 @@ def save(out):
 
 
 CASES = ['mft_cases', 'fraunhofer_cfg1', 'fft_cases', 'czt_cases', 'asp_cases', 'fresnel_cases', 'vortex_cases',
-         'vector_vortex_case', 'planner_case', 'fft_grid_case', 'pyramid_case', 'modulated_pyramid_case', 'lyot_case', 'subpixel_cases',
+         'vector_vortex_case', 'planner_case', 'fft_grid_case', 'host_functions_case',
+         'pyramid_case', 'modulated_pyramid_case', 'lyot_case', 'subpixel_cases',
          'atmosphere_case', 'dm_case', 'efc_case', 'pickle_case', 'spectral_noise_case']
 
 

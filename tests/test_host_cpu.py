@@ -204,3 +204,36 @@ def test_fft_grid_algebra_sweep():
         np.testing.assert_allclose(np.broadcast_to(qq, (2,)), r[14:16], rtol=1e-12)
         np.testing.assert_allclose(np.broadcast_to(ff, (2,)), r[16:18], rtol=1e-12)
         np.testing.assert_allclose(np.broadcast_to(ss, (2,)), r[18:20], rtol=1e-12, atol=1e-12)
+
+
+def test_grid_factories_and_turbulence_helpers_match_reference():
+    """make_uniform_grid / make_pupil_grid / make_focal_grid over odd and even sizes, centres, has_center and every
+    way of giving the focal sampling (hcipy/field/util.py:68-318); the Cn^2 <-> Fried-parameter conversions, the
+    von Karman PSD and phase covariance (hcipy/atmosphere/atmospheric_model.py:321-399)."""
+    from hcipy_gb300.atmosphere import von_karman_covariance
+    g = load_golden('host_functions')
+    grids = []
+    for dims, extent, center, has_center in [(8, 1.0, 0, False), (9, 1.0, 0, False), (9, 2.0, 0, True),
+                                             (10, 2.0, 0, True), ((6, 7), (1.0, 1.4), (0.1, -0.3), False),
+                                             ((6, 7), (1.0, 1.4), (0.1, -0.3), True)]:
+        grids.append(hg.make_uniform_grid(dims, extent, center, has_center))
+    for dims, diam in [(64, 1.0), (65, 2.0), ((40, 30), (1.0, 0.75))]:
+        grids.append(hg.make_pupil_grid(dims, diam))
+    for kw in [dict(q=4, num_airy=16), dict(q=3.3, num_airy=(8, 5.5)), dict(q=2, num_airy=10, spatial_resolution=0.5),
+               dict(q=4, num_airy=8, pupil_diameter=8.0, focal_length=20.0, reference_wavelength=1.6e-6),
+               dict(q=5, num_airy=6, f_number=12.0, reference_wavelength=7e-7)]:
+        grids.append(hg.make_focal_grid(**kw))
+    assert len(grids) == len(g['grids'])
+    for grid, ref in zip(grids, g['grids']):
+        n = int(ref[0])
+        assert grid.ndim == n
+        np.testing.assert_allclose(grid.delta, ref[1:1 + n], rtol=1e-15)
+        np.testing.assert_array_equal(grid.dims, ref[3:3 + n])
+        np.testing.assert_allclose(grid.zero, ref[5:5 + n], rtol=1e-14, atol=1e-16)
+    for row, back, wl in zip(g['cn2'], g['r0_back'], g['wavelengths']):
+        for r0, c, rb in zip(g['r0'], row, back):
+            assert hg.Cn_squared_from_fried_parameter(r0, wl) == pytest.approx(c, rel=1e-14)
+            assert hg.fried_parameter_from_Cn_squared(c, wl) == pytest.approx(rb, rel=1e-14)
+    psd = hg.power_spectral_density_von_karman(0.12, 22.0)(hg.make_pupil_grid(24, 40.0))
+    np.testing.assert_allclose(np.asarray(psd), g['psd'], rtol=1e-13)
+    np.testing.assert_allclose(von_karman_covariance(g['cov_r'], 0.12, 22.0), g['cov'], rtol=1e-12)
