@@ -409,6 +409,28 @@ def make_host_functions_case(hp, out):
                              'r0_back': back, 'psd': psd, 'cov_r': r, 'cov': cov}
 
 
+def make_influence_sweep_case(hp, out):
+    """Gaussian influence functions (hcipy/optics/deformable_mirror.py:43-93) beyond the default: other crosstalk
+    and cutoff values, x/y/z tilts of the mirror and oversampled evaluation, on a 24^2 pupil with 5 x 5
+    actuators; each basis stored as its CSR arrays."""
+    pupil = hp.make_pupil_grid(24, 1.0)
+    rec = {}
+    cases = [dict(crosstalk=0.15, cutoff=3), dict(crosstalk=0.3, cutoff=2), dict(crosstalk=0.15, cutoff=3, x_tilt=0.1),
+             dict(crosstalk=0.15, cutoff=3, y_tilt=0.2, z_tilt=0.3), dict(crosstalk=0.2, cutoff=2.5, oversampling=2),
+             dict(crosstalk=0.15, cutoff=3, z_tilt=0.25, oversampling=3)]
+    for i, kw in enumerate(cases):
+        basis = hp.make_gaussian_influence_functions(pupil, 5, 1 / 5, **kw)
+        import scipy.sparse
+        m = scipy.sparse.csr_matrix(basis.transformation_matrix)
+        m.sort_indices()
+        rec['data_%d' % i], rec['indices_%d' % i], rec['indptr_%d' % i] = m.data, m.indices, m.indptr
+        rec['shape_%d' % i] = np.array(m.shape)
+        for k in ('crosstalk', 'cutoff', 'x_tilt', 'y_tilt', 'z_tilt', 'oversampling'):
+            rec['%s_%d' % (k, i)] = np.float64(kw.get(k, {'oversampling': 1}.get(k, 0.0)))
+    rec['count'] = np.int64(len(cases))
+    out['influence_sweep'] = rec
+
+
 def make_pyramid_case(hp, out):
     """PyramidWavefrontSensorOptics (hcipy/wavefront_sensing/pyramid.py:94-199): forward of an aberrated pupil at
     two wavelengths (the pyramid phase depends on the refractive index and the wavenumber), backward of a random
@@ -671,6 +693,7 @@ def save(out):
 
 CASES = ['mft_cases', 'fraunhofer_cfg1', 'fft_cases', 'czt_cases', 'asp_cases', 'fresnel_cases', 'vortex_cases',
          'vector_vortex_case', 'planner_case', 'fft_grid_case', 'host_functions_case',
+         'influence_sweep_case',
          'pyramid_case', 'modulated_pyramid_case', 'lyot_case', 'subpixel_cases',
          'atmosphere_case', 'dm_case', 'efc_case', 'pickle_case', 'spectral_noise_case']
 

@@ -242,3 +242,21 @@ def test_vector_vortex_jones_entries():
         got = np.array([[j11[k], j12[k]], [j12[k], j22[k]]])
         assert np.allclose(got, ref, rtol=0, atol=1e-15)
         assert np.allclose(got @ got.conj().T, np.eye(2), rtol=0, atol=1e-15)
+
+
+def test_gaussian_influence_functions_sweep():
+    """Gaussian influence functions with other crosstalk and cutoff values, x/y/z-tilted mirrors and oversampled
+    evaluation (deformable_mirror.py:43-93) against the reference: the same nonzero pattern and values within
+    1e-15 (the reference evaluates the tilted and oversampled grids in another order)."""
+    import scipy.sparse
+    import hcipy_gb300 as hg
+    g = load_golden('influence_sweep')
+    pupil = hg.make_pupil_grid(24, 1.0)
+    for i in range(int(g['count'])):
+        kw = {k: float(g['%s_%d' % (k, i)]) for k in ('crosstalk', 'cutoff', 'x_tilt', 'y_tilt', 'z_tilt')}
+        kw['oversampling'] = int(g['oversampling_%d' % i])
+        ref = scipy.sparse.csr_matrix((g['data_%d' % i], g['indices_%d' % i], g['indptr_%d' % i]),
+                                      shape=tuple(g['shape_%d' % i])).toarray()
+        mine = hg.make_gaussian_influence_functions(pupil, 5, 1 / 5, **kw).transformation_matrix.toarray()
+        assert np.array_equal(mine != 0, ref != 0), i
+        assert np.max(np.abs(mine - ref)) < 1e-15, (i, kw)
