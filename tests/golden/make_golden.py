@@ -431,6 +431,26 @@ def make_influence_sweep_case(hp, out):
     out['influence_sweep'] = rec
 
 
+def make_atmosphere_matrices_case(hp, out):
+    """InfiniteAtmosphericLayer's stencils and autoregressive matrices (infinite_atmospheric_layer.py:111-202) for
+    a rectangular grid, a longer stencil and another outer scale and seed."""
+    rec = {}
+    for i, (dims, diam, stencil_length, L0, seed) in enumerate([((20, 14), (1.0, 0.7), 2, 25.0, 11),  # noqa: N806
+                                                                (16, 2.0, 3, 8.0, 12)]):
+        pupil = hp.make_pupil_grid(dims, diam)
+        layer = hp.InfiniteAtmosphericLayer(pupil, hp.Cn_squared_from_fried_parameter(0.2, 500e-9), L0=L0,
+                                            stencil_length=stencil_length, seed=seed)
+        rec.update({'A_vertical_%d' % i: layer.A_vertical, 'B_vertical_%d' % i: layer.B_vertical,
+                    'A_horizontal_%d' % i: layer.A_horizontal, 'B_horizontal_%d' % i: layer.B_horizontal,
+                    'stencil_bottom_%d' % i: layer.stencil_bottom_idx.astype(np.int64),
+                    'stencil_left_%d' % i: layer.stencil_left_idx.astype(np.int64),
+                    'dims_%d' % i: np.asarray(pupil.dims, np.int64), 'delta_%d' % i: np.asarray(pupil.delta),
+                    'zero_%d' % i: np.asarray(pupil.zero), 'stencil_length_%d' % i: np.int64(stencil_length),
+                    'L0_%d' % i: np.float64(L0), 'seed_%d' % i: np.int64(seed)})
+    rec['count'] = np.int64(2)
+    out['atmosphere_matrices'] = rec
+
+
 def make_pyramid_case(hp, out):
     """PyramidWavefrontSensorOptics (hcipy/wavefront_sensing/pyramid.py:94-199): forward of an aberrated pupil at
     two wavelengths (the pyramid phase depends on the refractive index and the wavenumber), backward of a random
@@ -693,7 +713,7 @@ def save(out):
 
 CASES = ['mft_cases', 'fraunhofer_cfg1', 'fft_cases', 'czt_cases', 'asp_cases', 'fresnel_cases', 'vortex_cases',
          'vector_vortex_case', 'planner_case', 'fft_grid_case', 'host_functions_case',
-         'influence_sweep_case',
+         'influence_sweep_case', 'atmosphere_matrices_case',
          'pyramid_case', 'modulated_pyramid_case', 'lyot_case', 'subpixel_cases',
          'atmosphere_case', 'dm_case', 'efc_case', 'pickle_case', 'spectral_noise_case']
 

@@ -260,3 +260,23 @@ def test_gaussian_influence_functions_sweep():
         mine = hg.make_gaussian_influence_functions(pupil, 5, 1 / 5, **kw).transformation_matrix.toarray()
         assert np.array_equal(mine != 0, ref != 0), i
         assert np.max(np.abs(mine - ref)) < 1e-15, (i, kw)
+
+
+def test_atmosphere_matrices_for_other_layers():
+    """Stencils and autoregressive matrices (infinite_atmospheric_layer.py:111-202) of a rectangular grid and of a
+    longer stencil with another outer scale against the reference: the same stencil draws, A within 1e-12, and
+    B B^T within 1e-12 (B is defined up to the signs of its singular vectors)."""
+    from hcipy_gb300 import atmosphere as at
+    from hcipy_gb300.field import CartesianGrid, RegularCoords
+    g = load_golden('atmosphere_matrices')
+    for i in range(int(g['count'])):
+        grid = CartesianGrid(RegularCoords(g['delta_%d' % i], g['dims_%d' % i], g['zero_%d' % i]))
+        nx, ny = (int(d) for d in g['dims_%d' % i])
+        bottom, left = at.make_stencils(nx, ny, int(g['stencil_length_%d' % i]),
+                                        np.random.default_rng(int(g['seed_%d' % i])))
+        assert np.array_equal(bottom, g['stencil_bottom_%d' % i]) and np.array_equal(left, g['stencil_left_%d' % i])
+        for where, stencil, key in (('bottom', bottom, 'vertical'), ('left', left, 'horizontal')):
+            a, b = at.ar_matrices(grid, stencil, where, float(g['L0_%d' % i]))
+            assert rel_err(a, g['A_%s_%d' % (key, i)]) < 1e-12, (i, key)
+            ref_b = g['B_%s_%d' % (key, i)]
+            assert rel_err(b @ b.T, ref_b @ ref_b.T) < 1e-12, (i, key)
