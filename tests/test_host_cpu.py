@@ -237,3 +237,17 @@ def test_grid_factories_and_turbulence_helpers_match_reference():
     psd = hg.power_spectral_density_von_karman(0.12, 22.0)(hg.make_pupil_grid(24, 40.0))
     np.testing.assert_allclose(np.asarray(psd), g['psd'], rtol=1e-13)
     np.testing.assert_allclose(von_karman_covariance(g['cov_r'], 0.12, 22.0), g['cov'], rtol=1e-12)
+
+
+def test_diffraction_scaled_focal_grids():
+    """The broadband workload's per-wavelength focal grids: q = 4 everywhere, the radius num_airy lambda0/lambda,
+    so 21 wavelengths over 0.9-1.1 lambda0 give uneven sizes from 284^2 down to 232^2 (1,386,546 pixels)."""
+    wls = np.linspace(0.9, 1.1, 21)
+    grids = hg.diffraction_scaled_focal_grids(4, 32, wls, 1.0)
+    sizes = [int(g.dims[0]) for g in grids]
+    assert sizes[0] == 284 and sizes[-1] == 232 and sizes == sorted(sizes, reverse=True)
+    assert all(int(g.dims[0]) == int(g.dims[1]) for g in grids)
+    assert sum(g.size for g in grids) == 1386546
+    for g, wl in zip(grids, wls):
+        np.testing.assert_allclose(g.delta, 0.25, rtol=0)
+        assert int(g.dims[0]) == int(2 * 4 * 32 / wl)
