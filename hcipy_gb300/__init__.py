@@ -8,8 +8,8 @@ from .field import (Field, CartesianGrid, RegularCoords, SeparatedCoords, Unstru
                     make_pupil_grid, make_focal_grid, make_focal_grid_from_pupil_grid)
 from .fourier import (FourierTransform, ComputationalComplexity, MatrixFourierTransform, make_fourier_transform,
                       make_fft_grid, get_fft_parameters, is_fft_grid)
-from .optics import (Wavefront, OpticalElement, AgnosticOpticalElement, Apodizer, PhaseApodizer, SurfaceApodizer,
-                     make_agnostic_forward, make_agnostic_backward)
+from .optics import (Wavefront, OpticalElement, AgnosticOpticalElement, EmptyOpticalElement, OpticalSystem,
+                     Apodizer, PhaseApodizer, SurfaceApodizer, make_agnostic_forward, make_agnostic_backward)
 from .propagation import FraunhoferPropagator, AngularSpectrumPropagator, FresnelPropagator
 from .fft import FastFourierTransform, ChirpZTransform, ZoomFastFourierTransform, FourierFilter
 from .wavefront_sensing import PyramidWavefrontSensorOptics, ModulatedPyramidWavefrontSensorOptics
@@ -32,7 +32,8 @@ __all__ = [
     'make_pupil_grid', 'make_focal_grid', 'make_focal_grid_from_pupil_grid',
     'FourierTransform', 'ComputationalComplexity', 'MatrixFourierTransform', 'make_fourier_transform',
     'make_fft_grid', 'get_fft_parameters', 'is_fft_grid',
-    'Wavefront', 'OpticalElement', 'AgnosticOpticalElement', 'Apodizer', 'PhaseApodizer',
+    'Wavefront', 'OpticalElement', 'AgnosticOpticalElement', 'EmptyOpticalElement', 'OpticalSystem', 'Apodizer',
+    'PhaseApodizer',
     'make_agnostic_forward', 'make_agnostic_backward',
     'FraunhoferPropagator', 'AngularSpectrumPropagator', 'FresnelPropagator', 'LyotCoronagraph',
     'MultiScaleCoronagraph', 'VortexCoronagraph', 'VectorVortexCoronagraph', 'PyramidWavefrontSensorOptics',

@@ -209,6 +209,45 @@ class OpticalElement(object):
         raise NotImplementedError()
 
 
+class EmptyOpticalElement(OpticalElement):
+    """An element that leaves the wavefront unchanged, to stand in for an optional element
+    (hcipy/optics/optical_element.py:153-218)."""
+
+    def forward(self, wavefront):
+        return wavefront
+
+    def backward(self, wavefront):
+        return wavefront
+
+
+class OpticalSystem(OpticalElement):
+    """A linear path of optical elements (hcipy/optics/optical_element.py:848-950): ``forward`` applies them in
+    order, ``backward`` applies their backward propagations in reverse order."""
+
+    def __init__(self, optical_elements):
+        self.optical_elements = optical_elements
+
+    @property
+    def optical_elements(self):
+        return self._optical_elements
+
+    @optical_elements.setter
+    def optical_elements(self, optical_elements):
+        self._optical_elements = list(optical_elements)
+
+    def forward(self, wavefront):
+        wf = wavefront
+        for element in self._optical_elements:
+            wf = element.forward(wf)
+        return wf
+
+    def backward(self, wavefront):
+        wf = wavefront
+        for element in reversed(self._optical_elements):
+            wf = element.backward(wf)
+        return wf
+
+
 class InstanceData(object):
     def __init__(self, input_grid, output_grid, wavelength):
         self.input_grid = input_grid

@@ -251,3 +251,30 @@ def test_diffraction_scaled_focal_grids():
     for g, wl in zip(grids, wls):
         np.testing.assert_allclose(g.delta, 0.25, rtol=0)
         assert int(g.dims[0]) == int(2 * 4 * 32 / wl)
+
+
+def test_optical_system_and_empty_element():
+    """OpticalSystem (optical_element.py:848-950) applies its elements' forwards in order and their backwards in
+    reverse order; EmptyOpticalElement (:153-218) returns the wavefront it is given.  Host logic: the elements
+    here record the calls."""
+    calls = []
+
+    class Step(hg.OpticalElement):
+        def __init__(self, name):
+            self.name = name
+
+        def forward(self, wf):
+            calls.append(('f', self.name))
+            return wf + [self.name]
+
+        def backward(self, wf):
+            calls.append(('b', self.name))
+            return wf + [self.name.upper()]
+
+    system = hg.OpticalSystem((Step('a'), hg.EmptyOpticalElement(), Step('b')))
+    assert isinstance(system.optical_elements, list) and len(system.optical_elements) == 3
+    assert system.forward([]) == ['a', 'b'] and system([]) == ['a', 'b']
+    assert system.backward([]) == ['B', 'A']
+    assert calls == [('f', 'a'), ('f', 'b'), ('f', 'a'), ('f', 'b'), ('b', 'b'), ('b', 'a')]
+    token = object()
+    assert hg.EmptyOpticalElement().forward(token) is token and hg.EmptyOpticalElement().backward(token) is token
