@@ -373,6 +373,7 @@ def make_fft_grid_case(hp, out):
 def make_host_functions_case(hp, out):
     """Host helpers with the reference's outputs: make_uniform_grid (odd and even sizes, centres, has_center),
     make_pupil_grid, make_focal_grid (spatial resolution, pupil diameter + focal length + wavelength, f-number),
+    make_focal_grid_from_pupil_grid,
     the Cn^2 / Fried-parameter conversions and the von Karman covariance and PSD
     (hcipy/field/util.py:68-318, hcipy/atmosphere/atmospheric_model.py:321-399)."""
     grids = []
@@ -396,6 +397,10 @@ def make_host_functions_case(hp, out):
                dict(q=5, num_airy=6, f_number=12.0, reference_wavelength=7e-7)]:
         g = hp.make_focal_grid(**kw)
         grids.append(row(g))
+    for dims, diam, kw in [(64, 1.0, dict(q=4, num_airy=16)),
+                           ((40, 30), (1.0, 0.75), dict(q=3, num_airy=(8, 6), focal_length=2.0, wavelength=0.5)),
+                           (33, 2.0, dict(q=2))]:
+        grids.append(row(hp.make_focal_grid_from_pupil_grid(hp.make_pupil_grid(dims, diam), **kw)))
     r0s = np.array([0.05, 0.1, 0.15, 0.3])
     wls = np.array([500e-9, 1.6e-6])
     cn2 = np.array([[hp.Cn_squared_from_fried_parameter(r, wl) for r in r0s] for wl in wls])

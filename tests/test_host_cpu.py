@@ -207,8 +207,8 @@ def test_fft_grid_algebra_sweep():
 
 
 def test_grid_factories_and_turbulence_helpers_match_reference():
-    """make_uniform_grid / make_pupil_grid / make_focal_grid over odd and even sizes, centres, has_center and every
-    way of giving the focal sampling (hcipy/field/util.py:68-318); the Cn^2 <-> Fried-parameter conversions, the
+    """make_uniform_grid / make_pupil_grid / make_focal_grid / make_focal_grid_from_pupil_grid over odd and even
+    sizes, centres, has_center and every way of giving the focal sampling (hcipy/field/util.py:68-318); the Cn^2 <-> Fried-parameter conversions, the
     von Karman PSD and phase covariance (hcipy/atmosphere/atmospheric_model.py:321-399)."""
     from hcipy_gb300.atmosphere import von_karman_covariance
     g = load_golden('host_functions')
@@ -223,6 +223,10 @@ def test_grid_factories_and_turbulence_helpers_match_reference():
                dict(q=4, num_airy=8, pupil_diameter=8.0, focal_length=20.0, reference_wavelength=1.6e-6),
                dict(q=5, num_airy=6, f_number=12.0, reference_wavelength=7e-7)]:
         grids.append(hg.make_focal_grid(**kw))
+    for dims, diam, kw in [(64, 1.0, dict(q=4, num_airy=16)),
+                           ((40, 30), (1.0, 0.75), dict(q=3, num_airy=(8, 6), focal_length=2.0, wavelength=0.5)),
+                           (33, 2.0, dict(q=2))]:
+        grids.append(hg.make_focal_grid_from_pupil_grid(hg.make_pupil_grid(dims, diam), **kw))
     assert len(grids) == len(g['grids'])
     for grid, ref in zip(grids, g['grids']):
         n = int(ref[0])
